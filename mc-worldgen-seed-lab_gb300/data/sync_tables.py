@@ -1,0 +1,24 @@
+"""Copy the seed-independent game tables that a world is built from into this package's data root.
+
+``mcgen_open(root, version)`` reads ``<root>/data/climate-<V>.txt`` (noise parameters, presets, depth
+gradient, ridges-folded constants, offset spline) and ``<root>/data/params/<V>/{overworld,nether}.tsv``
+(the multi-noise biome parameter lists), the same layout the reference engine loads
+(engine/mc_data.h:84-183).  The tables are game data extracted from Minecraft by the reference
+project; they are copied verbatim so the library can run where the reference tree is absent.
+
+Usage (build container only):  python mc-worldgen-seed-lab_gb300/data/sync_tables.py
+"""
+import os
+import shutil
+
+SRC = "/root/reference/data"
+DST = os.path.dirname(os.path.abspath(__file__))
+VERSIONS = ["26.1", "26.2", "26.3", "26.4-snapshot-2"]
+
+if __name__ == "__main__":
+    for v in VERSIONS:
+        shutil.copyfile(os.path.join(SRC, f"climate-{v}.txt"), os.path.join(DST, f"climate-{v}.txt"))
+        os.makedirs(os.path.join(DST, "params", v), exist_ok=True)
+        for f in ("overworld.tsv", "nether.tsv"):
+            shutil.copyfile(os.path.join(SRC, "params", v, f), os.path.join(DST, "params", v, f))
+    print("tables copied to", DST)
