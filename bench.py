@@ -1,0 +1,391 @@
+#!/usr/bin/env python3
+"""Benchmark of the bit-exact biome path on GB300 (one JSON line on rank 0).
+
+Workloads (synthetic inputs with the shapes of the published configurations):
+  seeds8   (default) Overworld 26.3, 65,536 SplitMix64(1) world seeds x the same 8 points
+           (x, z uniform in [-10000, 10000] blocks, y uniform in [-64, 320]; quart cells = block >> 2):
+           per-seed noise setup + climate + R-tree, ENGINE tie rule.  [65536, 8] biome ids.
+  grid256  Overworld 26.3, seed 12345, mcgen_biome_grid 256 x 256 cells, x,z in [-512, 512) step 4,
+           y = 64 (BiomeManager zoom + chunk-cell ties).  65,536 samples per step.
+
+A step is one pass of the workload.  `value` times steps with inputs resident in HBM through the
+device-pointer entry points; `e2e` times the same work through the host-buffer C ABI calls
+(mcgen_gb300_seed_points / mcgen_biome_grid) with pinned host buffers, copies included.
+--impl reference times the reference algorithm on the host's cores (the CPU oracle, which is the
+reference engine's CPU path restated; the reference's own build needs its source tree, which this host
+does not have) on a bounded sample of the same workload.
+
+Multi-GPU: replicas only (the path has no exchange step); each rank runs the full workload and
+`value` = all ranks' samples / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+if REPO not in sys.path:
+    sys.path.insert(0, REPO)
+
+METRIC = "bit-exact biome samples/sec"
+UNIT = "samples/s"
+GOLDEN = 0x9E3779B97F4A7C15
+
+
+def splitmix64(state: int, n: int) -> np.ndarray:
+    """n outputs of SplitMix64 from `state` (z += golden; Stafford-13 mix), as uint64."""
+    with np.errstate(over="ignore"):
+        z = (np.uint64(state) + np.arange(1, n + 1, dtype=np.uint64) * np.uint64(GOLDEN)).astype(np.uint64)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def config2_inputs(n_seeds: int = 65536):
+    """65,536 SplitMix64(1) seeds and 8 points from SplitMix64(101): x,z = -10000 + r % 20001,
+    y = -64 + r % 385 (blocks), quart cell = block >> 2."""
+    seeds = splitmix64(1, n_seeds).view(np.int64)
+    r = splitmix64(101, 24).astype(np.uint64)
+    x = -10000 + (r[0:8] % np.uint64(20001)).astype(np.int64)
+    y = -64 + (r[8:16] % np.uint64(385)).astype(np.int64)
+    z = -10000 + (r[16:24] % np.uint64(20001)).astype(np.int64)
+    pts = np.stack([x >> 2, y >> 2, z >> 2], 1).astype(np.int32)
+    return seeds, pts
+
+
+# ------------------------------------------------------------------------------------------ helpers
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle samples every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.t:
+                self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [s.strip() for s in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = max(mx, float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def gpu_peaks(mg) -> dict:
+    """Measured pipe rates (Gop/s) on this device; the host file gives only HBM and bf16 GEMM."""
+    return {k: round(mg.pipe_rate(k), 1) for k in ("fp32_fma", "fp64_fma", "fp64_add", "int32_mad",
+                                                   "cvt_f64_floor_s32", "cvt_s32_f64", "cvt_f64_f32", "int64_mad")}
+
+
+# Algorithmic work per launch of each kernel (what the reference algorithm must do, counted from its
+# source): (work units per launch, unit name, pipe peak key).
+def kernel_work(kernel: str, seeds8: bool, ns: int, np_: int, ntables: int) -> tuple[float, str, str] | None:
+    if kernel == "k_setup_xo":
+        # 256 Fisher-Yates steps per lattice, each one Xoroshiro128++ draw (9 64-bit ALU ops = 18 32-bit ops),
+        # a 32x32->64 multiply and compare (3 ops) and a swap (2 loads + 2 stores): 25 int32-pipe ops; plus
+        # 3 nextDouble draws (3 x 18 + 3 conversions) per lattice.
+        ops = ns * ntables * (256 * 25 + 3 * 21)
+        return ops, "Gop/s", "int32_mad"
+    return None
+
+
+def run_gb300(args, rank, world, local_rank):
+    import torch
+
+    import __graft_entry__ as ge
+
+    mg = ge.package()
+    mg.load()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    gen = mg.Generator.open(ge.data_root(), "26.3")
+    if args.workload == "seeds8":
+        seeds, pts = config2_inputs()
+        w = gen.world("minecraft:overworld", "normal", 0)
+        samples = seeds.size * len(pts)
+        d_seeds = torch.from_numpy(seeds).to(dev)
+        d_pts = torch.from_numpy(pts).to(dev)
+        d_out = torch.empty(samples, dtype=torch.uint8, device=dev)
+        h_seeds = torch.from_numpy(seeds).pin_memory()
+        h_pts = torch.from_numpy(pts).pin_memory()
+        h_out = torch.empty(samples, dtype=torch.uint8).pin_memory()
+        nt = 46
+
+        def dev_step(stream):
+            w.seed_points_dev(d_seeds.data_ptr(), seeds.size, d_pts.data_ptr(), len(pts), d_out.data_ptr(), 0, stream)
+
+        def host_step():
+            L = mg.load()
+            rc = L.mcgen_gb300_seed_points(w.handle, h_seeds.data_ptr(), seeds.size, h_pts.data_ptr(), len(pts),
+                                           h_out.data_ptr(), None)
+            if rc:
+                raise mg.McError(rc, "seed_points failed")
+
+        h2d = seeds.nbytes + pts.nbytes
+        d2h = samples
+        config = {"workload": "Overworld 26.3 normal, 65536 SplitMix64(1) seeds x 8 fixed points "
+                              "(x,z in [-10000,10000], y in [-64,320]), ENGINE tie rule",
+                  "seeds": int(seeds.size), "points_per_seed": int(len(pts)), "version": "26.3",
+                  "dimension": "overworld", "l2": "working set > L2 (65536 x 46 lattices = 965 MB per step)"}
+    else:
+        w = gen.world("minecraft:overworld", "normal", 12345)
+        nx = nz = 256
+        samples = nx * nz
+        d_out = torch.empty(samples, dtype=torch.uint8, device=dev)
+        h_out = torch.empty(samples, dtype=torch.uint8).pin_memory()
+        nt = 46
+        seeds = np.array([12345])
+        pts = np.zeros((1, 3))
+
+        def dev_step(stream):
+            w.biome_grid_dev(-512, -512, nx, nz, 4, 64, d_out.data_ptr(), stream)
+
+        def host_step():
+            rc = mg.load().mcgen_biome_grid(w.handle, -512, -512, nx, nz, 4, 64, h_out.data_ptr())
+            if rc:
+                raise mg.McError(rc, "biome_grid failed")
+
+        h2d, d2h = 0, samples
+        config = {"workload": "Overworld 26.3 normal, seed 12345, mcgen_biome_grid 256x256 x,z in [-512,512) "
+                              "step 4, y=64 (zoom + chunk-cell ties)", "version": "26.3", "dimension": "overworld",
+                  "l2": "L2 flushed between steps (256 MB write)"}
+
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev) if args.workload == "grid256" else None
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        dev_step(sh)
+    torch.cuda.synchronize(dev)
+    launches0 = mg.launch_count()
+    mg.profile(True)
+    barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local_rank) as clk:
+        if flush is None:
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            for _ in range(args.steps):
+                dev_step(sh)
+            ev1.record(stream)
+            torch.cuda.synchronize(dev)
+            ms = ev0.elapsed_time(ev1)
+        else:
+            ms = 0.0
+            for _ in range(args.steps):
+                flush.fill_(1)
+                ev0 = torch.cuda.Event(enable_timing=True)
+                ev1 = torch.cuda.Event(enable_timing=True)
+                ev0.record(stream)
+                dev_step(sh)
+                ev1.record(stream)
+                torch.cuda.synchronize(dev)
+                ms += ev0.elapsed_time(ev1)
+    barrier()
+    mg.profile(False)
+    prof = mg.profile_read()
+    launches = mg.launch_count() - launches0
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = samples * args.steps * world / (ms_max * 1e-3)
+
+    # end to end through the host-buffer C ABI (pinned host memory, copies inside the timed region)
+    for _ in range(max(1, args.warmup)):
+        host_step()
+    barrier()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        host_step()
+    torch.cuda.synchronize(dev)
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
+    e2e = samples * args.steps * world / float(te.item())
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32+f64+int64", "data": "synthetic (SplitMix64 seeds and points)",
+           "config": dict(config, parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+           "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+           "gpu_launches": int(launches)}
+    if rank == 0:
+        kern = {k: {"ms_total": round(v[0], 4), "launches": v[1], "avg_ms": round(v[0] / v[1], 5)} for k, v in prof.items()}
+        out["kernels"] = kern
+        clocks = clk.summary()
+        if clocks:
+            out["clocks"] = clocks
+        peaks = gpu_peaks(mg)
+        out["pipe_peaks_gops"] = peaks
+        if prof:
+            top = max(prof, key=lambda k: prof[k][0])
+            wk = kernel_work(top, args.workload == "seeds8", int(seeds.size), int(len(pts)), nt)
+            avg_s = prof[top][0] / prof[top][1] * 1e-3
+            if wk:
+                ops, unit, peak_key = wk
+                achieved = ops / avg_s / 1e9
+                out["roofline"] = {"kernel": top, "bound": peak_key, "achieved": round(achieved, 1),
+                                   "peak": peaks[peak_key], "unit": unit, "frac": round(achieved / peaks[peak_key], 4),
+                                   "traffic": None, "peak_source": "measured in-run (pipe microbenchmark)"}
+            else:
+                out["roofline"] = {"kernel": top, "bound": None, "achieved": None, "peak": None, "unit": None,
+                                   "frac": None, "traffic": None}
+        out["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_sample_s)
+        print(json.dumps(out), flush=True)
+
+
+def cpu_baseline(workload: str, budget_s: float) -> dict:
+    """The reference algorithm on this host's cores (CPU oracle, OpenMP over seeds or rows)."""
+    import __graft_entry__ as ge
+    from oracle import oracle as O
+
+    cores = os.cpu_count() or 1
+    w = O.World(ge.data_root(), "26.3", "overworld")
+    if workload == "seeds8":
+        seeds, pts = config2_inputs()
+        n = 256
+        while True:  # grow the sample until it takes a meaningful share of the budget
+            t0 = time.perf_counter()
+            w.points(seeds[:n], pts, threads=cores)
+            dt = time.perf_counter() - t0
+            if dt > budget_s / 4 or n >= seeds.size:
+                break
+            n = min(seeds.size, n * 4)
+        return {"value": n * len(pts) / dt, "unit": UNIT, "cores": cores, "kind": "port",
+                "sample": f"first {n} of the 65536 seeds x 8 points ({dt:.2f} s)"}
+    t0 = time.perf_counter()
+    rows = 64
+    w.biome_grid(12345, -512, -512, 256, rows, 4, 64, threads=cores)
+    dt = time.perf_counter() - t0
+    return {"value": 256 * rows / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{rows} of the 256 grid rows ({dt:.2f} s), rows over threads"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import __graft_entry__ as ge
+    from oracle import oracle as O
+
+    cores = os.cpu_count() or 1
+    w = O.World(ge.data_root(), "26.3", "overworld")
+    if args.workload == "seeds8":
+        seeds, pts = config2_inputs()
+        n = 4096
+        per_step = lambda: w.points(seeds[:n], pts, threads=cores)  # noqa: E731
+        samples = n * len(pts)
+        sample = f"first {n} of the 65536 seeds x 8 points per step"
+        config = {"workload": "Overworld 26.3 normal, 65536 SplitMix64(1) seeds x 8 fixed points, ENGINE tie rule",
+                  "version": "26.3", "dimension": "overworld"}
+    else:
+        rows = 32
+        per_step = lambda: w.biome_grid(12345, -512, -512, 256, rows, 4, 64, threads=cores)  # noqa: E731
+        samples = 256 * rows
+        sample = f"{rows} of 256 grid rows per step"
+        config = {"workload": "Overworld 26.3 normal, seed 12345, biome grid 256x256 step 4 y=64",
+                  "version": "26.3", "dimension": "overworld"}
+    for _ in range(args.warmup):
+        per_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        per_step()
+    dt = time.perf_counter() - t0
+    value = samples * args.steps / dt
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32+f64+int64", "data": "synthetic (SplitMix64 seeds and points)",
+           "config": config,
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=["seeds8", "grid256"], default="seeds8")
+    ap.add_argument("--cpu-sample-s", type=float, default=12.0)
+    args = ap.parse_args()
+    rank, world, local_rank = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    try:
+        run_gb300(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch
+
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

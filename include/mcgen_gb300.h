@@ -1,0 +1,76 @@
+/* mcgen_gb300.h -- additions to the libmcgen ABI (include/mcgen.h) for the GB300 biome engine.
+ *
+ * New symbols only; nothing in mcgen.h changes meaning.  They expose the forms the reference serves
+ * through other entry points:
+ *  - many seeds x fixed quart points, ENGINE tie rule: the reference engine's batch API
+ *    (crack/src/gpu_biomes/gpu_biomes.h:22-57 gb_points_gpu; CPU twin engine/cuda/mcg_host.c:36-83
+ *    mcg_ref_points);
+ *  - quart-resolution grids with an explicit tie rule: the reference's golden grids
+ *    (oracle/src/common/oracle/ClimateApi.java:35-58, GRID_CHAIN) and the engine's point queries
+ *    (engine/mc_biomes.h:58-62, ENGINE);
+ *  - device-pointer variants of the above and of mcgen_biome_grid, taking a cudaStream_t as void*, for
+ *    callers whose inputs already live in GPU memory.
+ *
+ * Tie rules (about 0.04% of Overworld cells have two R-tree leaves at equal fitness):
+ *   MCGEN_TIE_ENGINE     first minimum leaf in tree order (search without a candidate);
+ *   MCGEN_TIE_GRID_CHAIN candidate = leaf of the previous cell, row-major (iz outer);
+ *   MCGEN_TIE_CHUNK_CELL candidate chain along the chunk's fill order (what mcgen_biome_grid uses).
+ */
+#ifndef MCGEN_GB300_H
+#define MCGEN_GB300_H
+#include "mcgen.h"
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { MCGEN_TIE_ENGINE = 0, MCGEN_TIE_GRID_CHAIN = 1, MCGEN_TIE_CHUNK_CELL = 2 };
+
+/* Version / dimension / preset / seed of a world (McWorld is opaque in mcgen.h). */
+MCGEN_API int mcgen_gb300_world_info(const McWorld *w, int *version, int *dimension, int64_t *climate_seed,
+                                     int *float_branch);
+
+/* Quart grid at quart y for the world's climate seed: out[iz*nx+ix] = biome of quart cell
+ * (qx0+ix, qy, qz0+iz), no zoom.  tie_rule: MCGEN_TIE_ENGINE or MCGEN_TIE_GRID_CHAIN (the initial
+ * candidate is none).  New in this library; the reference computes these grids in its Java oracle
+ * (ClimateApi.grid) and, per point, in engine/cuda/mcg_host.c:36-83. */
+MCGEN_API int mcgen_gb300_quart_grid(const McWorld *w, int qx0, int qz0, int nx, int nz, int qy, int tie_rule,
+                                     uint8_t *out);
+
+/* Many seeds x fixed quart points, ENGINE rule: out[s*np+p] for seeds[s] at quart point
+ * qxyz[3p..3p+2]; targets (optional) receives the 6 quantised climate values per sample
+ * (Nether T,H,0,0,0,0; End zeros).  The world supplies version, dimension and preset; its own seed is
+ * ignored.  Replaces crack/src/gpu_biomes/gpu_biomes.h:22-57 gb_points_gpu (host buffers). */
+MCGEN_API int mcgen_gb300_seed_points(const McWorld *w, const int64_t *seeds, int ns, const int32_t *qxyz, int np,
+                                      uint8_t *out, int32_t *targets);
+
+/* Device-pointer forms: every pointer is CUDA device memory, work is queued on `stream`
+ * (a cudaStream_t, NULL = the legacy default stream) and the call returns without synchronising. */
+MCGEN_API int mcgen_gb300_seed_points_dev(const McWorld *w, const int64_t *d_seeds, int ns, const int32_t *d_qxyz,
+                                          int np, uint8_t *d_out, int32_t *d_targets, void *stream);
+MCGEN_API int mcgen_gb300_biome_grid_dev(const McWorld *w, int x0, int z0, int nx, int nz, int step, int y,
+                                         uint8_t *d_out, void *stream);
+MCGEN_API int mcgen_gb300_quart_grid_dev(const McWorld *w, int qx0, int qz0, int nx, int nz, int qy, int tie_rule,
+                                         uint8_t *d_out, void *stream);
+
+/* Number of kernel launches the library issued since load (for launch accounting in benchmarks). */
+MCGEN_API long long mcgen_gb300_launch_count(void);
+
+/* Per-kernel timing of the library's own launches: while enabled, each launch is bracketed by two CUDA
+ * events on its stream.  mcgen_gb300_profile(1) clears and starts, (0) stops; profile_read returns kernel
+ * `kernel`'s name (k_setup_xo, k_points, ...), summed milliseconds and launch count; MCGEN_E_ARG past the
+ * last kernel. */
+MCGEN_API int mcgen_gb300_profile(int enable);
+MCGEN_API int mcgen_gb300_profile_read(int kernel, const char **name, double *total_ms, long long *launches);
+
+/* Last CUDA error text seen by the library (empty when none). */
+MCGEN_API const char *mcgen_gb300_last_error(void);
+
+/* Pipe microbenchmarks on the current device, in giga-operations per second:
+ * 0 FP32 FMA, 1 FP64 FMA, 2 FP64 add, 3 int32 multiply-add, 4 double->int floor conversion,
+ * 5 int->double conversion, 6 double->float conversion, 7 64-bit wide integer multiply-add. */
+MCGEN_API int mcgen_gb300_pipe_rate(int pipe, double *gops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

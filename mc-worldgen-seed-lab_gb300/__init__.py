@@ -1,0 +1,328 @@
+"""Python binding of libmcgen_gb300.so -- the GB300 biome engine behind libmcgen's C ABI.
+
+Mirrors the reference's ctypes layer (blender/mcgen_addon/core/lib.py: ``load``, ``McError``,
+``Generator.open(...).world(dimension, preset, seeds)``, ``World.biome_at`` / ``World.biome_grid``) so
+callers and tests read like the reference's, plus the additions of include/mcgen_gb300.h (seeds x points,
+quart grids with a tie rule, device-pointer forms).
+
+The library is the product: loading fails loudly when libmcgen_gb300.so has not been built, and every
+biome call raises McError when no CUDA device is usable.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmcgen_gb300.so")
+DATA_ROOT = HERE  # data/climate-<V>.txt and data/params/<V>/ live under this directory
+
+MCGEN_OK, MCGEN_E_ARG, MCGEN_E_IO, MCGEN_E_DATA, MCGEN_E_VERSION = 0, 1, 2, 3, 4
+MCGEN_E_NOMEM, MCGEN_E_CANCEL, MCGEN_E_UNSUPPORTED, MCGEN_E_INTERNAL = 5, 6, 7, 8
+MCGEN_COMPUTE_CPU, MCGEN_COMPUTE_GPU, MCGEN_COMPUTE_AUTO = 0, 1, 2
+TIE_ENGINE, TIE_GRID_CHAIN, TIE_CHUNK_CELL = 0, 1, 2
+PIPES = {"fp32_fma": 0, "fp64_fma": 1, "fp64_add": 2, "int32_mad": 3, "cvt_f64_floor_s32": 4,
+         "cvt_s32_f64": 5, "cvt_f64_f32": 6, "int64_mad": 7}
+ERR_BUF = 1024
+_P = C.c_void_p
+
+
+class McError(RuntimeError):
+    def __init__(self, code: int, message: str, where: str = ""):
+        super().__init__(f"{where}: {message} (code {code})" if where else f"{message} (code {code})")
+        self.code = code
+        self.where = where
+
+
+class McSeeds(C.Structure):
+    _fields_ = [("climate", C.c_int64), ("terrain", C.c_int64), ("structures", C.c_int64), ("features", C.c_int64)]
+
+
+_PROTOS = {
+    "mcgen_version": (C.c_char_p, []),
+    "mcgen_abi_version": (C.c_int, []),
+    "mcgen_open": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(_P), C.c_char_p, C.c_size_t]),
+    "mcgen_close": (None, [_P]),
+    "mcgen_dimension_count": (C.c_int, [_P]),
+    "mcgen_dimension_name": (C.c_char_p, [_P, C.c_int]),
+    "mcgen_preset_count": (C.c_int, [_P, C.c_char_p]),
+    "mcgen_preset_name": (C.c_char_p, [_P, C.c_char_p, C.c_int]),
+    "mcgen_block_state_count": (C.c_int, [_P]),
+    "mcgen_biome_count": (C.c_int, [_P]),
+    "mcgen_biome_name": (C.c_char_p, [_P, C.c_int]),
+    "mcgen_tweak_count": (C.c_int, [_P]),
+    "mcgen_world_new": (C.c_int, [_P, C.c_char_p, C.c_char_p, C.POINTER(McSeeds), _P, C.c_int, C.POINTER(_P),
+                                  C.c_char_p, C.c_size_t]),
+    "mcgen_world_free": (None, [_P]),
+    "mcgen_world_min_y": (C.c_int, [_P]),
+    "mcgen_world_height": (C.c_int, [_P]),
+    "mcgen_world_sea_level": (C.c_int, [_P]),
+    "mcgen_biome_at": (C.c_int, [_P, C.c_int, C.c_int, C.c_int]),
+    "mcgen_biome_grid": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
+    "mcgen_gpu_biome_grid": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
+    "mcgen_biome_grid_cpu": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
+    "mcgen_gpu_biome_points": (C.c_int, [_P, C.c_int, _P, _P, C.POINTER(C.c_int)]),
+    "mcgen_generate_region": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint32, C.c_int, _P, _P,
+                                        C.POINTER(_P), C.c_char_p, C.c_size_t]),
+    "mcgen_gpu_set_features": (C.c_int, [C.c_int]),
+    "mcgen_gpu_get_features": (C.c_int, []),
+    "mcgen_gpu_set_library_path": (C.c_int, [C.c_char_p]),
+    "mcgen_gpu_device_count": (C.c_int, []),
+    "mcgen_gpu_device_info": (C.c_int, [C.c_int, C.c_char_p, C.c_size_t, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                        C.POINTER(C.c_size_t)]),
+    "mcgen_gpu_set_compute": (C.c_int, [C.c_int, C.c_int]),
+    "mcgen_gpu_get_compute": (C.c_int, []),
+    "mcgen_gpu_status": (C.c_int, [C.c_char_p, C.c_size_t]),
+    "mcgen_gpu_selftest": (C.c_int, [_P, C.c_int, C.c_char_p, C.c_size_t]),
+    "mcgen_gb300_world_info": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int64),
+                                         C.POINTER(C.c_int)]),
+    "mcgen_gb300_quart_grid": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P]),
+    "mcgen_gb300_quart_grid_dev": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P]),
+    "mcgen_gb300_seed_points": (C.c_int, [_P, _P, C.c_int, _P, C.c_int, _P, _P]),
+    "mcgen_gb300_seed_points_dev": (C.c_int, [_P, _P, C.c_int, _P, C.c_int, _P, _P, _P]),
+    "mcgen_gb300_biome_grid_dev": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P]),
+    "mcgen_gb300_launch_count": (C.c_longlong, []),
+    "mcgen_gb300_last_error": (C.c_char_p, []),
+    "mcgen_gb300_profile": (C.c_int, [C.c_int]),
+    "mcgen_gb300_profile_read": (C.c_int, [C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_double),
+                                           C.POINTER(C.c_longlong)]),
+    "mcgen_gb300_pipe_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+}
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load libmcgen_gb300.so (built in-tree by build.py).  Raises if it is missing: there is no fallback."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise McError(MCGEN_E_UNSUPPORTED, f"{p} not built (run the package's build.py)", "load")
+    L = C.CDLL(p)
+    for name, (res, args) in _PROTOS.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc: int, where: str, err=None):
+    if rc != MCGEN_OK:
+        msg = err.value.decode(errors="replace") if err is not None and err.value else ""
+        if not msg:
+            msg = (load().mcgen_gb300_last_error() or b"").decode(errors="replace") or "failed"
+        raise McError(rc, msg, where)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_P)
+
+
+def version_string() -> str:
+    return load().mcgen_version().decode()
+
+
+def device_count() -> int:
+    return load().mcgen_gpu_device_count()
+
+
+def gpu_status() -> tuple[bool, str]:
+    buf = C.create_string_buffer(2048)
+    ok = load().mcgen_gpu_status(buf, 2048)
+    return bool(ok), buf.value.decode(errors="replace")
+
+
+def launch_count() -> int:
+    return load().mcgen_gb300_launch_count()
+
+
+def profile(enable: bool) -> None:
+    """Start (clearing) or stop per-kernel CUDA-event timing of the library's launches."""
+    _check(load().mcgen_gb300_profile(1 if enable else 0), "mcgen_gb300_profile")
+
+
+def profile_read() -> dict:
+    """{kernel name: (total ms, launches)} for kernels launched while profiling was on."""
+    L = load()
+    out = {}
+    k = 0
+    while True:
+        name, ms, n = C.c_char_p(), C.c_double(), C.c_longlong()
+        if L.mcgen_gb300_profile_read(k, C.byref(name), C.byref(ms), C.byref(n)) != MCGEN_OK:
+            break
+        if n.value:
+            out[name.value.decode()] = (ms.value, n.value)
+        k += 1
+    return out
+
+
+def pipe_rate(pipe: str) -> float:
+    """Measured throughput of one GPU pipe in giga-operations per second (see PIPES)."""
+    g = C.c_double()
+    _check(load().mcgen_gb300_pipe_rate(PIPES[pipe], C.byref(g)), "mcgen_gb300_pipe_rate")
+    return g.value
+
+
+class Generator:
+    """McGen: one version's data (mcgen_open)."""
+
+    def __init__(self, handle, data_root: str, version: str):
+        self._h = handle
+        self.data_root = data_root
+        self.version = version
+
+    @classmethod
+    def open(cls, data_root: str = DATA_ROOT, version: str = "26.3") -> "Generator":
+        L = load()
+        h = _P()
+        err = C.create_string_buffer(ERR_BUF)
+        _check(L.mcgen_open(data_root.encode(), version.encode(), C.byref(h), err, ERR_BUF), "mcgen_open", err)
+        return cls(h, data_root, version)
+
+    def close(self):
+        if self._h:
+            load().mcgen_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def dimensions(self) -> list[str]:
+        L = load()
+        return [L.mcgen_dimension_name(self._h, i).decode() for i in range(L.mcgen_dimension_count(self._h))]
+
+    def presets(self, dimension: str) -> list[str]:
+        L = load()
+        d = dimension.encode()
+        return [L.mcgen_preset_name(self._h, d, i).decode() for i in range(L.mcgen_preset_count(self._h, d))]
+
+    def biome_names(self) -> list[str]:
+        L = load()
+        return [L.mcgen_biome_name(self._h, i).decode() for i in range(L.mcgen_biome_count(self._h))]
+
+    def world(self, dimension: str = "minecraft:overworld", preset: str = "normal", seeds=0) -> "World":
+        return World.create(self, dimension, preset, seeds)
+
+    def selftest(self, npoints: int = 384) -> str:
+        buf = C.create_string_buffer(8192)
+        _check(load().mcgen_gpu_selftest(self._h, npoints, buf, 8192), "mcgen_gpu_selftest")
+        return buf.value.decode()
+
+
+def _norm_seeds(seeds) -> McSeeds:
+    if isinstance(seeds, McSeeds):
+        return seeds
+    if isinstance(seeds, (tuple, list)):
+        return McSeeds(*[int(s) for s in seeds])
+    s = int(seeds)
+    return McSeeds(s, s, s, s)
+
+
+class World:
+    """McWorld: dimension + preset + seeds."""
+
+    def __init__(self, handle, gen: Generator, dimension: str, preset: str, seeds: McSeeds):
+        self._h = handle
+        self.gen = gen
+        self.dimension = dimension
+        self.preset = preset
+        self.seeds = seeds
+
+    @classmethod
+    def create(cls, gen: Generator, dimension: str, preset: str, seeds) -> "World":
+        L = load()
+        sd = _norm_seeds(seeds)
+        h = _P()
+        err = C.create_string_buffer(ERR_BUF)
+        _check(L.mcgen_world_new(gen._h, dimension.encode(), preset.encode() if preset else None, C.byref(sd), None, 0,
+                                 C.byref(h), err, ERR_BUF), "mcgen_world_new", err)
+        return cls(h, gen, dimension, preset, sd)
+
+    def close(self):
+        if self._h:
+            load().mcgen_world_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def min_y(self) -> int:
+        return load().mcgen_world_min_y(self._h)
+
+    @property
+    def height(self) -> int:
+        return load().mcgen_world_height(self._h)
+
+    @property
+    def sea_level(self) -> int:
+        return load().mcgen_world_sea_level(self._h)
+
+    # ---- libmcgen biome calls ----
+    def biome_at(self, x: int, y: int, z: int) -> int:
+        return load().mcgen_biome_at(self._h, int(x), int(y), int(z))
+
+    def biome_grid(self, x0: int, z0: int, nx: int, nz: int, step: int = 1, y: int = 63) -> np.ndarray:
+        out = np.empty((nz, nx), np.uint8)
+        _check(load().mcgen_biome_grid(self._h, int(x0), int(z0), int(nx), int(nz), int(step), int(y), _ptr(out)),
+               "mcgen_biome_grid")
+        return out
+
+    def biome_points(self, xyz) -> np.ndarray:
+        xyz = np.ascontiguousarray(xyz, dtype=np.int32).reshape(-1, 3)
+        out = np.empty(len(xyz), np.uint8)
+        ncpu = C.c_int()
+        _check(load().mcgen_gpu_biome_points(self._h, len(xyz), _ptr(xyz), _ptr(out), C.byref(ncpu)),
+               "mcgen_gpu_biome_points")
+        return out
+
+    # ---- additions (mcgen_gb300.h) ----
+    def quart_grid(self, qx0: int, qz0: int, nx: int, nz: int, qy: int, tie_rule: int = TIE_ENGINE) -> np.ndarray:
+        out = np.empty((nz, nx), np.uint8)
+        _check(load().mcgen_gb300_quart_grid(self._h, qx0, qz0, nx, nz, qy, tie_rule, _ptr(out)),
+               "mcgen_gb300_quart_grid")
+        return out
+
+    def seed_points(self, seeds, qxyz, want_targets: bool = False):
+        seeds = np.ascontiguousarray(seeds, dtype=np.int64)
+        qxyz = np.ascontiguousarray(qxyz, dtype=np.int32).reshape(-1, 3)
+        out = np.empty((len(seeds), len(qxyz)), np.uint8)
+        tg = np.empty((len(seeds), len(qxyz), 6), np.int32) if want_targets else None
+        _check(load().mcgen_gb300_seed_points(self._h, _ptr(seeds), len(seeds), _ptr(qxyz), len(qxyz), _ptr(out),
+                                              _ptr(tg) if tg is not None else None), "mcgen_gb300_seed_points")
+        return (out, tg) if want_targets else out
+
+    # device-pointer forms: integer addresses of device buffers and a cudaStream_t handle
+    def seed_points_dev(self, d_seeds: int, ns: int, d_qxyz: int, np_: int, d_out: int, d_targets: int = 0,
+                        stream: int = 0):
+        _check(load().mcgen_gb300_seed_points_dev(self._h, d_seeds, ns, d_qxyz, np_, d_out, d_targets or None,
+                                                  stream or None), "mcgen_gb300_seed_points_dev")
+
+    def biome_grid_dev(self, x0, z0, nx, nz, step, y, d_out: int, stream: int = 0):
+        _check(load().mcgen_gb300_biome_grid_dev(self._h, x0, z0, nx, nz, step, y, d_out, stream or None),
+               "mcgen_gb300_biome_grid_dev")
+
+    def quart_grid_dev(self, qx0, qz0, nx, nz, qy, tie_rule, d_out: int, stream: int = 0):
+        _check(load().mcgen_gb300_quart_grid_dev(self._h, qx0, qz0, nx, nz, qy, tie_rule, d_out, stream or None),
+               "mcgen_gb300_quart_grid_dev")

@@ -1,0 +1,389 @@
+/* device.cuh -- sm_103a device functions of the biome path.
+ *
+ * Compiled with --fmad=false and IEEE division/square root: every float/double operation below is
+ * rounded separately, in the reference's order, so results are bit-identical to the reference engine
+ * (engine/mc_noise.h, mc_climate.h, mc_biomes.h, mc_end.h) and libmcgen's biome map
+ * (libmcgen/src/region.c, biome.c).
+ */
+#ifndef MG_DEVICE_CUH
+#define MG_DEVICE_CUH
+#include <stdint.h>
+
+#include "mg_types.h"
+
+#define MG_SECOND_STACK 1.0181268882175227 /* NormalNoise second-stack input factor */
+
+namespace mgd {
+
+/* ------------------------------------------------------------------ RNG (engine/mc_rng.h) */
+struct Xo { uint64_t lo, hi; };
+__device__ __forceinline__ uint64_t rotl64(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+__device__ __forceinline__ uint64_t stafford13(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ Xo xo_make(uint64_t lo, uint64_t hi) {
+    Xo r;
+    if ((lo | hi) == 0) { lo = 0x9E3779B97F4A7C15ULL; hi = 0x6A09E667F3BCC909ULL; }
+    r.lo = lo;
+    r.hi = hi;
+    return r;
+}
+/* XoroshiroRandomSource(long): upgradeSeedTo128bit */
+__device__ __forceinline__ Xo xo_from_seed(int64_t seed) {
+    uint64_t a = (uint64_t)seed ^ 0x6A09E667F3BCC909ULL;
+    return xo_make(stafford13(a), stafford13(a + 0x9E3779B97F4A7C15ULL));
+}
+__device__ __forceinline__ uint64_t xo_next(Xo &r) {
+    uint64_t s0 = r.lo, s1 = r.hi;
+    uint64_t out = rotl64(s0 + s1, 17) + s0;
+    s1 ^= s0;
+    r.lo = rotl64(s0, 49) ^ s1 ^ (s1 << 21);
+    r.hi = rotl64(s1, 28);
+    return out;
+}
+/* nextInt(bound), Lemire multiply with rejection (XoroshiroRandomSource.nextInt) */
+__device__ __forceinline__ int xo_int(Xo &r, uint32_t bound) {
+    uint64_t m = (uint64_t)(uint32_t)xo_next(r) * bound;
+    if ((uint32_t)m < bound) {
+        uint32_t thresh = (0u - bound) % bound;
+        while ((uint32_t)m < thresh) m = (uint64_t)(uint32_t)xo_next(r) * bound;
+    }
+    return (int)(m >> 32);
+}
+__device__ __forceinline__ double xo_double(Xo &r) { return (double)(xo_next(r) >> 11) * 0x1.0p-53; }
+
+/* java.util.Random LCG */
+#define MG_LCG_MUL 0x5DEECE66DULL
+#define MG_LCG_MASK 0xFFFFFFFFFFFFULL
+__device__ __forceinline__ uint64_t lcg_init(int64_t seed) { return ((uint64_t)seed ^ MG_LCG_MUL) & MG_LCG_MASK; }
+__device__ __forceinline__ int32_t lcg_bits(uint64_t &s, int bits) {
+    s = (s * MG_LCG_MUL + 0xBULL) & MG_LCG_MASK;
+    return (int32_t)(uint32_t)(s >> (48 - bits));
+}
+__device__ __forceinline__ int lcg_int(uint64_t &s, int32_t bound) {
+    if ((bound & -bound) == bound) return (int)(((int64_t)bound * (int64_t)lcg_bits(s, 31)) >> 31);
+    for (;;) {
+        int32_t b = lcg_bits(s, 31), v = b % bound;
+        if ((int32_t)((uint32_t)b - (uint32_t)v + (uint32_t)(bound - 1)) >= 0) return v;
+    }
+}
+__device__ __forceinline__ double lcg_double(uint64_t &s) {
+    int64_t hi = lcg_bits(s, 26), lo = lcg_bits(s, 27);
+    return (double)((hi << 27) + lo) * 0x1.0p-53;
+}
+/* s' = A^n s + C_n (mod 2^48): the state after n calls, for a constant step count */
+__device__ __forceinline__ uint64_t lcg_jump(uint64_t s, uint32_t n) {
+    uint64_t mul = 1, add = 0, cm = MG_LCG_MUL, ca = 0xB;
+    while (n) {
+        if (n & 1) { mul = (mul * cm) & MG_LCG_MASK; add = (add * cm + ca) & MG_LCG_MASK; }
+        ca = ((cm + 1) * ca) & MG_LCG_MASK;
+        cm = (cm * cm) & MG_LCG_MASK;
+        n >>= 1;
+    }
+    return (s * mul + add) & MG_LCG_MASK;
+}
+
+/* ------------------------------------------------------------------ Java floor */
+/* Mth.floor for |v| < 2^31 (cvt.rmi) */
+__device__ __forceinline__ int ifloor(double v) { return __double2int_rd(v); }
+__device__ __forceinline__ int64_t lfloor(double v) { return __double2ll_rd(v); }
+
+/* ------------------------------------------------------------------ lattice header */
+/* fill the y/z splits a zero input coordinate uses */
+__device__ __forceinline__ void lattice_header(MgLattice &L) {
+    L.iy = ifloor(L.oy);
+    L.iz = ifloor(L.oz);
+    L.fyd = L.oy - (double)L.iy;
+    L.fzd = L.oz - (double)L.iz;
+    L.fy = (float)L.fyd;
+    L.fz = (float)L.fzd;
+}
+
+/* ------------------------------------------------------------------ Perlin octave (shared lattice math) */
+/* gradient dot with SimplexNoise.GRADIENT[h & 15]: every vector has two +-1 components, so the dot is a
+ * signed sum of two coordinates.  (It can differ from g.x*x + g.y*y + g.z*z only in the sign of an
+ * exactly-zero result, which no later step of the path can observe: the layer sum starts at +0.) */
+template <typename T>
+__device__ __forceinline__ T gdot(int h, T x, T y, T z) {
+    h &= 15;
+    T u = h < 8 ? x : y;
+    T v = h < 4 ? y : ((h == 12 || h == 14) ? x : z);
+    return ((h & 1) ? -u : u) + ((h & 2) ? -v : v);
+}
+template <typename T>
+__device__ __forceinline__ T fade(T t) {
+    return t * t * t * (t * (t * (T)6 - (T)15) + (T)10);
+}
+template <typename T>
+__device__ __forceinline__ T lerp(T t, T a, T b) { return a + t * (b - a); }
+
+/* ImprovedNoise.sampleAndLerp with split coordinates (engine/mc_noise.h:54-75 / 90-110). */
+template <typename T>
+__device__ __forceinline__ T octave(const uint8_t *__restrict__ p, int ix, T fx, int iy, T fy, int iz, T fz) {
+    int a = p[ix & 255], b = p[(ix + 1) & 255];
+    int aa = p[(a + iy) & 255], ab = p[(a + iy + 1) & 255];
+    int ba = p[(b + iy) & 255], bb = p[(b + iy + 1) & 255];
+    T gx = fx - (T)1, gy = fy - (T)1, gz = fz - (T)1;
+    T c000 = gdot<T>(p[(aa + iz) & 255], fx, fy, fz);
+    T c100 = gdot<T>(p[(ba + iz) & 255], gx, fy, fz);
+    T c010 = gdot<T>(p[(ab + iz) & 255], fx, gy, fz);
+    T c110 = gdot<T>(p[(bb + iz) & 255], gx, gy, fz);
+    T c001 = gdot<T>(p[(aa + iz + 1) & 255], fx, fy, gz);
+    T c101 = gdot<T>(p[(ba + iz + 1) & 255], gx, fy, gz);
+    T c011 = gdot<T>(p[(ab + iz + 1) & 255], fx, gy, gz);
+    T c111 = gdot<T>(p[(bb + iz + 1) & 255], gx, gy, gz);
+    T u = fade<T>(fx), v = fade<T>(fy), w = fade<T>(fz);
+    return lerp<T>(w, lerp<T>(v, lerp<T>(u, c000, c100), lerp<T>(u, c010, c110)),
+                   lerp<T>(v, lerp<T>(u, c001, c101), lerp<T>(u, c011, c111)));
+}
+
+/* 26.3 PerlinNoise.wrap: identity inside (-2^24, 2^24) (engine/mc_noise.h:86-89) */
+__device__ __forceinline__ double wrap_new(double x) {
+    const double lim = 16777215.999999998;
+    if (x >= -lim && x < lim) return x;
+    return x - (double)lfloor(x / 33554432.0 + 0.5) * 33554432.0;
+}
+/* 26.1/26.2 PerlinNoise.wrap (engine/mc_noise.h:76-77); exact identity for |x| < 2^23 */
+__device__ __forceinline__ double wrap_old(double x) {
+    if (fabs(x) < 8388608.0) return x;
+    return x - (double)lfloor(x / 33554432.0 + 0.5) * 33554432.0;
+}
+/* one input coordinate -> lattice cell and fraction */
+__device__ __forceinline__ void split_f(double v, double off, int &i, float &f) {
+    double s = wrap_new(v) + off;
+    i = ifloor(s);
+    f = (float)(s - (double)i);
+}
+__device__ __forceinline__ void split_d(double v, double off, int &i, double &f) {
+    double s = wrap_old(v) + off;
+    i = ifloor(s);
+    f = s - (double)i;
+}
+
+/* Octave with input (x, 0, z) and with input (x, y, 0): the zero coordinate uses the table's split. */
+__device__ __forceinline__ float oct_f_y0(const MgLattice *__restrict__ L, double x, double z) {
+    int ix, iz;
+    float fx, fz;
+    split_f(x, L->ox, ix, fx);
+    split_f(z, L->oz, iz, fz);
+    return octave<float>(L->p, ix, fx, L->iy, L->fy, iz, fz);
+}
+__device__ __forceinline__ float oct_f_z0(const MgLattice *__restrict__ L, double x, double y) {
+    int ix, iy;
+    float fx, fy;
+    split_f(x, L->ox, ix, fx);
+    split_f(y, L->oy, iy, fy);
+    return octave<float>(L->p, ix, fx, iy, fy, L->iz, L->fz);
+}
+__device__ __forceinline__ double oct_d_y0(const MgLattice *__restrict__ L, double x, double z) {
+    int ix, iz;
+    double fx, fz;
+    split_d(x, L->ox, ix, fx);
+    split_d(z, L->oz, iz, fz);
+    return octave<double>(L->p, ix, fx, L->iy, L->fyd, iz, fz);
+}
+__device__ __forceinline__ double oct_d_z0(const MgLattice *__restrict__ L, double x, double y) {
+    int ix, iy;
+    double fx, fy;
+    split_d(x, L->ox, ix, fx);
+    split_d(y, L->oy, iy, fy);
+    return octave<double>(L->p, ix, fx, iy, fy, L->iz, L->fzd);
+}
+
+/* ------------------------------------------------------------------ NormalNoise (engine/mc_noise.h:285-324)
+ * Every NormalNoise on the biome path has one input coordinate equal to zero: the five climate noises
+ * and the Nether noises take (x, 0, z), ShiftA (x, 0, z), ShiftB (z, x, 0).  The second stack's input
+ * x*(f*c) equals (x*c)*f exactly (f is a power of two), so xc = x*c is formed once per point. */
+/* float branch, non-legacy (interleaved first_k, second_k) */
+__device__ __forceinline__ float nn_f_y0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
+                                         double xc, double zc) {
+    float acc = 0.0f;
+    const MgLattice *A = T + N.base, *B = A + N.nlev;
+    for (int k = 0; k < N.nlev; k++) {
+        double f = N.freq[k];
+        acc += N.amp_f[k] * oct_f_y0(A + k, x * f, z * f);
+        acc += N.amp_f[k] * oct_f_y0(B + k, xc * f, zc * f);
+    }
+    return acc;
+}
+__device__ __forceinline__ float nn_f_z0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double y,
+                                         double xc, double yc) {
+    float acc = 0.0f;
+    const MgLattice *A = T + N.base, *B = A + N.nlev;
+    for (int k = 0; k < N.nlev; k++) {
+        double f = N.freq[k];
+        acc += N.amp_f[k] * oct_f_z0(A + k, x * f, y * f);
+        acc += N.amp_f[k] * oct_f_z0(B + k, xc * f, yc * f);
+    }
+    return acc;
+}
+/* float branch, legacy Nether form (whole first stack, then whole second stack) */
+__device__ __forceinline__ float nn_f_legacy_y0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
+                                                double xc, double zc) {
+    float acc = 0.0f;
+    const MgLattice *A = T + N.base, *B = A + N.nlev;
+    for (int k = 0; k < N.nlev; k++) acc += N.amp_f[k] * oct_f_y0(A + k, x * N.freq[k], z * N.freq[k]);
+    for (int k = 0; k < N.nlev; k++) acc += N.amp_f[k] * oct_f_y0(B + k, xc * N.freq[k], zc * N.freq[k]);
+    return acc;
+}
+/* double branch: (first + second) * valueFactor */
+__device__ __forceinline__ double nn_d_y0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
+                                          double xc, double zc) {
+    double a = 0.0, b = 0.0;
+    const MgLattice *A = T + N.base, *B = A + N.nlev;
+    for (int k = 0; k < N.nlev; k++) {
+        double f = N.freq[k];
+        a += N.amp_d[k] * oct_d_y0(A + k, x * f, z * f) * N.vf_d[k];
+    }
+    for (int k = 0; k < N.nlev; k++) {
+        double f = N.freq[k];
+        b += N.amp_d[k] * oct_d_y0(B + k, xc * f, zc * f) * N.vf_d[k];
+    }
+    return (a + b) * N.vfac;
+}
+__device__ __forceinline__ double nn_d_z0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double y,
+                                          double xc, double yc) {
+    double a = 0.0, b = 0.0;
+    const MgLattice *A = T + N.base, *B = A + N.nlev;
+    for (int k = 0; k < N.nlev; k++) {
+        double f = N.freq[k];
+        a += N.amp_d[k] * oct_d_z0(A + k, x * f, y * f) * N.vf_d[k];
+    }
+    for (int k = 0; k < N.nlev; k++) {
+        double f = N.freq[k];
+        b += N.amp_d[k] * oct_d_z0(B + k, xc * f, yc * f) * N.vf_d[k];
+    }
+    return (a + b) * N.vfac;
+}
+
+/* ------------------------------------------------------------------ offset spline (engine/mc_climate.h:38-66)
+ * CubicSpline.Multipoint.apply, evaluated with an explicit stack instead of recursion. */
+__device__ __forceinline__ float spline_eval(const MgSpline &S, const float co[4]) {
+    if (S.root < 0) return S.cval[~S.root];
+    struct Frame { int node, i; float in, y1; int state; };
+    Frame st[12];
+    int sp = 0;
+    float ret = 0.0f;
+    st[0].node = S.root;
+    st[0].state = 0;
+    sp = 1;
+    while (sp > 0) {
+        Frame &f = st[sp - 1];
+        int o = S.first[f.node], n = S.npts[f.node];
+        if (f.state == 0) {
+            float in = co[S.coord[f.node]];
+            int lo = 0, len = n; /* Mth.binarySearch(0, n, i -> in < loc[i]) */
+            while (len > 0) {
+                int half = len >> 1, mid = lo + half;
+                if (in < S.loc[o + mid]) len = half;
+                else { lo = mid + 1; len -= half + 1; }
+            }
+            f.in = in;
+            f.i = lo - 1;
+            int c;
+            if (f.i < 0 || f.i == n - 1) { f.state = 1; c = S.child[o + (f.i < 0 ? 0 : n - 1)]; }
+            else { f.state = 2; c = S.child[o + f.i]; }
+            if (c < 0) { ret = S.cval[~c]; continue; } /* constant child: deliver at once */
+            st[sp].node = c;
+            st[sp].state = 0;
+            sp++;
+            continue;
+        }
+        if (f.state == 1) { /* linear extension at the first or last point */
+            int e = f.i < 0 ? 0 : n - 1;
+            float d = S.der[o + e];
+            ret = d == 0.0f ? ret : ret + d * (f.in - S.loc[o + e]);
+            sp--;
+            continue;
+        }
+        if (f.state == 2) { /* have y1, fetch y2 */
+            f.y1 = ret;
+            f.state = 3;
+            int c = S.child[o + f.i + 1];
+            if (c < 0) { ret = S.cval[~c]; continue; }
+            st[sp].node = c;
+            st[sp].state = 0;
+            sp++;
+            continue;
+        }
+        /* state 3: cubic Hermite interpolation */
+        float x1 = S.loc[o + f.i], x2 = S.loc[o + f.i + 1];
+        float t = (f.in - x1) / (x2 - x1);
+        float d1 = S.der[o + f.i], d2 = S.der[o + f.i + 1];
+        float y1 = f.y1, y2 = ret;
+        float a = d1 * (x2 - x1) - (y2 - y1);
+        float b = -d2 * (x2 - x1) + (y2 - y1);
+        ret = lerp<float>(t, y1, y2) + t * (1.0f - t) * lerp<float>(t, a, b);
+        sp--;
+    }
+    return ret;
+}
+
+/* ------------------------------------------------------------------ biome R-tree (engine/mc_biomes.h:31-62) */
+__device__ __forceinline__ uint64_t node_dist(const MgTreeNode &n, const int32_t *t) {
+    uint64_t s = 0;
+#pragma unroll
+    for (int d = 0; d < 6; d++) {
+        int32_t a = t[d] - (int32_t)n.hi[d], b = (int32_t)n.lo[d] - t[d];
+        int32_t x = max(max(a, b), 0);
+        s += (uint64_t)((int64_t)x * x);
+    }
+    /* seventh dimension: the target's offset coordinate is 0 */
+    int32_t a = -(int32_t)n.hi[6], b = (int32_t)n.lo[6];
+    int32_t x = max(max(a, b), 0);
+    s += (uint64_t)((int64_t)x * x);
+    return s;
+}
+/* Climate.RTree.SubTree.search, iterative: descend into a child iff its box distance is below the best
+ * leaf distance so far; a leaf replaces the best iff strictly closer.  cand < 0: no candidate. */
+__device__ __forceinline__ int tree_search(const MgTreeNode *__restrict__ T, const int32_t *t, int cand,
+                                           uint64_t &best) {
+    int res = cand;
+    best = cand < 0 ? ~0ULL : node_dist(T[cand], t);
+    int stk_node[10];
+    int stk_next[10];
+    int sp = 0;
+    stk_node[0] = 0;
+    stk_next[0] = 0;
+    sp = 1;
+    while (sp > 0) {
+        int nd = stk_node[sp - 1];
+        int c = stk_next[sp - 1];
+        int cnt = T[nd].count;
+        if (c >= cnt) { sp--; continue; }
+        stk_next[sp - 1] = c + 1;
+        int ci = T[nd].first + c;
+        uint64_t cd = node_dist(T[ci], t);
+        if (cd < best) {
+            if (T[ci].count == 0) { best = cd; res = ci; }
+            else if (sp < 10) { stk_node[sp] = ci; stk_next[sp] = 0; sp++; }
+        }
+    }
+    return res;
+}
+/* leaves at fitness d, capped at 2 (libmcgen/src/biome.c:76-85) */
+__device__ __forceinline__ int tree_count_at(const MgTreeNode *__restrict__ T, const int32_t *t, uint64_t d) {
+    int stk_node[10], stk_next[10], sp = 1, cnt = 0;
+    stk_node[0] = 0;
+    stk_next[0] = 0;
+    while (sp > 0 && cnt < 2) {
+        int nd = stk_node[sp - 1], c = stk_next[sp - 1];
+        if (c >= T[nd].count) { sp--; continue; }
+        stk_next[sp - 1] = c + 1;
+        int ci = T[nd].first + c;
+        uint64_t cd = node_dist(T[ci], t);
+        if (cd <= d) {
+            if (T[ci].count == 0) cnt += (cd == d);
+            else if (sp < 10) { stk_node[sp] = ci; stk_next[sp] = 0; sp++; }
+        }
+    }
+    return cnt;
+}
+
+/* (long)(v * 10000f) */
+__device__ __forceinline__ int32_t quantize(float v) { return (int32_t)(int64_t)(v * 10000.0f); }
+
+}  // namespace mgd
+#endif

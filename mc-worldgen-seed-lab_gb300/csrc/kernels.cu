@@ -1,0 +1,630 @@
+/* kernels.cu -- sm_103a kernels of the biome path and their host launchers.
+ *
+ *  per-seed setup   k_setup_xo      one thread per (seed, lattice): Xoroshiro positional seeding and the
+ *                                   256-step Fisher-Yates shuffle in a bank-conflict-free shared layout
+ *                   k_setup_legacy  Nether biome noises: java.util.Random, octaves from the zero octave down
+ *                   k_setup_end     End island simplex: LCG(seed) jumped 17292 steps, one shuffle
+ *  per-point        k_points        seeds x quart points (ENGINE tie rule), lattices read through L1
+ *                   k_grid          one seed's quart grid, lattices staged in shared memory;
+ *                                   ENGINE biomes or GRID_CHAIN records (leaf, fitness, tie flag, target)
+ *                   k_chain_resolve GRID_CHAIN replay for the (rare) tied cells
+ *                   k_blockgrid     libmcgen mcgen_biome_grid: BiomeManager zoom + chunk-cell tie chain
+ *                   k_end_chunks    End island class per chunk
+ */
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "device.cuh"
+#include "launch.h"
+#include "prof.h"
+
+using namespace mgd;
+
+/* the cooperative 16-byte copies below rely on these layouts */
+static_assert(sizeof(MgLattice) % 16 == 0, "lattice size");
+static_assert(sizeof(MgSpline) % 16 == 0, "spline size");
+static_assert(offsetof(MgWorldDesc, spline) % 16 == 0, "spline alignment in the description");
+static_assert(sizeof(MgWorldDesc) <= 24576, "world description must fit the kernel parameter space");
+
+namespace mg {
+
+static long long g_launches = 0;
+long long launch_count() { return g_launches; }
+static inline void count_launch() { __atomic_add_fetch(&g_launches, 1, __ATOMIC_RELAXED); }
+
+/* ============================================================================ per-seed setup */
+#define SETUP_NT 128
+/* Shuffle state of thread t: byte i lives in byte (i & 3) of word perm[i >> 2][t], so every access of a
+ * thread hits bank t % 32 whatever i is: the 32 lanes of a warp never conflict. */
+__device__ __forceinline__ void perm_identity(uint32_t (*perm)[SETUP_NT], int t) {
+    for (int w = 0; w < 64; w++) perm[w][t] = 0x03020100u + 0x04040404u * (uint32_t)w;
+}
+__device__ __forceinline__ void perm_swap(uint8_t *base, int t, int i, int j) {
+    uint8_t *a = base + (((i >> 2) * SETUP_NT + t) << 2) + (i & 3);
+    uint8_t *b = base + (((j >> 2) * SETUP_NT + t) << 2) + (j & 3);
+    uint8_t x = *a, y = *b;
+    *a = y;
+    *b = x;
+}
+__device__ __forceinline__ void perm_store(uint32_t (*perm)[SETUP_NT], int t, MgLattice *L) {
+    uint4 *dst = reinterpret_cast<uint4 *>(L->p);
+#pragma unroll 4
+    for (int q = 0; q < 16; q++) dst[q] = make_uint4(perm[4 * q][t], perm[4 * q + 1][t], perm[4 * q + 2][t], perm[4 * q + 3][t]);
+}
+__device__ __forceinline__ void header_store(MgLattice &h, MgLattice *L) {
+    lattice_header(h);
+    const uint4 *src = reinterpret_cast<const uint4 *>(&h);
+    uint4 *dst = reinterpret_cast<uint4 *>(L);
+#pragma unroll
+    for (int q = 0; q < 4; q++) dst[q] = src[q];
+}
+
+/* Overworld: lattice j of seed s; table layout noise-major, then stack, then level
+ * (engine/mc_climate.h:95-106, engine/mc_noise.h:255-265). */
+__global__ void __launch_bounds__(SETUP_NT) k_setup_xo(const __grid_constant__ MgWorldDesc W, const int64_t *__restrict__ seeds,
+                                                       int ns, MgLattice *__restrict__ out) {
+    __shared__ uint32_t perm[64][SETUP_NT];
+    const int t = threadIdx.x;
+    const int nt = W.ntables;
+    const long long g = (long long)blockIdx.x * SETUP_NT + t;
+    if (g >= (long long)ns * nt) return;
+    const int s = (int)(g / nt), j = (int)(g % nt);
+    int i = 0;
+    while (i < MG_OW_NOISES - 1 && j >= W.noise[i + 1].base) i++;
+    const MgNoise &N = W.noise[i];
+    const int r = j - N.base, st = r >= N.nlev, k = r - st * N.nlev;
+    Xo root = xo_from_seed(seeds[s]);
+    uint64_t plo = xo_next(root), phi = xo_next(root);   /* forkPositional */
+    Xo nr = xo_make(W.nhl[i] ^ plo, W.nhh[i] ^ phi);      /* fromHashOf("minecraft:<noise>") */
+    uint64_t a = xo_next(nr), b = xo_next(nr);            /* first stack's forkPositional */
+    if (st) { a = xo_next(nr); b = xo_next(nr); }         /* second stack's */
+    Xo x = xo_make(N.hlo[k] ^ a, N.hhi[k] ^ b);           /* fromHashOf("octave_<n>") */
+    MgLattice h;
+    h.ox = xo_double(x) * 256.0;
+    h.oy = xo_double(x) * 256.0;
+    h.oz = xo_double(x) * 256.0;
+    perm_identity(perm, t);
+    uint8_t *base = reinterpret_cast<uint8_t *>(&perm[0][0]);
+    for (int q = 0; q < 256; q++) perm_swap(base, t, q, q + xo_int(x, 256u - (uint32_t)q));
+    MgLattice *L = out + g;
+    header_store(h, L);
+    perm_store(perm, t, L);
+}
+
+/* one legacy lattice from the LCG into the thread's shuffle slot, then to `L` (if non-null) */
+__device__ __forceinline__ void legacy_lattice(uint64_t &s, uint32_t (*perm)[SETUP_NT], int t, MgLattice *L) {
+    MgLattice h;
+    h.ox = lcg_double(s) * 256.0;
+    h.oy = lcg_double(s) * 256.0;
+    h.oz = lcg_double(s) * 256.0;
+    perm_identity(perm, t);
+    uint8_t *base = reinterpret_cast<uint8_t *>(&perm[0][0]);
+    for (int q = 0; q < 256; q++) perm_swap(base, t, q, q + lcg_int(s, 256 - q));
+    if (L) {
+        header_store(h, L);
+        perm_store(perm, t, L);
+    }
+}
+/* Nether biome noises: temperature from LCG(seed), vegetation from LCG(seed + 1); each stack builds the
+ * zero octave first, then octaves zero-1 .. 0, skipping 262 draws for an absent one
+ * (engine/mc_noise.h:266-282, engine/cuda/mcg_host.c:49-51). */
+__global__ void __launch_bounds__(SETUP_NT) k_setup_legacy(const __grid_constant__ MgWorldDesc W, const int64_t *__restrict__ seeds,
+                                                           int ns, MgLattice *__restrict__ out) {
+    __shared__ uint32_t perm[64][SETUP_NT];
+    const int t = threadIdx.x;
+    const long long g = (long long)blockIdx.x * SETUP_NT + t;
+    if (g >= 2LL * ns) return;
+    const int s = (int)(g >> 1), n = (int)(g & 1);
+    const MgNoise &N = W.nether[n];
+    uint64_t st = lcg_init((int64_t)((uint64_t)seeds[s] + (uint64_t)n));
+    MgLattice *T = out + (size_t)s * W.ntables + N.base;
+    int slot[MG_MAX_OCT];
+    for (int q = 0; q < MG_MAX_OCT; q++) slot[q] = -1;
+    for (int k = 0; k < N.nlev; k++) slot[N.idx[k]] = k;
+    const int zero = -N.first;
+    for (int stack = 0; stack < 2; stack++) {
+        MgLattice *S = T + stack * N.nlev;
+        bool keep_zero = zero >= 0 && zero < N.octs && slot[zero] >= 0;
+        legacy_lattice(st, perm, t, keep_zero ? S + slot[zero] : nullptr);
+        for (int q = zero - 1; q >= 0; q--) {
+            if (q < N.octs && slot[q] >= 0) legacy_lattice(st, perm, t, S + slot[q]);
+            else st = lcg_jump(st, 262);
+        }
+    }
+}
+/* End: LegacyRandomSource(seed).consumeCount(17292), then the simplex lattice (engine/mc_end.h:18-22) */
+__global__ void __launch_bounds__(SETUP_NT) k_setup_end(const int64_t *__restrict__ seeds, int ns, MgLattice *__restrict__ out) {
+    __shared__ uint32_t perm[64][SETUP_NT];
+    const int t = threadIdx.x;
+    const long long g = (long long)blockIdx.x * SETUP_NT + t;
+    if (g >= ns) return;
+    uint64_t st = lcg_jump(lcg_init(seeds[g]), 17292);
+    legacy_lattice(st, perm, t, out + g);
+}
+
+/* ============================================================================ climate */
+/* Overworld climate of quart cell (qx, qy, qz) -> 6 quantised targets (engine/mc_climate.h:113-170). */
+template <bool FM>
+__device__ __forceinline__ void climate_ow(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
+                                           int qx, int qy, int qz, int32_t tg[6]) {
+    const double X = (double)qx, Z = (double)qz; /* blockX * 0.25 with blockX = 4 qx */
+    const double Xc = X * MG_SECOND_STACK, Zc = Z * MG_SECOND_STACK;
+    const int by = qy * 4;
+    if (FM) {
+        float sx = nn_f_y0(W.noise[0], T, X, Z, Xc, Zc) * 4.0f; /* ShiftA (x, 0, z) */
+        float sz = nn_f_z0(W.noise[0], T, Z, X, Zc, Xc) * 4.0f; /* ShiftB (z, x, 0) */
+        double x = X + (double)sx, z = Z + (double)sz;
+        double xc = x * MG_SECOND_STACK, zc = z * MG_SECOND_STACK;
+        float tv = nn_f_y0(W.noise[1], T, x, z, xc, zc);
+        float hv = nn_f_y0(W.noise[2], T, x, z, xc, zc);
+        float cv = nn_f_y0(W.noise[3], T, x, z, xc, zc);
+        float ev = nn_f_y0(W.noise[4], T, x, z, xc, zc);
+        float rv = nn_f_y0(W.noise[5], T, x, z, xc, zc);
+        float a = fabsf(rv) + W.rf_f[0];
+        float rf = (fabsf(a) + W.rf_f[1]) * W.rf_f[2];
+        float co[4] = {cv, ev, rv, rf};
+        float off = W.off_f + spline_eval(S, co);
+        int lo = min(W.grad_from_y, W.grad_to_y), hi = max(W.grad_from_y, W.grad_to_y);
+        int yy = by < lo ? lo : (by > hi ? hi : by);
+        float fac = (W.grad_to_f - W.grad_from_f) / (float)(W.grad_to_y - W.grad_from_y);
+        float depth = (W.grad_from_f + (float)(yy - W.grad_from_y) * fac) + off;
+        tg[0] = quantize(tv); tg[1] = quantize(hv); tg[2] = quantize(cv);
+        tg[3] = quantize(ev); tg[4] = quantize(depth); tg[5] = quantize(rv);
+    } else {
+        double sx = nn_d_y0(W.noise[0], T, X, Z, Xc, Zc) * 4.0;
+        double sz = nn_d_z0(W.noise[0], T, Z, X, Zc, Xc) * 4.0;
+        double x = X + sx, z = Z + sz;
+        double xc = x * MG_SECOND_STACK, zc = z * MG_SECOND_STACK;
+        double tv = nn_d_y0(W.noise[1], T, x, z, xc, zc);
+        double hv = nn_d_y0(W.noise[2], T, x, z, xc, zc);
+        double cv = nn_d_y0(W.noise[3], T, x, z, xc, zc);
+        double ev = nn_d_y0(W.noise[4], T, x, z, xc, zc);
+        double rv = nn_d_y0(W.noise[5], T, x, z, xc, zc);
+        double rf = (fabs(fabs(rv) + W.rf_d[0]) + W.rf_d[1]) * W.rf_d[2];
+        float co[4] = {(float)cv, (float)ev, (float)rv, (float)rf};
+        double off = 0.0 + (W.off_d + (double)spline_eval(S, co)) * 1.0;
+        double fac = ((double)by - (double)W.grad_from_y) / ((double)W.grad_to_y - (double)W.grad_from_y);
+        double g = fac < 0.0 ? W.grad_from_d
+                             : (fac > 1.0 ? W.grad_to_d : W.grad_from_d + fac * (W.grad_to_d - W.grad_from_d));
+        double depth = g + off;
+        tg[0] = quantize((float)tv); tg[1] = quantize((float)hv); tg[2] = quantize((float)cv);
+        tg[3] = quantize((float)ev); tg[4] = quantize((float)depth); tg[5] = quantize((float)rv);
+    }
+}
+/* Nether: temperature and vegetation at (x/4, 0, z/4) (engine/cuda/mcg_host.c:63-74) */
+template <bool FM>
+__device__ __forceinline__ void climate_nether(const MgWorldDesc &W, const MgLattice *__restrict__ T, int qx, int qz,
+                                               int32_t tg[6]) {
+    const double X = (double)qx, Z = (double)qz;
+    const double Xc = X * MG_SECOND_STACK, Zc = Z * MG_SECOND_STACK;
+    float t, h;
+    if (FM) {
+        t = nn_f_legacy_y0(W.nether[0], T, X, Z, Xc, Zc);
+        h = nn_f_legacy_y0(W.nether[1], T, X, Z, Xc, Zc);
+    } else {
+        t = (float)nn_d_y0(W.nether[0], T, X, Z, Xc, Zc);
+        h = (float)nn_d_y0(W.nether[1], T, X, Z, Xc, Zc);
+    }
+    tg[0] = quantize(t);
+    tg[1] = quantize(h);
+    tg[2] = tg[3] = tg[4] = tg[5] = 0;
+}
+template <bool FM, int DIM>
+__device__ __forceinline__ void cell_target(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
+                                            int qx, int qy, int qz, int32_t tg[6]) {
+    if (DIM == MG_OVERWORLD) climate_ow<FM>(W, S, T, qx, qy, qz, tg);
+    else climate_nether<FM>(W, T, qx, qz, tg);
+}
+
+/* ============================================================================ End islands (engine/mc_end.h) */
+__device__ __forceinline__ double simplex2(const uint8_t *__restrict__ p, double xin, double yin, double F2, double G2) {
+    double s = (xin + yin) * F2;
+    int i = ifloor(xin + s), j = ifloor(yin + s);
+    double t = (double)(i + j) * G2;
+    double x0 = xin - ((double)i - t), y0 = yin - ((double)j - t);
+    int i1 = x0 > y0 ? 1 : 0, j1 = 1 - i1;
+    double x1 = x0 - (double)i1 + G2, y1 = y0 - (double)j1 + G2;
+    double x2 = x0 - 1.0 + 2.0 * G2, y2 = y0 - 1.0 + 2.0 * G2;
+    int ii = i & 255, jj = j & 255;
+    int g0 = p[(ii + p[jj]) & 255] % 12;
+    int g1 = p[(ii + i1 + p[(jj + j1) & 255]) & 255] % 12;
+    int g2 = p[(ii + 1 + p[(jj + 1) & 255]) & 255] % 12;
+    double n = 0.0, acc[3];
+    const double xs[3] = {x0, x1, x2}, ys[3] = {y0, y1, y2};
+    const int gs[3] = {g0, g1, g2};
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        double tt = 0.5 - xs[c] * xs[c] - ys[c] * ys[c] - 0.0 * 0.0;
+        if (tt < 0.0) acc[c] = 0.0;
+        else {
+            tt *= tt;
+            acc[c] = tt * tt * gdot<double>(gs[c], xs[c], ys[c], 0.0);
+        }
+    }
+    n = acc[0] + acc[1] + acc[2];
+    return 70.0 * n;
+}
+__device__ __forceinline__ float clampf(float v, float lo, float hi) { return v < lo ? lo : (v < hi ? v : hi); }
+/* EndIslandDensityFunction.getHeightValue at (sx, sz) = (block / 8) */
+__device__ float end_height(const uint8_t *__restrict__ p, bool fm, int sx, int sz, double F2, double G2) {
+    int cx = sx / 2, cz = sz / 2, ox = sx % 2, oz = sz % 2;
+    float best;
+    if (!fm) {
+        int32_t sq = (int32_t)((uint32_t)sx * (uint32_t)sx + (uint32_t)sz * (uint32_t)sz); /* Java int overflow */
+        float len = (float)sqrt((double)(float)sq);
+        best = clampf(100.0f - len * 8.0f, -100.0f, 80.0f);
+    } else best = -100.0f;
+    for (int dx = -12; dx <= 12; dx++)
+        for (int dz = -12; dz <= 12; dz++) {
+            long long tx = (long long)cx + dx, tz = (long long)cz + dz;
+            if (tx * tx + tz * tz <= 4096LL) continue;
+            double nv = simplex2(p, (double)tx, (double)tz, F2, G2);
+            bool island = fm ? ((float)nv < -0.9f) : (nv < (double)-0.9f);
+            if (!island) continue;
+            float size = fmodf(fabsf((float)tx) * 3439.0f + fabsf((float)tz) * 147.0f, 13.0f) + 9.0f;
+            float xd = (float)(ox - dx * 2), zd = (float)(oz - dz * 2);
+            float h = clampf(100.0f - (float)sqrt((double)(xd * xd + zd * zd)) * size, -100.0f, 80.0f);
+            best = best > h ? best : h;
+        }
+    return best;
+}
+/* TheEndBiomeSource class of chunk (cx, cz): 0 the_end, 1 highlands, 2 midlands, 3 small islands, 4 barrens */
+__device__ int end_chunk_class(const uint8_t *__restrict__ p, bool fm, int cx, int cz, double F2, double G2) {
+    if ((long long)cx * cx + (long long)cz * cz <= 4096LL) return 0;
+    int bx = (cx * 2 + 1) * 8, bz = (cz * 2 + 1) * 8;
+    float h = end_height(p, fm, bx / 8, bz / 8, F2, G2);
+    double e;
+    if (!fm) e = ((double)h - 8.0) / 128.0;
+    else {
+        float dx = (float)(0 - bx), dz = (float)(0 - bz);
+        float len = (float)sqrt((double)(dx * dx + 0.0f * 0.0f + dz * dz));
+        float c = (clampf(100.0f - len, -100.0f, 80.0f) - 8.0f) * 0.0078125f;
+        float o = (h - 8.0f) / 128.0f;
+        e = (double)(c > o ? c : o);
+    }
+    if (e > 0.25) return 1;
+    if (e >= -0.0625) return 2;
+    return e < -0.21875 ? 3 : 4;
+}
+
+/* ============================================================================ sampling kernels */
+/* Stage the seed-independent spline and one seed's lattices in shared memory. */
+__device__ __forceinline__ void stage(const MgWorldDesc &W, const MgLattice *__restrict__ src, int n, MgLattice *dstT,
+                                      MgSpline *dstS, bool spline) {
+    const uint4 *a = reinterpret_cast<const uint4 *>(src);
+    uint4 *b = reinterpret_cast<uint4 *>(dstT);
+    for (int i = threadIdx.x; i < n * (int)(sizeof(MgLattice) / 16); i += blockDim.x) b[i] = a[i];
+    if (spline) {
+        const uint4 *c = reinterpret_cast<const uint4 *>(&W.spline);
+        uint4 *d = reinterpret_cast<uint4 *>(dstS);
+        for (int i = threadIdx.x; i < (int)(sizeof(MgSpline) / 16); i += blockDim.x) d[i] = c[i];
+    }
+}
+
+/* seeds x points, ENGINE rule.  One thread per sample; lattices of the sample's seed through L1. */
+template <bool FM, int DIM>
+__global__ void __launch_bounds__(128) k_points(const __grid_constant__ MgWorldDesc W, const MgTreeNode *__restrict__ tree,
+                                                const MgLattice *__restrict__ states, int ns,
+                                                const int32_t *__restrict__ pts, int np, uint8_t *__restrict__ out,
+                                                int32_t *__restrict__ targets) {
+    __shared__ MgSpline S;
+    if (DIM == MG_OVERWORLD) {
+        const uint4 *c = reinterpret_cast<const uint4 *>(&W.spline);
+        uint4 *d = reinterpret_cast<uint4 *>(&S);
+        for (int i = threadIdx.x; i < (int)(sizeof(MgSpline) / 16); i += blockDim.x) d[i] = c[i];
+        __syncthreads();
+    }
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (long long)ns * np) return;
+    const int s = (int)(g / np), p = (int)(g % np);
+    const int qx = pts[3 * p], qy = pts[3 * p + 1], qz = pts[3 * p + 2];
+    const MgLattice *T = states + (size_t)s * W.ntables;
+    int32_t tg[6];
+    if (DIM == MG_END) {
+        out[g] = (uint8_t)W.end_ids[end_chunk_class(T->p, FM, (qx * 4) >> 4, (qz * 4) >> 4, W.end_f2, W.end_g2)];
+        if (targets)
+            for (int k = 0; k < 6; k++) targets[g * 6 + k] = 0;
+        return;
+    }
+    cell_target<FM, DIM>(W, S, T, qx, qy, qz, tg);
+    uint64_t d;
+    int leaf = tree_search(tree, tg, -1, d);
+    out[g] = tree[leaf].biome;
+    if (targets)
+        for (int k = 0; k < 6; k++) targets[g * 6 + k] = tg[k];
+}
+
+/* One seed's quart grid.  ENGINE: biome ids.  GRID_CHAIN: first minimum leaf, its fitness, tie flag and
+ * the target of every cell, for k_chain_resolve. */
+struct ChainRec { int32_t tg[6]; uint64_t d; int32_t leaf; int32_t tie; };
+template <bool FM, int DIM, bool CHAIN>
+__global__ void __launch_bounds__(128) k_grid(const __grid_constant__ MgWorldDesc W, const MgTreeNode *__restrict__ tree,
+                                              const MgLattice *__restrict__ state, int qx0, int qz0, int nx, int nz,
+                                              int qy, uint8_t *__restrict__ out, ChainRec *__restrict__ rec) {
+    extern __shared__ uint4 smem_raw[];
+    MgSpline *S = reinterpret_cast<MgSpline *>(smem_raw);
+    MgLattice *T = reinterpret_cast<MgLattice *>(S + 1);
+    stage(W, state, W.ntables, T, S, DIM == MG_OVERWORLD);
+    __syncthreads();
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (long long)nx * nz) return;
+    const int ix = (int)(g % nx), iz = (int)(g / nx);
+    int32_t tg[6];
+    cell_target<FM, DIM>(W, *S, T, qx0 + ix, qy, qz0 + iz, tg);
+    uint64_t d;
+    int leaf = tree_search(tree, tg, -1, d);
+    out[g] = tree[leaf].biome;
+    if (CHAIN) {
+        ChainRec r;
+        for (int k = 0; k < 6; k++) r.tg[k] = tg[k];
+        r.d = d;
+        r.leaf = leaf;
+        r.tie = tree_count_at(tree, tg, d) >= 2;
+        rec[g] = r;
+    }
+}
+/* GRID_CHAIN: a tied cell takes the previous cell's leaf when that leaf is also at minimum fitness.
+ * Walk back to the nearest untied cell (whose leaf is its own first minimum) and replay forward. */
+__global__ void k_chain_resolve(const MgTreeNode *__restrict__ tree, const ChainRec *__restrict__ rec, long long n,
+                                uint8_t *__restrict__ out) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n || !rec[g].tie) return;
+    long long j = g - 1;
+    while (j >= 0 && rec[j].tie) j--;
+    int leaf = j >= 0 ? rec[j].leaf : -1;
+    for (long long k = j + 1; k <= g; k++) {
+        const ChainRec &r = rec[k];
+        if (leaf < 0 || node_dist(tree[leaf], r.tg) != r.d) leaf = r.leaf;
+    }
+    out[g] = tree[leaf].biome;
+}
+
+/* ---------------------------------------------------------------------------- BiomeManager zoom
+ * (libmcgen/src/region.c:61-85) */
+__device__ __forceinline__ int64_t zoom_step(int64_t r, int64_t c) {
+    uint64_t v = (uint64_t)r;
+    v *= v * 6364136223846793005ULL + 1442695040888963407ULL;
+    return (int64_t)(v + (uint64_t)c);
+}
+__device__ __forceinline__ double zoom_jitter(int64_t r) {
+    int64_t m = (r >> 24) % 1024;
+    if (m < 0) m += 1024;
+    return ((double)m / 1024.0 - 0.5) * 0.9;
+}
+__device__ __forceinline__ double zoom_dist(int64_t seed, int x, int y, int z, double dx, double dy, double dz) {
+    int64_t r = seed;
+    r = zoom_step(r, x); r = zoom_step(r, y); r = zoom_step(r, z);
+    r = zoom_step(r, x); r = zoom_step(r, y); r = zoom_step(r, z);
+    double jx = zoom_jitter(r);
+    r = zoom_step(r, seed);
+    double jy = zoom_jitter(r);
+    r = zoom_step(r, seed);
+    double jz = zoom_jitter(r);
+    return (dz + jz) * (dz + jz) + (dy + jy) * (dy + jy) + (dx + jx) * (dx + jx);
+}
+__device__ __forceinline__ void zoom_cell(int64_t zseed, int x, int y, int z, int &cx, int &cy, int &cz) {
+    int ax = x - 2, ay = y - 2, az = z - 2;
+    int px = ax >> 2, py = ay >> 2, pz = az >> 2;
+    double fx = (ax & 3) / 4.0, fy = (ay & 3) / 4.0, fz = (az & 3) / 4.0;
+    int best = 0;
+    double bd = __longlong_as_double(0x7FF0000000000000LL);
+    for (int i = 0; i < 8; i++) {
+        bool ex = (i & 4) == 0, ey = (i & 2) == 0, ez = (i & 1) == 0;
+        double d = zoom_dist(zseed, ex ? px : px + 1, ey ? py : py + 1, ez ? pz : pz + 1, ex ? fx : fx - 1.0,
+                             ey ? fy : fy - 1.0, ez ? fz : fz - 1.0);
+        if (bd > d) { best = i; bd = d; }
+    }
+    cx = (best & 4) == 0 ? px : px + 1;
+    cy = (best & 2) == 0 ? py : py + 1;
+    cz = (best & 1) == 0 ? pz : pz + 1;
+}
+/* world_biome_cell (libmcgen/src/biome.c:87-114): y clamped into the dimension; a tied cell walks back along
+ * LevelChunkSection.fillBiomesFromNoise order (sections bottom-up, then x, y, z) to an untied cell or the
+ * column's first cell, then replays the candidate chain forward.  The walk is bounded by the column. */
+template <bool FM, int DIM>
+__device__ int cell_chunk(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
+                          const MgTreeNode *__restrict__ tree, int qx, int qy, int qz) {
+    const int qmin = W.min_y >> 2, qh = W.height >> 2;
+    qy = qy < qmin ? qmin : (qy > qmin + qh - 1 ? qmin + qh - 1 : qy);
+    const int bx = qx & ~3, bz = qz & ~3, ly = qy - qmin;
+    const int idx0 = (ly >> 2) * 64 + (qx & 3) * 16 + (ly & 3) * 4 + (qz & 3);
+    int32_t tg[6];
+    uint64_t d;
+    int idx = idx0, leaf;
+    for (;;) {
+        int sec = idx >> 6, r = idx & 63;
+        cell_target<FM, DIM>(W, S, T, bx + (r >> 4), qmin + sec * 4 + ((r >> 2) & 3), bz + (r & 3), tg);
+        leaf = tree_search(tree, tg, -1, d);
+        if (idx == 0 || tree_count_at(tree, tg, d) < 2) break;
+        idx--;
+    }
+    for (int k = idx + 1; k <= idx0; k++) { /* replay the chain forward */
+        int sec = k >> 6, r = k & 63;
+        cell_target<FM, DIM>(W, S, T, bx + (r >> 4), qmin + sec * 4 + ((r >> 2) & 3), bz + (r & 3), tg);
+        int l0 = tree_search(tree, tg, -1, d);
+        if (node_dist(tree[leaf], tg) != d) leaf = l0;
+    }
+    return tree[leaf].biome;
+}
+/* mcgen_biome_grid: out[iz*nx+ix] = biome_at(x0 + ix*step, y, z0 + iz*step) (libmcgen/src/region.c:86-108) */
+template <bool FM, int DIM>
+__global__ void __launch_bounds__(128) k_blockgrid(const __grid_constant__ MgWorldDesc W, const MgTreeNode *__restrict__ tree,
+                                                   const MgLattice *__restrict__ state, int64_t zseed, int x0, int z0,
+                                                   int nx, int nz, int step, int y, const int32_t *__restrict__ xyz,
+                                                   uint8_t *__restrict__ out, const uint8_t *__restrict__ end_cls,
+                                                   int ecx0, int ecz0, int encx) {
+    extern __shared__ uint4 smem_raw[];
+    MgSpline *S = reinterpret_cast<MgSpline *>(smem_raw);
+    MgLattice *T = reinterpret_cast<MgLattice *>(S + 1);
+    if (DIM != MG_END) {
+        stage(W, state, W.ntables, T, S, DIM == MG_OVERWORLD);
+        __syncthreads();
+    }
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (long long)nx * nz) return;
+    int bxk, byk, bzk;
+    if (xyz) { bxk = xyz[3 * g]; byk = xyz[3 * g + 1]; bzk = xyz[3 * g + 2]; }
+    else { bxk = x0 + (int)(g % nx) * step; byk = y; bzk = z0 + (int)(g / nx) * step; }
+    int cx, cy, cz;
+    zoom_cell(zseed, bxk, byk, bzk, cx, cy, cz);
+    if (DIM == MG_END) {
+        int chx = (cx * 4) >> 4, chz = (cz * 4) >> 4;
+        int c = end_cls ? end_cls[(size_t)(chz - ecz0) * encx + (chx - ecx0)]
+                        : end_chunk_class(state->p, FM, chx, chz, W.end_f2, W.end_g2);
+        out[g] = (uint8_t)W.end_ids[c];
+        return;
+    }
+    out[g] = (uint8_t)cell_chunk<FM, DIM>(W, *S, T, tree, cx, cy, cz);
+}
+/* End class of chunks [cx0, cx0+ncx) x [cz0, cz0+ncz) */
+template <bool FM>
+__global__ void __launch_bounds__(128) k_end_chunks(const MgLattice *__restrict__ state, int cx0, int cz0, int ncx,
+                                                    int ncz, uint8_t *__restrict__ cls, double F2, double G2) {
+    __shared__ uint8_t p[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) p[i] = state->p[i];
+    __syncthreads();
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (long long)ncx * ncz) return;
+    cls[g] = (uint8_t)end_chunk_class(p, FM, cx0 + (int)(g % ncx), cz0 + (int)(g / ncx), F2, G2);
+}
+
+/* ============================================================================ host launchers */
+static inline unsigned blocks_for(long long n, int nt) { return (unsigned)((n + nt - 1) / nt); }
+static size_t grid_smem(const MgWorldDesc &W) { return sizeof(MgSpline) + (size_t)W.ntables * sizeof(MgLattice); }
+
+int launch_setup(const MgWorldDesc &W, const int64_t *d_seeds, int ns, MgLattice *d_states, cudaStream_t st) {
+    if (ns <= 0) return 0;
+    if (W.dim == MG_OVERWORLD) {
+        long long n = (long long)ns * W.ntables;
+        { ProfScope ps_(K_SETUP_XO, st); k_setup_xo<<<blocks_for(n, SETUP_NT), SETUP_NT, 0, st>>>(W, d_seeds, ns, d_states); }
+    } else if (W.dim == MG_NETHER) {
+        { ProfScope ps_(K_SETUP_LEGACY, st); k_setup_legacy<<<blocks_for(2LL * ns, SETUP_NT), SETUP_NT, 0, st>>>(W, d_seeds, ns, d_states); }
+    } else {
+        { ProfScope ps_(K_SETUP_END, st); k_setup_end<<<blocks_for(ns, SETUP_NT), SETUP_NT, 0, st>>>(d_seeds, ns, d_states); }
+    }
+    count_launch();
+    return (int)cudaGetLastError();
+}
+
+template <bool FM, int DIM>
+static void points_t(const MgWorldDesc &W, const MgTreeNode *tree, const MgLattice *states, int ns, const int32_t *pts,
+                     int np, uint8_t *out, int32_t *tg, cudaStream_t st) {
+    long long n = (long long)ns * np;
+    { ProfScope ps_(K_POINTS, st); k_points<FM, DIM><<<blocks_for(n, 128), 128, 0, st>>>(W, tree, states, ns, pts, np, out, tg); }
+}
+int launch_points(const MgWorldDesc &W, const MgTreeNode *tree, const MgLattice *states, int ns, const int32_t *pts,
+                  int np, uint8_t *out, int32_t *tg, cudaStream_t st) {
+    if ((long long)ns * np <= 0) return 0;
+    if (W.fmode) {
+        if (W.dim == MG_OVERWORLD) points_t<true, MG_OVERWORLD>(W, tree, states, ns, pts, np, out, tg, st);
+        else if (W.dim == MG_NETHER) points_t<true, MG_NETHER>(W, tree, states, ns, pts, np, out, tg, st);
+        else points_t<true, MG_END>(W, tree, states, ns, pts, np, out, tg, st);
+    } else {
+        if (W.dim == MG_OVERWORLD) points_t<false, MG_OVERWORLD>(W, tree, states, ns, pts, np, out, tg, st);
+        else if (W.dim == MG_NETHER) points_t<false, MG_NETHER>(W, tree, states, ns, pts, np, out, tg, st);
+        else points_t<false, MG_END>(W, tree, states, ns, pts, np, out, tg, st);
+    }
+    count_launch();
+    return (int)cudaGetLastError();
+}
+
+template <bool FM, int DIM, bool CHAIN>
+static void grid_t(const MgWorldDesc &W, const MgTreeNode *tree, const MgLattice *state, int qx0, int qz0, int nx, int nz,
+                   int qy, uint8_t *out, ChainRec *rec, cudaStream_t st) {
+    size_t sm = grid_smem(W);
+    cudaFuncSetAttribute(k_grid<FM, DIM, CHAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    { ProfScope ps_(K_GRID, st); k_grid<FM, DIM, CHAIN><<<blocks_for((long long)nx * nz, 128), 128, sm, st>>>(W, tree, state, qx0, qz0, nx, nz, qy, out, rec); }
+}
+__global__ void k_end_lookup(const __grid_constant__ MgWorldDesc W, const uint8_t *__restrict__ cls, int cx0, int cz0,
+                             int ncx, int qx0, int qz0, int nx, int nz, uint8_t *__restrict__ out) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (long long)nx * nz) return;
+    int qx = qx0 + (int)(g % nx), qz = qz0 + (int)(g / nx);
+    int cx = (qx * 4) >> 4, cz = (qz * 4) >> 4;
+    out[g] = (uint8_t)W.end_ids[cls[(size_t)(cz - cz0) * ncx + (cx - cx0)]];
+}
+int launch_end_lookup(const MgWorldDesc &W, const uint8_t *cls, int cx0, int cz0, int ncx, int qx0, int qz0, int nx,
+                      int nz, uint8_t *out, cudaStream_t st) {
+    { ProfScope ps_(K_END_LOOKUP, st); k_end_lookup<<<blocks_for((long long)nx * nz, 256), 256, 0, st>>>(W, cls, cx0, cz0, ncx, qx0, qz0, nx, nz, out); }
+    count_launch();
+    return (int)cudaGetLastError();
+}
+size_t chain_scratch_bytes(long long ncells) { return (size_t)ncells * sizeof(ChainRec); }
+int launch_quart_grid(const MgWorldDesc &W, const MgTreeNode *tree, const MgLattice *state, int qx0, int qz0, int nx, int nz, int qy, int rule, uint8_t *out, void *scratch, cudaStream_t st) {
+    long long n = (long long)nx * nz;
+    if (n <= 0) return 0;
+    if (W.dim == MG_END) {
+        /* chunk classes over the grid's chunk range, then one lookup per cell */
+        int cx0 = (qx0 * 4) >> 4, cz0 = (qz0 * 4) >> 4;
+        int cx1 = ((qx0 + nx - 1) * 4) >> 4, cz1 = ((qz0 + nz - 1) * 4) >> 4;
+        int ncx = cx1 - cx0 + 1, ncz = cz1 - cz0 + 1;
+        uint8_t *cls = (uint8_t *)scratch;
+        if (W.fmode) { ProfScope ps_(K_END_CHUNKS, st); k_end_chunks<true><<<blocks_for((long long)ncx * ncz, 128), 128, 0, st>>>(state, cx0, cz0, ncx, ncz, cls, W.end_f2, W.end_g2); }
+        else { ProfScope ps_(K_END_CHUNKS, st); k_end_chunks<false><<<blocks_for((long long)ncx * ncz, 128), 128, 0, st>>>(state, cx0, cz0, ncx, ncz, cls, W.end_f2, W.end_g2); }
+        count_launch();
+        return launch_end_lookup(W, cls, cx0, cz0, ncx, qx0, qz0, nx, nz, out, st);
+    }
+    bool chain = rule == MG_TIE_GRID_CHAIN;
+    ChainRec *rec = (ChainRec *)scratch;
+    if (W.fmode) {
+        if (W.dim == MG_OVERWORLD) {
+            if (chain) grid_t<true, MG_OVERWORLD, true>(W, tree, state, qx0, qz0, nx, nz, qy, out, rec, st);
+            else grid_t<true, MG_OVERWORLD, false>(W, tree, state, qx0, qz0, nx, nz, qy, out, rec, st);
+        } else {
+            if (chain) grid_t<true, MG_NETHER, true>(W, tree, state, qx0, qz0, nx, nz, qy, out, rec, st);
+            else grid_t<true, MG_NETHER, false>(W, tree, state, qx0, qz0, nx, nz, qy, out, rec, st);
+        }
+    } else {
+        if (W.dim == MG_OVERWORLD) {
+            if (chain) grid_t<false, MG_OVERWORLD, true>(W, tree, state, qx0, qz0, nx, nz, qy, out, rec, st);
+            else grid_t<false, MG_OVERWORLD, false>(W, tree, state, qx0, qz0, nx, nz, qy, out, rec, st);
+        } else {
+            if (chain) grid_t<false, MG_NETHER, true>(W, tree, state, qx0, qz0, nx, nz, qy, out, rec, st);
+            else grid_t<false, MG_NETHER, false>(W, tree, state, qx0, qz0, nx, nz, qy, out, rec, st);
+        }
+    }
+    count_launch();
+    if (chain) {
+        { ProfScope ps_(K_CHAIN_RESOLVE, st); k_chain_resolve<<<blocks_for(n, 256), 256, 0, st>>>(tree, rec, n, out); }
+        count_launch();
+    }
+    return (int)cudaGetLastError();
+}
+
+template <bool FM, int DIM>
+static void blockgrid_t(const MgWorldDesc &W, const MgTreeNode *tree, const MgLattice *state, int64_t zseed, int x0,
+                        int z0, int nx, int nz, int step, int y, const int32_t *xyz, uint8_t *out, const uint8_t *cls,
+                        int ecx0, int ecz0, int encx, cudaStream_t st) {
+    size_t sm = DIM == MG_END ? 0 : grid_smem(W);
+    if (sm) cudaFuncSetAttribute(k_blockgrid<FM, DIM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    ProfScope ps_(K_BLOCKGRID, st);
+    k_blockgrid<FM, DIM><<<blocks_for((long long)nx * nz, 128), 128, sm, st>>>(W, tree, state, zseed, x0, z0, nx, nz, step,
+                                                                            y, xyz, out, cls, ecx0, ecz0, encx);
+}
+/* Block-coordinate biomes: a grid (xyz == nullptr) or n = nx points (nz == 1) at xyz. For the End,
+ * `scratch` holds the chunk classes of [ecx0, ecx0+encx) x [ecz0, ecz0+encz). */
+int launch_block_biomes(const MgWorldDesc &W, const MgTreeNode *tree, const MgLattice *state, int64_t zseed, int x0,
+                        int z0, int nx, int nz, int step, int y, const int32_t *xyz, uint8_t *out, void *scratch,
+                        int ecx0, int ecz0, int encx, int encz, cudaStream_t st) {
+    if ((long long)nx * nz <= 0) return 0;
+    uint8_t *cls = (uint8_t *)scratch; /* End chunk classes, or null: evaluate per sample */
+    if (W.dim == MG_END && cls) {
+        if (W.fmode) { ProfScope ps_(K_END_CHUNKS, st); k_end_chunks<true><<<blocks_for((long long)encx * encz, 128), 128, 0, st>>>(state, ecx0, ecz0, encx, encz, cls, W.end_f2, W.end_g2); }
+        else { ProfScope ps_(K_END_CHUNKS, st); k_end_chunks<false><<<blocks_for((long long)encx * encz, 128), 128, 0, st>>>(state, ecx0, ecz0, encx, encz, cls, W.end_f2, W.end_g2); }
+        count_launch();
+    }
+    if (W.fmode) {
+        if (W.dim == MG_OVERWORLD) blockgrid_t<true, MG_OVERWORLD>(W, tree, state, zseed, x0, z0, nx, nz, step, y, xyz, out, cls, ecx0, ecz0, encx, st);
+        else if (W.dim == MG_NETHER) blockgrid_t<true, MG_NETHER>(W, tree, state, zseed, x0, z0, nx, nz, step, y, xyz, out, cls, ecx0, ecz0, encx, st);
+        else blockgrid_t<true, MG_END>(W, tree, state, zseed, x0, z0, nx, nz, step, y, xyz, out, cls, ecx0, ecz0, encx, st);
+    } else {
+        if (W.dim == MG_OVERWORLD) blockgrid_t<false, MG_OVERWORLD>(W, tree, state, zseed, x0, z0, nx, nz, step, y, xyz, out, cls, ecx0, ecz0, encx, st);
+        else if (W.dim == MG_NETHER) blockgrid_t<false, MG_NETHER>(W, tree, state, zseed, x0, z0, nx, nz, step, y, xyz, out, cls, ecx0, ecz0, encx, st);
+        else blockgrid_t<false, MG_END>(W, tree, state, zseed, x0, z0, nx, nz, step, y, xyz, out, cls, ecx0, ecz0, encx, st);
+    }
+    count_launch();
+    return (int)cudaGetLastError();
+}
+
+}  // namespace mg

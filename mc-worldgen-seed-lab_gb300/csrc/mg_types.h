@@ -1,0 +1,92 @@
+/* mg_types.h -- plain-old-data layouts shared by the host world builder and the sm_103a kernels.
+ *
+ * Everything here is seed-independent except MgLattice (one Perlin octave of one seed), which the
+ * per-seed setup kernel writes and the sampling kernels read.
+ */
+#ifndef MG_TYPES_H
+#define MG_TYPES_H
+#include <stdint.h>
+
+#define MG_MAX_OCT 12        /* octaves per NormalNoise stack (continentalness has 9) */
+#define MG_OW_NOISES 6       /* offset (shift), temperature, vegetation, continentalness, erosion, ridge */
+#define MG_MAX_TABLES 64     /* lattices per seed: Overworld 46, Nether 8, End 1 */
+#define MG_SPL_MP 128        /* offset-spline multipoint nodes (26.x: 53) */
+#define MG_SPL_PTS 512       /* offset-spline points (26.x: 253) */
+#define MG_SPL_CONST 512     /* offset-spline constant leaves (26.x: 201) */
+#define MG_TREE_DIMS 7
+
+enum { MG_OVERWORLD = 0, MG_NETHER = 1, MG_END = 2 };
+enum { MG_V26_1 = 0, MG_V26_2 = 1, MG_V26_3 = 2, MG_V26_4 = 3 };
+/* how equal-fitness leaves resolve (see include/mcgen_gb300.h) */
+enum { MG_TIE_ENGINE = 0, MG_TIE_GRID_CHAIN = 1, MG_TIE_CHUNK_CELL = 2 };
+
+/* One NormalNoise, seed-independent.  Level k of stack s uses lattice table base + s*nlev + k. */
+typedef struct {
+    int32_t nlev;       /* present octaves per stack */
+    int32_t legacy;     /* Nether biome noise: LCG init, stack-then-stack summation (float branch) */
+    int32_t base;       /* first table index of this noise inside a seed's lattice array */
+    int32_t octs;       /* amplitude-array length (legacy init walks it) */
+    int32_t first;      /* first octave */
+    int32_t idx[MG_MAX_OCT];       /* amplitude index of level k */
+    uint64_t hlo[MG_MAX_OCT], hhi[MG_MAX_OCT]; /* md5("octave_<n>") halves */
+    double freq[MG_MAX_OCT];       /* input factor of level k (a power of two) */
+    double amp_d[MG_MAX_OCT];      /* double branch: amplitude */
+    double vf_d[MG_MAX_OCT];       /* double branch: value factor of the level */
+    double vfac;                   /* double branch: NormalNoise value factor */
+    float amp_f[MG_MAX_OCT];       /* float branch: layer amplitude */
+} MgNoise;
+
+/* Offset spline (CubicSpline over continents, erosion, ridges, ridges_folded), float.
+ * A child reference c >= 0 names multipoint node c; c < 0 names constant ~c. */
+typedef struct __attribute__((aligned(16))) {
+    int32_t nmp, npt, nconst, root;
+    uint8_t coord[MG_SPL_MP];      /* 0 continents, 1 erosion, 2 ridges, 3 ridges_folded */
+    uint8_t npts[MG_SPL_MP];
+    uint16_t first[MG_SPL_MP];
+    float loc[MG_SPL_PTS];
+    float der[MG_SPL_PTS];
+    int16_t child[MG_SPL_PTS];
+    float cval[MG_SPL_CONST];
+} MgSpline;
+
+/* R-tree node on the device: children of a subtree are contiguous [first, first+count);
+ * a leaf has count == 0.  Bounds are quantised climate values (|v| <= 12000 in every table). */
+typedef struct {
+    int16_t lo[MG_TREE_DIMS];
+    int16_t hi[MG_TREE_DIMS];
+    uint16_t first;
+    uint8_t count;
+    uint8_t biome;
+} MgTreeNode;
+
+/* Seed-independent world description, copied once to the device. */
+typedef struct {
+    int32_t version, dim, fmode;   /* fmode 1: float branch (26.3+), 0: double branch */
+    int32_t min_y, height;
+    int32_t ntables;               /* lattices per seed */
+    MgNoise noise[MG_OW_NOISES];   /* Overworld */
+    uint64_t nhl[MG_OW_NOISES], nhh[MG_OW_NOISES]; /* md5("minecraft:<noise>") */
+    MgNoise nether[2];             /* Nether temperature, vegetation */
+    int32_t grad_from_y, grad_to_y;
+    double grad_from_d, grad_to_d, off_d;
+    double rf_d[3];
+    float grad_from_f, grad_to_f, off_f;
+    float rf_f[3];
+    int32_t end_ids[5];            /* the_end, end_highlands, end_midlands, small_end_islands, end_barrens */
+    double end_f2, end_g2;         /* 2-D simplex skew 0.5*(sqrt(3)-1) and unskew (3-sqrt(3))/6 */
+    int32_t tree_root, tree_nodes, tree_leaves;
+    MgSpline spline;
+} MgWorldDesc;
+
+/* One Perlin octave of one seed: offsets, the y/z lattice split of the offsets (used whenever
+ * that input coordinate is zero), and the permutation. 320 bytes, 16-byte aligned. */
+typedef struct __attribute__((aligned(16))) {
+    double ox, oy, oz;
+    double fyd, fzd;   /* oy - floor(oy), oz - floor(oz) (double branch) */
+    int32_t iy, iz;    /* floor(oy), floor(oz) */
+    float fy, fz;      /* (float)(oy - iy), (float)(oz - iz) (float branch) */
+    uint8_t pad[8];
+    uint8_t p[256];
+} MgLattice;
+
+#endif

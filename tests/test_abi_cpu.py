@@ -1,0 +1,127 @@
+"""C-ABI host-side tests (CPU only, no GPU compute).
+
+The library must build, load, and export every symbol include/*.h declares; host-side logic (data loading,
+argument checks, names, error codes) is exercised without launching a kernel.
+"""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+import __graft_entry__ as ge
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="session")
+def mg():
+    ge._build_module().build()
+    m = ge.package()
+    m.load()
+    return m
+
+
+def declared_symbols():
+    names = []
+    for h in ("mcgen.h", "mcgen_gb300.h"):
+        src = open(os.path.join(REPO, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names += re.findall(r"MCGEN_API\s+[^;(]*?\b(mcgen_\w+)\s*\(", src)
+    return sorted(set(names))
+
+
+def test_exports_every_declared_symbol(mg):
+    lib = C.CDLL(mg.LIB_PATH)
+    names = declared_symbols()
+    assert len(names) >= 50
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_version(mg):
+    L = mg.load()
+    assert L.mcgen_abi_version() == 1
+    assert b"abi 1" in L.mcgen_version()
+
+
+def test_open_errors(mg):
+    with pytest.raises(mg.McError) as e:
+        mg.Generator.open(ge.data_root(), "25.9")
+    assert e.value.code == mg.MCGEN_E_VERSION
+    with pytest.raises(mg.McError) as e:
+        mg.Generator.open("/nonexistent-data-root", "26.3")
+    assert e.value.code == mg.MCGEN_E_IO
+
+
+@pytest.mark.parametrize("version", ["26.1", "26.2", "26.3", "26.4-snapshot-2"])
+def test_names_and_presets(mg, version):
+    g = mg.Generator.open(ge.data_root(), version)
+    assert g.dimensions() == ["minecraft:overworld", "minecraft:the_nether", "minecraft:the_end"]
+    assert g.presets("minecraft:overworld") == ["normal", "amplified", "large_biomes"]
+    assert g.presets("minecraft:the_nether") == ["normal"]
+    names = g.biome_names()
+    assert len(names) == 67 and names[0] == "minecraft:badlands" and names[41] == "minecraft:plains"
+    L = mg.load()
+    assert L.mcgen_block_state_count(g._h) == 0 and L.mcgen_tweak_count(g._h) == 0
+
+
+def test_world_new_errors(mg):
+    g = mg.Generator.open(ge.data_root(), "26.3")
+    with pytest.raises(mg.McError) as e:
+        g.world("minecraft:overworld_caves", "normal", 1)
+    assert e.value.code == mg.MCGEN_E_ARG
+    with pytest.raises(mg.McError) as e:
+        g.world("minecraft:the_nether", "amplified", 1)
+    assert e.value.code == mg.MCGEN_E_ARG
+    w = g.world("minecraft:overworld", "large_biomes", 7)
+    assert (w.min_y, w.height, w.sea_level) == (-64, 384, 63)
+    n = g.world("minecraft:the_nether", None, 7)
+    assert (n.min_y, n.height, n.sea_level) == (0, 256, 32)
+
+
+def test_world_info(mg):
+    g = mg.Generator.open(ge.data_root(), "26.1")
+    w = g.world("overworld", "normal", -42)
+    v, d, s, f = C.c_int(), C.c_int(), C.c_int64(), C.c_int()
+    assert mg.load().mcgen_gb300_world_info(w.handle, C.byref(v), C.byref(d), C.byref(s), C.byref(f)) == 0
+    assert (v.value, d.value, s.value, f.value) == (0, 0, -42, 0)
+
+
+def test_no_cpu_path(mg):
+    """Biomes are computed on the GPU only: the CPU entry points refuse loudly."""
+    g = mg.Generator.open(ge.data_root(), "26.3")
+    w = g.world("minecraft:overworld", "normal", 1)
+    L = mg.load()
+    buf = (C.c_uint8 * 4)()
+    assert L.mcgen_biome_grid_cpu(w.handle, 0, 0, 2, 2, 4, 64, C.cast(buf, C.c_void_p)) == mg.MCGEN_E_UNSUPPORTED
+    assert L.mcgen_gpu_set_compute(mg.MCGEN_COMPUTE_CPU, -1) == mg.MCGEN_E_UNSUPPORTED
+    out = C.c_void_p()
+    assert L.mcgen_generate_region(w.handle, 0, 0, 1, 1, 1, 0, None, None, C.byref(out), None, 0) == mg.MCGEN_E_UNSUPPORTED
+
+
+def test_argument_checks(mg):
+    g = mg.Generator.open(ge.data_root(), "26.3")
+    w = g.world("minecraft:overworld", "normal", 1)
+    L = mg.load()
+    buf = (C.c_uint8 * 4)()
+    p = C.cast(buf, C.c_void_p)
+    assert L.mcgen_biome_grid(w.handle, 0, 0, 0, 2, 4, 64, p) == mg.MCGEN_E_ARG
+    assert L.mcgen_biome_grid(w.handle, 0, 0, 2, 2, 0, 64, p) == mg.MCGEN_E_ARG
+    assert L.mcgen_biome_grid(None, 0, 0, 2, 2, 4, 64, p) == mg.MCGEN_E_ARG
+    assert L.mcgen_biome_grid(w.handle, 0, 0, 2, 2, 4, 64, None) == mg.MCGEN_E_ARG
+    assert L.mcgen_gb300_quart_grid(w.handle, 0, 0, 2, 2, 16, 7, p) == mg.MCGEN_E_ARG
+    assert L.mcgen_biome_at(None, 0, 0, 0) == -1
+
+
+@pytest.mark.skipif(ge.package().device_count() > 0 if os.path.exists(ge.package().LIB_PATH) else False,
+                    reason="a CUDA device is present")
+def test_no_device_fails_loudly(mg):
+    g = mg.Generator.open(ge.data_root(), "26.3")
+    w = g.world("minecraft:overworld", "normal", 1)
+    with pytest.raises(mg.McError) as e:
+        w.biome_grid(0, 0, 4, 4, 4, 64)
+    assert e.value.code == mg.MCGEN_E_UNSUPPORTED
+    assert w.biome_at(0, 64, 0) == -1
+    ok, status = mg.gpu_status()
+    assert not ok and "unavailable" in status

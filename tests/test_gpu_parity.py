@@ -1,0 +1,185 @@
+"""GPU parity: the sm_103a kernels, called through the C ABI, against the oracle and the golden fixtures.
+
+Bit-exact for every id and quantised target.  Cases follow the reference's own tests: the Java-oracle
+golden vectors (climate rows, FNV grid digests, zoom rows), the reference engine's random seed x point
+tables (every version, dimension and Overworld preset), and the reference GPU test's method of many
+seeds x points at growing coordinate scales (crack/src/gpu_biomes/test_gpu_biomes.cu:18,56-75).
+"""
+import numpy as np
+import pytest
+
+import __graft_entry__ as ge
+from golden_io import VERSIONS, grid_hashes, misc, parse_refpoint_name, refpoint_files, tsv_rows
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+ALL_VERSIONS = VERSIONS + ["26.4-snapshot-2"]
+
+
+@pytest.fixture(scope="module")
+def mg():
+    m = ge.package()
+    m.load()
+    if m.device_count() < 1:
+        pytest.fail("no CUDA device: the GPU tests need one (there is no CPU path)")
+    return m
+
+
+@pytest.fixture(scope="module")
+def gens(mg):
+    return {v: mg.Generator.open(ge.data_root(), v) for v in ALL_VERSIONS}
+
+
+NAMES = ["minecraft:" + n for n in O.biome_names()]
+
+
+@pytest.mark.parametrize("path", refpoint_files(), ids=lambda p: p.rsplit("/", 1)[1][10:-4])
+def test_reference_engine_points(gens, path):
+    """Seeds x quart points from the reference engine's own CPU path: biome ids and targets."""
+    version, dim, preset = parse_refpoint_name(path)
+    z = np.load(path)
+    w = gens[version].world("minecraft:" + dim, preset, 0)
+    b, tg = w.seed_points(z["seeds"], z["pts"], want_targets=True)
+    assert np.array_equal(b, z["biome"]), int((b != z["biome"]).sum())
+    if dim != "the_end":
+        assert np.array_equal(tg, z["targets"])
+
+
+@pytest.mark.parametrize("version", VERSIONS)
+@pytest.mark.parametrize("dim", ["overworld", "the_nether", "the_end"])
+def test_golden_climate_rows(gens, version, dim):
+    """Java-oracle climate rows: 6 targets exact; biome exact or an R-tree fitness tie."""
+    rows = tsv_rows(version, f"climate_{dim}.tsv")
+    w = gens[version].world("minecraft:" + dim, "normal", 0)
+    ow = O.World(ge.data_root(), version, dim)
+    by_seed = {}
+    for r in rows:
+        by_seed.setdefault(int(r[0]), []).append(r)
+    mism = 0
+    for seed, rs in by_seed.items():
+        pts = np.array([[int(r[1]), int(r[2]), int(r[3])] for r in rs], np.int32)
+        b, tg = w.seed_points(np.array([seed], np.int64), pts, want_targets=True)
+        for i, r in enumerate(rs):
+            name = r[6] if dim == "the_end" else r[10]
+            if dim != "the_end":
+                assert list(tg[0, i]) == [int(x) for x in r[4:10]], r
+            if NAMES[b[0, i]] != name:
+                _, _, nmin = ow.tree_find(tg[0, i].astype(np.int64))
+                assert dim != "the_end" and nmin >= 2, r
+                mism += 1
+    assert mism <= 2
+
+
+@pytest.mark.parametrize("version", VERSIONS)
+def test_golden_grid_hashes(gens, version):
+    """All FNV-1a64 digests of the golden 1024^2 (End 512^2) quart grids, GRID_CHAIN tie rule."""
+    n = 0
+    for dim, seed, qx0, qz0, size, qy, h in grid_hashes(version):
+        w = gens[version].world("minecraft:" + dim, "normal", seed)
+        g = w.quart_grid(qx0, qz0, size, size, qy, ge.package().TIE_GRID_CHAIN)
+        assert O.fnv1a64_names(g) == h, (dim, seed)
+        n += 1
+    assert n == 18
+
+
+@pytest.mark.parametrize("version", VERSIONS)
+def test_golden_blockbiome(gens, version):
+    """BiomeManager zoom rows (blockbiome) through mcgen_biome_at."""
+    for d in misc(version, "blockbiome"):
+        w = gens[version].world("minecraft:" + d["dim"], d.get("preset", "normal"), d["seed"])
+        assert NAMES[w.biome_at(d["x"], d["y"], d["z"])] == d["biome"], d
+
+
+@pytest.mark.parametrize("version", ALL_VERSIONS)
+@pytest.mark.parametrize("dim", ["overworld", "the_nether", "the_end"])
+def test_biome_grid_dropin(gens, version, dim):
+    """mcgen_biome_grid (zoom + chunk-cell ties) against the oracle: step 4 at y=64, a step-1 patch at a
+    negative corner, and a sparse large-coordinate grid."""
+    for seed, args in ((12345, (-512, -512, 64, 64, 4, 64)), (-7, (-1000, -37, 40, 24, 1, -50)),
+                       (2**63 - 1, (-9_000_000, 5_000_000, 16, 16, 1_000_003, 100))):
+        w = gens[version].world("minecraft:" + dim, "normal", seed)
+        got = w.biome_grid(*args)
+        exp = O.World(ge.data_root(), version, dim).biome_grid(seed, *args)
+        assert np.array_equal(got, exp), (seed, args, int((got != exp).sum()))
+
+
+@pytest.mark.parametrize("version", ["26.1", "26.3"])
+@pytest.mark.parametrize("preset", ["amplified", "large_biomes"])
+def test_biome_grid_presets(gens, version, preset):
+    w = gens[version].world("minecraft:overworld", preset, 99)
+    got = w.biome_grid(-300, 200, 48, 48, 8, 70)
+    exp = O.World(ge.data_root(), version, "overworld", preset).biome_grid(99, -300, 200, 48, 48, 8, 70)
+    assert np.array_equal(got, exp)
+
+
+@pytest.mark.parametrize("version", ALL_VERSIONS)
+def test_block_points(gens, version):
+    """mcgen_gpu_biome_points at random block points, including world-height extremes (y clamp)."""
+    rng = np.random.default_rng(11)
+    for dim in ("overworld", "the_nether", "the_end"):
+        w = gens[version].world("minecraft:" + dim, "normal", 8675309)
+        xyz = np.stack([rng.integers(-200000, 200000, 300), rng.integers(-200, 500, 300),
+                        rng.integers(-200000, 200000, 300)], 1).astype(np.int32)
+        got = w.biome_points(xyz)
+        exp = O.World(ge.data_root(), version, dim).block_points(8675309, xyz)
+        assert np.array_equal(got, exp), dim
+
+
+@pytest.mark.parametrize("version", ["26.1", "26.3"])
+@pytest.mark.parametrize("dim", ["overworld", "the_nether", "the_end"])
+def test_quart_grid_engine(gens, version, dim):
+    w = gens[version].world("minecraft:" + dim, "normal", 4242)
+    got = w.quart_grid(-200, 100, 96, 80, 16, ge.package().TIE_ENGINE)
+    exp = O.World(ge.data_root(), version, dim).quart_grid(4242, -200, 100, 96, 80, 16, O.TIE_ENGINE)
+    assert np.array_equal(got, exp)
+
+
+@pytest.mark.parametrize("version", ["26.1", "26.3"])
+def test_many_seeds_scales(gens, version):
+    """The reference GPU test's shape: edge seeds + random seeds x points at four coordinate scales,
+    up to +-7.5M quarts (crack/src/gpu_biomes/test_gpu_biomes.cu:18,56-63)."""
+    rng = np.random.default_rng(3)
+    seeds = np.concatenate([np.array([0, 1, -1, 2**63 - 1, -2**63, 12345, 1 << 32, -(1 << 48), 0x5DEECE66D], np.int64),
+                            rng.integers(-2**63, 2**63 - 1, 503, dtype=np.int64)])
+    for scale in (64, 4096, 262144, 7_500_000):
+        pts = np.stack([rng.integers(-scale, scale, 16), rng.integers(-16, 80, 16), rng.integers(-scale, scale, 16)], 1)
+        for dim in ("overworld", "the_nether"):
+            w = gens[version].world("minecraft:" + dim, "normal", 0)
+            b, tg = w.seed_points(seeds, pts, want_targets=True)
+            eb, etg = O.World(ge.data_root(), version, dim).points(seeds, pts, want_targets=True)
+            assert np.array_equal(tg, etg), (scale, dim)
+            assert np.array_equal(b, eb), (scale, dim)
+
+
+def test_config1_dropin_full(gens):
+    """Overworld 26.3, seed 12345, 256x256 cells x,z in [-512,512) step 4 at y=64: the drop-in form of
+    the plain-method workload, bit-exact against the oracle."""
+    w = gens["26.3"].world("minecraft:overworld", "normal", 12345)
+    got = w.biome_grid(-512, -512, 256, 256, 4, 64)
+    exp = O.World(ge.data_root(), "26.3", "overworld").biome_grid(12345, -512, -512, 256, 256, 4, 64)
+    assert np.array_equal(got, exp)
+
+
+def test_config2_shape(gens):
+    """65,536 SplitMix64 seeds x 8 points (Overworld 26.3): a 4,096-seed stride sample bit-exact against
+    the oracle, and the full batch deterministic across calls."""
+    import bench
+
+    seeds, pts = bench.config2_inputs()
+    w = gens["26.3"].world("minecraft:overworld", "normal", 0)
+    a = w.seed_points(seeds, pts)
+    b = w.seed_points(seeds, pts)
+    assert np.array_equal(a, b)
+    sub = np.arange(0, len(seeds), 16)
+    exp = O.World(ge.data_root(), "26.3", "overworld").points(seeds[sub], pts)
+    assert np.array_equal(a[sub], exp)
+
+
+def test_edge_sizes(gens):
+    w = gens["26.3"].world("minecraft:overworld", "normal", 1)
+    one = w.biome_grid(5, 5, 1, 1, 1, 64)
+    assert one.shape == (1, 1) and one[0, 0] == w.biome_at(5, 64, 5)
+    assert w.seed_points(np.zeros(0, np.int64), np.zeros((3, 3), np.int32)).shape == (0, 3)
+    row = w.quart_grid(0, 0, 1000, 1, 16, 0)
+    exp = O.World(ge.data_root(), "26.3", "overworld").quart_grid(1, 0, 0, 1000, 1, 16)
+    assert np.array_equal(row, exp)
