@@ -52,6 +52,18 @@ MCGEN_API int mcgen_gb300_biome_grid_dev(const McWorld *w, int x0, int z0, int n
 MCGEN_API int mcgen_gb300_quart_grid_dev(const McWorld *w, int qx0, int qz0, int nx, int nz, int qy, int tie_rule,
                                          uint8_t *d_out, void *stream);
 
+/* Allocation-free form of mcgen_gb300_seed_points_dev, for callers that cannot let a library allocate
+ * device memory (their own memory arena, latency-critical loops, no allocation after set-up).  No
+ * counterpart in the reference.  The per-seed noise lattices go to one fixed 16 MiB device array inside
+ * the library instead of per-call scratch, so ns * (lattices per seed) * 320 bytes must fit: at most 1,139
+ * Overworld, 6,553 Nether or 52,428 End seeds per call; larger calls return MCGEN_E_ARG (split them).
+ * The caller passes device inputs and outputs as for _dev.  The world must already be on the device (any
+ * earlier biome call on it puts it there), else MCGEN_E_ARG.  The first call on a device looks up the
+ * array's address; make it before any stream capture.  Calls share the array: calls whose GPU work
+ * overlaps race on it. */
+MCGEN_API int mcgen_gb300_seed_points_noalloc(const McWorld *w, const int64_t *d_seeds, int ns, const int32_t *d_qxyz,
+                                              int np, uint8_t *d_out, int32_t *d_targets, void *stream);
+
 /* Number of kernel launches the library issued since load (for launch accounting in benchmarks). */
 MCGEN_API long long mcgen_gb300_launch_count(void);
 

@@ -83,6 +83,7 @@ _PROTOS = {
     "mcgen_gb300_seed_points": (C.c_int, [_P, _P, C.c_int, _P, C.c_int, _P, _P]),
     "mcgen_gb300_seed_points_dev": (C.c_int, [_P, _P, C.c_int, _P, C.c_int, _P, _P, _P]),
     "mcgen_gb300_biome_grid_dev": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _P, _P]),
+    "mcgen_gb300_seed_points_noalloc": (C.c_int, [_P, _P, C.c_int, _P, C.c_int, _P, _P, _P]),
     "mcgen_gb300_launch_count": (C.c_longlong, []),
     "mcgen_gb300_last_error": (C.c_char_p, []),
     "mcgen_gb300_profile": (C.c_int, [C.c_int]),

@@ -17,28 +17,10 @@
 
 #include "../../include/mcgen.h"
 #include "../../include/mcgen_gb300.h"
+#include "abi_internal.h"
 #include "launch.h"
 #include "prof.h"
 #include "world.h"
-
-struct McGen {
-    int version;
-    std::string root;
-};
-
-struct McWorld {
-    McGen *g;
-    int dim;
-    std::string preset;
-    McSeeds seeds;
-    int64_t zoom_seed;
-    MgWorldDesc desc;
-    std::vector<MgTreeNode> tree;
-    /* device copies, created on first GPU use */
-    int dev_ready;
-    MgTreeNode *d_tree;
-    MgLattice *d_state;
-};
 
 namespace {
 
@@ -180,6 +162,11 @@ int block_biomes_dev(const McWorld *w, int x0, int z0, int nx, int nz, int step,
 }
 
 }  // namespace
+
+namespace mg {
+std::mutex &abi_lock() { return g_lock; }
+int abi_device() { return g_device; }
+}  // namespace mg
 
 /* ============================================================================ version, data */
 extern "C" {
