@@ -153,7 +153,7 @@ def run_gb300(args, rank, world, local_rank):
     dev = torch.device("cuda", local_rank)
     gen = mg.Generator.open(ge.data_root(), "26.3")
     if args.workload == "seeds8":
-        seeds, pts = config2_inputs()
+        seeds, pts = config2_inputs(args.seeds)
         w = gen.world("minecraft:overworld", "normal", 0)
         samples = seeds.size * len(pts)
         d_seeds = torch.from_numpy(seeds).to(dev)
@@ -250,15 +250,16 @@ def run_gb300(args, rank, world, local_rank):
     value = samples * args.steps * world / (ms_max * 1e-3)
 
     # end to end through the host-buffer C ABI (pinned host memory, copies inside the timed region)
-    for _ in range(max(1, args.warmup)):
-        host_step()
+    if not args.skip_extras:
+        for _ in range(max(1, args.warmup)):
+            host_step()
     barrier()
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(0 if args.skip_extras else args.steps):
         host_step()
     torch.cuda.synchronize(dev)
-    e2e_s = time.perf_counter() - t0
+    e2e_s = max(time.perf_counter() - t0, 1e-9)
     te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
     if world > 1:
         torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
@@ -276,13 +277,13 @@ def run_gb300(args, rank, world, local_rank):
         clocks = clk.summary()
         if clocks:
             out["clocks"] = clocks
-        peaks = gpu_peaks(mg)
+        peaks = gpu_peaks(mg) if not args.skip_extras else {}
         out["pipe_peaks_gops"] = peaks
         if prof:
             top = max(prof, key=lambda k: prof[k][0])
             wk = kernel_work(top, args.workload == "seeds8", int(seeds.size), int(len(pts)), nt)
             avg_s = prof[top][0] / prof[top][1] * 1e-3
-            if wk:
+            if wk and peaks:
                 ops, unit, peak_key = wk
                 achieved = ops / avg_s / 1e9
                 out["roofline"] = {"kernel": top, "bound": peak_key, "achieved": round(achieved, 1),
@@ -291,7 +292,8 @@ def run_gb300(args, rank, world, local_rank):
             else:
                 out["roofline"] = {"kernel": top, "bound": None, "achieved": None, "peak": None, "unit": None,
                                    "frac": None, "traffic": None}
-        out["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_sample_s)
+        if not args.skip_extras:
+            out["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_sample_s)
         print(json.dumps(out), flush=True)
 
 
@@ -369,6 +371,9 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=["seeds8", "grid256"], default="seeds8")
     ap.add_argument("--cpu-sample-s", type=float, default=12.0)
+    ap.add_argument("--seeds", type=int, default=65536, help="seeds8: number of seeds (65536 = the configuration)")
+    ap.add_argument("--skip-extras", action="store_true",
+                    help="profiling runs: no e2e pass, no pipe peaks, no CPU baseline")
     args = ap.parse_args()
     rank, world, local_rank = dist_env()
     if args.impl == "reference":

@@ -77,6 +77,13 @@ MCGEN_API int mcgen_gb300_profile_read(int kernel, const char **name, double *to
 /* Last CUDA error text seen by the library (empty when none). */
 MCGEN_API const char *mcgen_gb300_last_error(void);
 
+/* Device self-check of the exact integer coordinate split used by every octave sample: n generated
+ * inputs (quart coordinates, shifted and second-stack coordinates, tiny/huge values, sums landing on or
+ * near integers and in (-1, 0), edge offsets) through both the fast split and the plain double arithmetic
+ * of the reference; *bad_f / *bad_d count differing results of the float (26.3) and double (26.1/26.2)
+ * branches.  Same seed, same inputs. */
+MCGEN_API int mcgen_gb300_check_split(long long n, unsigned long long seed, long long *bad_f, long long *bad_d);
+
 /* Pipe microbenchmarks on the current device, in giga-operations per second:
  * 0 FP32 FMA, 1 FP64 FMA, 2 FP64 add, 3 int32 multiply-add, 4 double->int floor conversion,
  * 5 int->double conversion, 6 double->float conversion, 7 64-bit wide integer multiply-add. */

@@ -90,6 +90,8 @@ _PROTOS = {
     "mcgen_gb300_profile_read": (C.c_int, [C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_double),
                                            C.POINTER(C.c_longlong)]),
     "mcgen_gb300_pipe_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+    "mcgen_gb300_check_split": (C.c_int, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong),
+                                          C.POINTER(C.c_longlong)]),
 }
 
 _lib = None
@@ -160,6 +162,13 @@ def profile_read() -> dict:
             out[name.value.decode()] = (ms.value, n.value)
         k += 1
     return out
+
+
+def check_split(n: int, seed: int = 1) -> tuple[int, int]:
+    """Mismatches (float branch, double branch) of the fast coordinate split against the plain one."""
+    bf, bd = C.c_longlong(), C.c_longlong()
+    _check(load().mcgen_gb300_check_split(n, seed, C.byref(bf), C.byref(bd)), "mcgen_gb300_check_split")
+    return bf.value, bd.value
 
 
 def pipe_rate(pipe: str) -> float:

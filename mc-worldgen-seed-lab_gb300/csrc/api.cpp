@@ -477,6 +477,13 @@ MCGEN_API int mcgen_gb300_quart_grid_dev(const McWorld *w, int qx0, int qz0, int
 
 static int seed_points_on(const McWorld *w, const int64_t *d_seeds, int ns, const int32_t *d_pts, int np,
                           uint8_t *d_out, int32_t *d_tg, cudaStream_t st) {
+    if (mg::fused_supported(w->desc)) { /* Overworld: lattices built and sampled on chip */
+        DevBuf clim(st);
+        cudaError_t e = clim.alloc(mg::fused_scratch_bytes(w->desc, (long long)ns * np));
+        if (e) return cuda_code(e);
+        int rc = mg::launch_ow_seed_points(w->desc, w->d_tree, d_seeds, ns, d_pts, np, d_out, d_tg, clim.p, st);
+        return rc ? cuda_code((cudaError_t)rc) : MCGEN_OK;
+    }
     DevBuf states(st);
     cudaError_t e = states.alloc(sizeof(MgLattice) * (size_t)ns * (size_t)w->desc.ntables);
     if (e) return cuda_code(e);

@@ -119,24 +119,44 @@ __device__ __forceinline__ T fade(T t) {
 template <typename T>
 __device__ __forceinline__ T lerp(T t, T a, T b) { return a + t * (b - a); }
 
+/* Permutation access: a plain 256-byte table, or a thread's own table in the interleaved shared layout
+ * (byte i of thread t in byte i & 3 of word [i >> 2][t]; every access of a thread hits bank t % 32). */
+struct PlainPerm {
+    const uint8_t *p;
+    __device__ __forceinline__ int operator()(int i) const { return p[i & 255]; }
+};
+template <int NT>
+struct IlvPerm {
+    const uint8_t *base; /* start of the [64][NT] word array */
+    int t;
+    __device__ __forceinline__ int operator()(int i) const {
+        i &= 255;
+        return base[((((i >> 2) * NT) + t) << 2) | (i & 3)];
+    }
+};
+
 /* ImprovedNoise.sampleAndLerp with split coordinates (engine/mc_noise.h:54-75 / 90-110). */
-template <typename T>
-__device__ __forceinline__ T octave(const uint8_t *__restrict__ p, int ix, T fx, int iy, T fy, int iz, T fz) {
-    int a = p[ix & 255], b = p[(ix + 1) & 255];
-    int aa = p[(a + iy) & 255], ab = p[(a + iy + 1) & 255];
-    int ba = p[(b + iy) & 255], bb = p[(b + iy + 1) & 255];
+template <typename T, typename P>
+__device__ __forceinline__ T octave_p(const P &p, int ix, T fx, int iy, T fy, int iz, T fz) {
+    int a = p(ix), b = p(ix + 1);
+    int aa = p(a + iy), ab = p(a + iy + 1);
+    int ba = p(b + iy), bb = p(b + iy + 1);
     T gx = fx - (T)1, gy = fy - (T)1, gz = fz - (T)1;
-    T c000 = gdot<T>(p[(aa + iz) & 255], fx, fy, fz);
-    T c100 = gdot<T>(p[(ba + iz) & 255], gx, fy, fz);
-    T c010 = gdot<T>(p[(ab + iz) & 255], fx, gy, fz);
-    T c110 = gdot<T>(p[(bb + iz) & 255], gx, gy, fz);
-    T c001 = gdot<T>(p[(aa + iz + 1) & 255], fx, fy, gz);
-    T c101 = gdot<T>(p[(ba + iz + 1) & 255], gx, fy, gz);
-    T c011 = gdot<T>(p[(ab + iz + 1) & 255], fx, gy, gz);
-    T c111 = gdot<T>(p[(bb + iz + 1) & 255], gx, gy, gz);
+    T c000 = gdot<T>(p(aa + iz), fx, fy, fz);
+    T c100 = gdot<T>(p(ba + iz), gx, fy, fz);
+    T c010 = gdot<T>(p(ab + iz), fx, gy, fz);
+    T c110 = gdot<T>(p(bb + iz), gx, gy, fz);
+    T c001 = gdot<T>(p(aa + iz + 1), fx, fy, gz);
+    T c101 = gdot<T>(p(ba + iz + 1), gx, fy, gz);
+    T c011 = gdot<T>(p(ab + iz + 1), fx, gy, gz);
+    T c111 = gdot<T>(p(bb + iz + 1), gx, gy, gz);
     T u = fade<T>(fx), v = fade<T>(fy), w = fade<T>(fz);
     return lerp<T>(w, lerp<T>(v, lerp<T>(u, c000, c100), lerp<T>(u, c010, c110)),
                    lerp<T>(v, lerp<T>(u, c001, c101), lerp<T>(u, c011, c111)));
+}
+template <typename T>
+__device__ __forceinline__ T octave(const uint8_t *__restrict__ p, int ix, T fx, int iy, T fy, int iz, T fz) {
+    return octave_p<T>(PlainPerm{p}, ix, fx, iy, fy, iz, fz);
 }
 
 /* 26.3 PerlinNoise.wrap: identity inside (-2^24, 2^24) (engine/mc_noise.h:86-89) */
@@ -150,52 +170,154 @@ __device__ __forceinline__ double wrap_old(double x) {
     if (fabs(x) < 8388608.0) return x;
     return x - (double)lfloor(x / 33554432.0 + 0.5) * 33554432.0;
 }
-/* one input coordinate -> lattice cell and fraction */
-__device__ __forceinline__ void split_f(double v, double off, int &i, float &f) {
+/* One input coordinate -> lattice cell and fraction, as the reference computes it (all in double). */
+__device__ __forceinline__ void split_f_plain(double v, double off, int &i, float &f) {
     double s = wrap_new(v) + off;
     i = ifloor(s);
     f = (float)(s - (double)i);
 }
-__device__ __forceinline__ void split_d(double v, double off, int &i, double &f) {
+__device__ __forceinline__ void split_d_plain(double v, double off, int &i, double &f) {
     double s = wrap_old(v) + off;
     i = ifloor(s);
     f = s - (double)i;
 }
 
-/* Octave with input (x, 0, z) and with input (x, y, 0): the zero coordinate uses the table's split. */
-__device__ __forceinline__ float oct_f_y0(const MgLattice *__restrict__ L, double x, double z) {
+/* fb * 2^-sh rounded to nearest-even float (fb < 2^53; the result exponent must be >= -126) */
+__device__ __forceinline__ float scaled_to_f32(uint64_t fb, int sh) {
+    if (fb == 0) return 0.0f;
+    const int L = 64 - __clzll((long long)fb);
+    int ex = L - 1 - sh;
+    uint32_t mant;
+    if (L <= 24) {
+        mant = (uint32_t)(fb << (24 - L));
+    } else {
+        const int r = L - 24;
+        const uint64_t rem = fb & ((1ULL << r) - 1), half = 1ULL << (r - 1);
+        mant = (uint32_t)(fb >> r);
+        if (rem > half || (rem == half && (mant & 1u))) {
+            mant++;
+            if (mant == (1u << 24)) { mant >>= 1; ex++; }
+        }
+    }
+    return __uint_as_float(((uint32_t)(ex + 127) << 23) | (mant & 0x7FFFFFu));
+}
+/* fb * 2^-sh exactly as a double (fb < 2^53) */
+__device__ __forceinline__ double scaled_to_f64(uint64_t fb, int sh) {
+    if (fb == 0) return 0.0;
+    const int L = 64 - __clzll((long long)fb);
+    const uint64_t mant = fb << (53 - L);
+    return __longlong_as_double((long long)(((uint64_t)(L - 1 - sh + 1023) << 52) | (mant & ((1ULL << 52) - 1))));
+}
+
+/* The same split for v = x * 2^k, exactly equal to split_*_plain(x * f, off) with f = 2^k, but with one
+ * FP64-pipe operation (the rounded add s = v + off) instead of eight: GB300 runs FP64 at about 1/70 of the
+ * FP32 rate.  x * 2^k is an exponent add; the wrap is the identity for |v| < 2^23; floor(s) and the exact
+ * fraction s - floor(s) come from the bits of s, and the float fraction is rounded to nearest-even in
+ * integer arithmetic.  Cases outside those bounds (|v| >= 2^23, s in (-1, 0), tiny s) take the plain path. */
+template <bool F32>
+__device__ __forceinline__ bool split_bits(double s, int &i, float &ff, double &fd) {
+    const uint64_t b = (uint64_t)__double_as_longlong(s);
+    const int ebits = (int)((b >> 52) & 0x7FF);
+    const bool neg = (b >> 63) != 0;
+    if (ebits == 0) {
+        if ((b << 1) != 0) return false; /* subnormal */
+        i = 0;                            /* +-0: floor 0, fraction s - 0 = s */
+        ff = neg ? -0.0f : 0.0f;
+        fd = s;
+        return true;
+    }
+    const int e = ebits - 1023;
+    if (e > 30) return false;
+    const uint64_t m = (b & ((1ULL << 52) - 1)) | (1ULL << 52);
+    if (!neg) {
+        if (e >= 0) {
+            const int sh = 52 - e;
+            i = (int)(m >> sh);
+            const uint64_t fb = m & ((1ULL << sh) - 1);
+            if (F32) ff = scaled_to_f32(fb, sh);
+            else fd = scaled_to_f64(fb, sh);
+        } else {
+            if (F32 && e < -126) return false;
+            i = 0;
+            if (F32) ff = scaled_to_f32(m, 52 - e);
+            else fd = s;
+        }
+        return true;
+    }
+    if (e < 0) return false; /* s in (-1, 0): the reference's s - floor(s) rounds */
+    const int sh = 52 - e;
+    const uint64_t ip = m >> sh, fb = m & ((1ULL << sh) - 1);
+    if (fb == 0) {
+        i = -(int)ip;
+        ff = 0.0f;
+        fd = 0.0;
+    } else {
+        i = -(int)ip - 1;
+        if (F32) ff = scaled_to_f32((1ULL << sh) - fb, sh);
+        else fd = scaled_to_f64((1ULL << sh) - fb, sh);
+    }
+    return true;
+}
+/* x * 2^k by an exponent add when x is a normal double and the product stays below 2^23 in magnitude */
+__device__ __forceinline__ bool scale_small(double x, int k, double &v) {
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+    const int ebits = (int)((b >> 52) & 0x7FF);
+    if (ebits == 0) {
+        if ((b << 1) != 0) return false;
+        v = x; /* +-0 */
+        return true;
+    }
+    const int ne = ebits + k;
+    if (ne <= 0 || ne >= 1023 + 23) return false;
+    v = __longlong_as_double((long long)(b + ((uint64_t)(int64_t)k << 52)));
+    return true;
+}
+__device__ __forceinline__ void split_fk(double x, double f, int k, double off, int &i, float &fr) {
+    double v, fd;
+    if (scale_small(x, k, v) && split_bits<true>(v + off, i, fr, fd)) return;
+    split_f_plain(x * f, off, i, fr);
+}
+__device__ __forceinline__ void split_dk(double x, double f, int k, double off, int &i, double &fr) {
+    double v;
+    float ff;
+    if (scale_small(x, k, v) && split_bits<false>(v + off, i, ff, fr)) return;
+    split_d_plain(x * f, off, i, fr);
+}
+
+/* Octave with input (x*f, 0, z*f) and with input (x*f, y*f, 0); the zero coordinate uses the table's split. */
+__device__ __forceinline__ float oct_f_y0(const MgLattice *__restrict__ L, double x, double z, double f, int k) {
     int ix, iz;
     float fx, fz;
-    split_f(x, L->ox, ix, fx);
-    split_f(z, L->oz, iz, fz);
+    split_fk(x, f, k, L->ox, ix, fx);
+    split_fk(z, f, k, L->oz, iz, fz);
     return octave<float>(L->p, ix, fx, L->iy, L->fy, iz, fz);
 }
-__device__ __forceinline__ float oct_f_z0(const MgLattice *__restrict__ L, double x, double y) {
+__device__ __forceinline__ float oct_f_z0(const MgLattice *__restrict__ L, double x, double y, double f, int k) {
     int ix, iy;
     float fx, fy;
-    split_f(x, L->ox, ix, fx);
-    split_f(y, L->oy, iy, fy);
+    split_fk(x, f, k, L->ox, ix, fx);
+    split_fk(y, f, k, L->oy, iy, fy);
     return octave<float>(L->p, ix, fx, iy, fy, L->iz, L->fz);
 }
-__device__ __forceinline__ double oct_d_y0(const MgLattice *__restrict__ L, double x, double z) {
+__device__ __forceinline__ double oct_d_y0(const MgLattice *__restrict__ L, double x, double z, double f, int k) {
     int ix, iz;
     double fx, fz;
-    split_d(x, L->ox, ix, fx);
-    split_d(z, L->oz, iz, fz);
+    split_dk(x, f, k, L->ox, ix, fx);
+    split_dk(z, f, k, L->oz, iz, fz);
     return octave<double>(L->p, ix, fx, L->iy, L->fyd, iz, fz);
 }
-__device__ __forceinline__ double oct_d_z0(const MgLattice *__restrict__ L, double x, double y) {
+__device__ __forceinline__ double oct_d_z0(const MgLattice *__restrict__ L, double x, double y, double f, int k) {
     int ix, iy;
     double fx, fy;
-    split_d(x, L->ox, ix, fx);
-    split_d(y, L->oy, iy, fy);
+    split_dk(x, f, k, L->ox, ix, fx);
+    split_dk(y, f, k, L->oy, iy, fy);
     return octave<double>(L->p, ix, fx, iy, fy, L->iz, L->fzd);
 }
 
 /* ------------------------------------------------------------------ NormalNoise (engine/mc_noise.h:285-324)
  * Every NormalNoise on the biome path has one input coordinate equal to zero: the five climate noises
  * and the Nether noises take (x, 0, z), ShiftA (x, 0, z), ShiftB (z, x, 0).  The second stack's input
- * x*(f*c) equals (x*c)*f exactly (f is a power of two), so xc = x*c is formed once per point. */
+ * x*(f*c) equals (x*c)*f exactly (f = 2^k), so xc = x*c is formed once per point. */
 /* float branch, non-legacy (interleaved first_k, second_k) */
 __device__ __forceinline__ float nn_f_y0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
                                          double xc, double zc) {
@@ -203,8 +325,8 @@ __device__ __forceinline__ float nn_f_y0(const MgNoise &N, const MgLattice *__re
     const MgLattice *A = T + N.base, *B = A + N.nlev;
     for (int k = 0; k < N.nlev; k++) {
         double f = N.freq[k];
-        acc += N.amp_f[k] * oct_f_y0(A + k, x * f, z * f);
-        acc += N.amp_f[k] * oct_f_y0(B + k, xc * f, zc * f);
+        acc += N.amp_f[k] * oct_f_y0(A + k, x, z, f, N.fexp[k]);
+        acc += N.amp_f[k] * oct_f_y0(B + k, xc, zc, f, N.fexp[k]);
     }
     return acc;
 }
@@ -214,8 +336,8 @@ __device__ __forceinline__ float nn_f_z0(const MgNoise &N, const MgLattice *__re
     const MgLattice *A = T + N.base, *B = A + N.nlev;
     for (int k = 0; k < N.nlev; k++) {
         double f = N.freq[k];
-        acc += N.amp_f[k] * oct_f_z0(A + k, x * f, y * f);
-        acc += N.amp_f[k] * oct_f_z0(B + k, xc * f, yc * f);
+        acc += N.amp_f[k] * oct_f_z0(A + k, x, y, f, N.fexp[k]);
+        acc += N.amp_f[k] * oct_f_z0(B + k, xc, yc, f, N.fexp[k]);
     }
     return acc;
 }
@@ -224,8 +346,8 @@ __device__ __forceinline__ float nn_f_legacy_y0(const MgNoise &N, const MgLattic
                                                 double xc, double zc) {
     float acc = 0.0f;
     const MgLattice *A = T + N.base, *B = A + N.nlev;
-    for (int k = 0; k < N.nlev; k++) acc += N.amp_f[k] * oct_f_y0(A + k, x * N.freq[k], z * N.freq[k]);
-    for (int k = 0; k < N.nlev; k++) acc += N.amp_f[k] * oct_f_y0(B + k, xc * N.freq[k], zc * N.freq[k]);
+    for (int k = 0; k < N.nlev; k++) acc += N.amp_f[k] * oct_f_y0(A + k, x, z, N.freq[k], N.fexp[k]);
+    for (int k = 0; k < N.nlev; k++) acc += N.amp_f[k] * oct_f_y0(B + k, xc, zc, N.freq[k], N.fexp[k]);
     return acc;
 }
 /* double branch: (first + second) * valueFactor */
@@ -235,11 +357,11 @@ __device__ __forceinline__ double nn_d_y0(const MgNoise &N, const MgLattice *__r
     const MgLattice *A = T + N.base, *B = A + N.nlev;
     for (int k = 0; k < N.nlev; k++) {
         double f = N.freq[k];
-        a += N.amp_d[k] * oct_d_y0(A + k, x * f, z * f) * N.vf_d[k];
+        a += N.amp_d[k] * oct_d_y0(A + k, x, z, f, N.fexp[k]) * N.vf_d[k];
     }
     for (int k = 0; k < N.nlev; k++) {
         double f = N.freq[k];
-        b += N.amp_d[k] * oct_d_y0(B + k, xc * f, zc * f) * N.vf_d[k];
+        b += N.amp_d[k] * oct_d_y0(B + k, xc, zc, f, N.fexp[k]) * N.vf_d[k];
     }
     return (a + b) * N.vfac;
 }
@@ -249,11 +371,11 @@ __device__ __forceinline__ double nn_d_z0(const MgNoise &N, const MgLattice *__r
     const MgLattice *A = T + N.base, *B = A + N.nlev;
     for (int k = 0; k < N.nlev; k++) {
         double f = N.freq[k];
-        a += N.amp_d[k] * oct_d_z0(A + k, x * f, y * f) * N.vf_d[k];
+        a += N.amp_d[k] * oct_d_z0(A + k, x, y, f, N.fexp[k]) * N.vf_d[k];
     }
     for (int k = 0; k < N.nlev; k++) {
         double f = N.freq[k];
-        b += N.amp_d[k] * oct_d_z0(B + k, xc * f, yc * f) * N.vf_d[k];
+        b += N.amp_d[k] * oct_d_z0(B + k, xc, yc, f, N.fexp[k]) * N.vf_d[k];
     }
     return (a + b) * N.vfac;
 }
@@ -322,18 +444,23 @@ __device__ __forceinline__ float spline_eval(const MgSpline &S, const float co[4
 }
 
 /* ------------------------------------------------------------------ biome R-tree (engine/mc_biomes.h:31-62) */
+__device__ __forceinline__ int32_t lo16(uint32_t w) { return (int32_t)(int16_t)(w & 0xFFFFu); }
+__device__ __forceinline__ int32_t hi16(uint32_t w) { return (int32_t)w >> 16; }
+__device__ __forceinline__ uint64_t dim_sq(int32_t t, int32_t lo, int32_t hi) {
+    const int32_t x = max(max(t - hi, lo - t), 0);
+    return (uint64_t)(uint32_t)x * (uint32_t)x;
+}
+/* squared distance of target t (6 quantised values; the offset coordinate is 0) to a node's box */
 __device__ __forceinline__ uint64_t node_dist(const MgTreeNode &n, const int32_t *t) {
-    uint64_t s = 0;
-#pragma unroll
-    for (int d = 0; d < 6; d++) {
-        int32_t a = t[d] - (int32_t)n.hi[d], b = (int32_t)n.lo[d] - t[d];
-        int32_t x = max(max(a, b), 0);
-        s += (uint64_t)((int64_t)x * x);
-    }
-    /* seventh dimension: the target's offset coordinate is 0 */
-    int32_t a = -(int32_t)n.hi[6], b = (int32_t)n.lo[6];
-    int32_t x = max(max(a, b), 0);
-    s += (uint64_t)((int64_t)x * x);
+    const uint4 a = *reinterpret_cast<const uint4 *>(&n);                              /* lo[0..5], hi[0..1] */
+    const uint4 b = *(reinterpret_cast<const uint4 *>(&n) + 1);                        /* hi[2..5], d7, links */
+    uint64_t s = b.z;
+    s += dim_sq(t[0], lo16(a.x), lo16(a.w));
+    s += dim_sq(t[1], hi16(a.x), hi16(a.w));
+    s += dim_sq(t[2], lo16(a.y), lo16(b.x));
+    s += dim_sq(t[3], hi16(a.y), hi16(b.x));
+    s += dim_sq(t[4], lo16(a.z), lo16(b.y));
+    s += dim_sq(t[5], hi16(a.z), hi16(b.y));
     return s;
 }
 /* Climate.RTree.SubTree.search, iterative: descend into a child iff its box distance is below the best

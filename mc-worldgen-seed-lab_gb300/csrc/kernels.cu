@@ -15,6 +15,7 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include "climate.cuh"
 #include "device.cuh"
 #include "launch.h"
 #include "prof.h"
@@ -32,6 +33,7 @@ namespace mg {
 static long long g_launches = 0;
 long long launch_count() { return g_launches; }
 static inline void count_launch() { __atomic_add_fetch(&g_launches, 1, __ATOMIC_RELAXED); }
+void count_launch_external() { count_launch(); }
 
 /* ============================================================================ per-seed setup */
 #define SETUP_NT 128
@@ -143,151 +145,6 @@ __global__ void __launch_bounds__(SETUP_NT) k_setup_end(const int64_t *__restric
     legacy_lattice(st, perm, t, out + g);
 }
 
-/* ============================================================================ climate */
-/* Overworld climate of quart cell (qx, qy, qz) -> 6 quantised targets (engine/mc_climate.h:113-170). */
-template <bool FM>
-__device__ __forceinline__ void climate_ow(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
-                                           int qx, int qy, int qz, int32_t tg[6]) {
-    const double X = (double)qx, Z = (double)qz; /* blockX * 0.25 with blockX = 4 qx */
-    const double Xc = X * MG_SECOND_STACK, Zc = Z * MG_SECOND_STACK;
-    const int by = qy * 4;
-    if (FM) {
-        float sx = nn_f_y0(W.noise[0], T, X, Z, Xc, Zc) * 4.0f; /* ShiftA (x, 0, z) */
-        float sz = nn_f_z0(W.noise[0], T, Z, X, Zc, Xc) * 4.0f; /* ShiftB (z, x, 0) */
-        double x = X + (double)sx, z = Z + (double)sz;
-        double xc = x * MG_SECOND_STACK, zc = z * MG_SECOND_STACK;
-        float tv = nn_f_y0(W.noise[1], T, x, z, xc, zc);
-        float hv = nn_f_y0(W.noise[2], T, x, z, xc, zc);
-        float cv = nn_f_y0(W.noise[3], T, x, z, xc, zc);
-        float ev = nn_f_y0(W.noise[4], T, x, z, xc, zc);
-        float rv = nn_f_y0(W.noise[5], T, x, z, xc, zc);
-        float a = fabsf(rv) + W.rf_f[0];
-        float rf = (fabsf(a) + W.rf_f[1]) * W.rf_f[2];
-        float co[4] = {cv, ev, rv, rf};
-        float off = W.off_f + spline_eval(S, co);
-        int lo = min(W.grad_from_y, W.grad_to_y), hi = max(W.grad_from_y, W.grad_to_y);
-        int yy = by < lo ? lo : (by > hi ? hi : by);
-        float fac = (W.grad_to_f - W.grad_from_f) / (float)(W.grad_to_y - W.grad_from_y);
-        float depth = (W.grad_from_f + (float)(yy - W.grad_from_y) * fac) + off;
-        tg[0] = quantize(tv); tg[1] = quantize(hv); tg[2] = quantize(cv);
-        tg[3] = quantize(ev); tg[4] = quantize(depth); tg[5] = quantize(rv);
-    } else {
-        double sx = nn_d_y0(W.noise[0], T, X, Z, Xc, Zc) * 4.0;
-        double sz = nn_d_z0(W.noise[0], T, Z, X, Zc, Xc) * 4.0;
-        double x = X + sx, z = Z + sz;
-        double xc = x * MG_SECOND_STACK, zc = z * MG_SECOND_STACK;
-        double tv = nn_d_y0(W.noise[1], T, x, z, xc, zc);
-        double hv = nn_d_y0(W.noise[2], T, x, z, xc, zc);
-        double cv = nn_d_y0(W.noise[3], T, x, z, xc, zc);
-        double ev = nn_d_y0(W.noise[4], T, x, z, xc, zc);
-        double rv = nn_d_y0(W.noise[5], T, x, z, xc, zc);
-        double rf = (fabs(fabs(rv) + W.rf_d[0]) + W.rf_d[1]) * W.rf_d[2];
-        float co[4] = {(float)cv, (float)ev, (float)rv, (float)rf};
-        double off = 0.0 + (W.off_d + (double)spline_eval(S, co)) * 1.0;
-        double fac = ((double)by - (double)W.grad_from_y) / ((double)W.grad_to_y - (double)W.grad_from_y);
-        double g = fac < 0.0 ? W.grad_from_d
-                             : (fac > 1.0 ? W.grad_to_d : W.grad_from_d + fac * (W.grad_to_d - W.grad_from_d));
-        double depth = g + off;
-        tg[0] = quantize((float)tv); tg[1] = quantize((float)hv); tg[2] = quantize((float)cv);
-        tg[3] = quantize((float)ev); tg[4] = quantize((float)depth); tg[5] = quantize((float)rv);
-    }
-}
-/* Nether: temperature and vegetation at (x/4, 0, z/4) (engine/cuda/mcg_host.c:63-74) */
-template <bool FM>
-__device__ __forceinline__ void climate_nether(const MgWorldDesc &W, const MgLattice *__restrict__ T, int qx, int qz,
-                                               int32_t tg[6]) {
-    const double X = (double)qx, Z = (double)qz;
-    const double Xc = X * MG_SECOND_STACK, Zc = Z * MG_SECOND_STACK;
-    float t, h;
-    if (FM) {
-        t = nn_f_legacy_y0(W.nether[0], T, X, Z, Xc, Zc);
-        h = nn_f_legacy_y0(W.nether[1], T, X, Z, Xc, Zc);
-    } else {
-        t = (float)nn_d_y0(W.nether[0], T, X, Z, Xc, Zc);
-        h = (float)nn_d_y0(W.nether[1], T, X, Z, Xc, Zc);
-    }
-    tg[0] = quantize(t);
-    tg[1] = quantize(h);
-    tg[2] = tg[3] = tg[4] = tg[5] = 0;
-}
-template <bool FM, int DIM>
-__device__ __forceinline__ void cell_target(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
-                                            int qx, int qy, int qz, int32_t tg[6]) {
-    if (DIM == MG_OVERWORLD) climate_ow<FM>(W, S, T, qx, qy, qz, tg);
-    else climate_nether<FM>(W, T, qx, qz, tg);
-}
-
-/* ============================================================================ End islands (engine/mc_end.h) */
-__device__ __forceinline__ double simplex2(const uint8_t *__restrict__ p, double xin, double yin, double F2, double G2) {
-    double s = (xin + yin) * F2;
-    int i = ifloor(xin + s), j = ifloor(yin + s);
-    double t = (double)(i + j) * G2;
-    double x0 = xin - ((double)i - t), y0 = yin - ((double)j - t);
-    int i1 = x0 > y0 ? 1 : 0, j1 = 1 - i1;
-    double x1 = x0 - (double)i1 + G2, y1 = y0 - (double)j1 + G2;
-    double x2 = x0 - 1.0 + 2.0 * G2, y2 = y0 - 1.0 + 2.0 * G2;
-    int ii = i & 255, jj = j & 255;
-    int g0 = p[(ii + p[jj]) & 255] % 12;
-    int g1 = p[(ii + i1 + p[(jj + j1) & 255]) & 255] % 12;
-    int g2 = p[(ii + 1 + p[(jj + 1) & 255]) & 255] % 12;
-    double n = 0.0, acc[3];
-    const double xs[3] = {x0, x1, x2}, ys[3] = {y0, y1, y2};
-    const int gs[3] = {g0, g1, g2};
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        double tt = 0.5 - xs[c] * xs[c] - ys[c] * ys[c] - 0.0 * 0.0;
-        if (tt < 0.0) acc[c] = 0.0;
-        else {
-            tt *= tt;
-            acc[c] = tt * tt * gdot<double>(gs[c], xs[c], ys[c], 0.0);
-        }
-    }
-    n = acc[0] + acc[1] + acc[2];
-    return 70.0 * n;
-}
-__device__ __forceinline__ float clampf(float v, float lo, float hi) { return v < lo ? lo : (v < hi ? v : hi); }
-/* EndIslandDensityFunction.getHeightValue at (sx, sz) = (block / 8) */
-__device__ float end_height(const uint8_t *__restrict__ p, bool fm, int sx, int sz, double F2, double G2) {
-    int cx = sx / 2, cz = sz / 2, ox = sx % 2, oz = sz % 2;
-    float best;
-    if (!fm) {
-        int32_t sq = (int32_t)((uint32_t)sx * (uint32_t)sx + (uint32_t)sz * (uint32_t)sz); /* Java int overflow */
-        float len = (float)sqrt((double)(float)sq);
-        best = clampf(100.0f - len * 8.0f, -100.0f, 80.0f);
-    } else best = -100.0f;
-    for (int dx = -12; dx <= 12; dx++)
-        for (int dz = -12; dz <= 12; dz++) {
-            long long tx = (long long)cx + dx, tz = (long long)cz + dz;
-            if (tx * tx + tz * tz <= 4096LL) continue;
-            double nv = simplex2(p, (double)tx, (double)tz, F2, G2);
-            bool island = fm ? ((float)nv < -0.9f) : (nv < (double)-0.9f);
-            if (!island) continue;
-            float size = fmodf(fabsf((float)tx) * 3439.0f + fabsf((float)tz) * 147.0f, 13.0f) + 9.0f;
-            float xd = (float)(ox - dx * 2), zd = (float)(oz - dz * 2);
-            float h = clampf(100.0f - (float)sqrt((double)(xd * xd + zd * zd)) * size, -100.0f, 80.0f);
-            best = best > h ? best : h;
-        }
-    return best;
-}
-/* TheEndBiomeSource class of chunk (cx, cz): 0 the_end, 1 highlands, 2 midlands, 3 small islands, 4 barrens */
-__device__ int end_chunk_class(const uint8_t *__restrict__ p, bool fm, int cx, int cz, double F2, double G2) {
-    if ((long long)cx * cx + (long long)cz * cz <= 4096LL) return 0;
-    int bx = (cx * 2 + 1) * 8, bz = (cz * 2 + 1) * 8;
-    float h = end_height(p, fm, bx / 8, bz / 8, F2, G2);
-    double e;
-    if (!fm) e = ((double)h - 8.0) / 128.0;
-    else {
-        float dx = (float)(0 - bx), dz = (float)(0 - bz);
-        float len = (float)sqrt((double)(dx * dx + 0.0f * 0.0f + dz * dz));
-        float c = (clampf(100.0f - len, -100.0f, 80.0f) - 8.0f) * 0.0078125f;
-        float o = (h - 8.0f) / 128.0f;
-        e = (double)(c > o ? c : o);
-    }
-    if (e > 0.25) return 1;
-    if (e >= -0.0625) return 2;
-    return e < -0.21875 ? 3 : 4;
-}
-
 /* ============================================================================ sampling kernels */
 /* Stage the seed-independent spline and one seed's lattices in shared memory. */
 __device__ __forceinline__ void stage(const MgWorldDesc &W, const MgLattice *__restrict__ src, int n, MgLattice *dstT,
@@ -380,73 +237,6 @@ __global__ void k_chain_resolve(const MgTreeNode *__restrict__ tree, const Chain
     out[g] = tree[leaf].biome;
 }
 
-/* ---------------------------------------------------------------------------- BiomeManager zoom
- * (libmcgen/src/region.c:61-85) */
-__device__ __forceinline__ int64_t zoom_step(int64_t r, int64_t c) {
-    uint64_t v = (uint64_t)r;
-    v *= v * 6364136223846793005ULL + 1442695040888963407ULL;
-    return (int64_t)(v + (uint64_t)c);
-}
-__device__ __forceinline__ double zoom_jitter(int64_t r) {
-    int64_t m = (r >> 24) % 1024;
-    if (m < 0) m += 1024;
-    return ((double)m / 1024.0 - 0.5) * 0.9;
-}
-__device__ __forceinline__ double zoom_dist(int64_t seed, int x, int y, int z, double dx, double dy, double dz) {
-    int64_t r = seed;
-    r = zoom_step(r, x); r = zoom_step(r, y); r = zoom_step(r, z);
-    r = zoom_step(r, x); r = zoom_step(r, y); r = zoom_step(r, z);
-    double jx = zoom_jitter(r);
-    r = zoom_step(r, seed);
-    double jy = zoom_jitter(r);
-    r = zoom_step(r, seed);
-    double jz = zoom_jitter(r);
-    return (dz + jz) * (dz + jz) + (dy + jy) * (dy + jy) + (dx + jx) * (dx + jx);
-}
-__device__ __forceinline__ void zoom_cell(int64_t zseed, int x, int y, int z, int &cx, int &cy, int &cz) {
-    int ax = x - 2, ay = y - 2, az = z - 2;
-    int px = ax >> 2, py = ay >> 2, pz = az >> 2;
-    double fx = (ax & 3) / 4.0, fy = (ay & 3) / 4.0, fz = (az & 3) / 4.0;
-    int best = 0;
-    double bd = __longlong_as_double(0x7FF0000000000000LL);
-    for (int i = 0; i < 8; i++) {
-        bool ex = (i & 4) == 0, ey = (i & 2) == 0, ez = (i & 1) == 0;
-        double d = zoom_dist(zseed, ex ? px : px + 1, ey ? py : py + 1, ez ? pz : pz + 1, ex ? fx : fx - 1.0,
-                             ey ? fy : fy - 1.0, ez ? fz : fz - 1.0);
-        if (bd > d) { best = i; bd = d; }
-    }
-    cx = (best & 4) == 0 ? px : px + 1;
-    cy = (best & 2) == 0 ? py : py + 1;
-    cz = (best & 1) == 0 ? pz : pz + 1;
-}
-/* world_biome_cell (libmcgen/src/biome.c:87-114): y clamped into the dimension; a tied cell walks back along
- * LevelChunkSection.fillBiomesFromNoise order (sections bottom-up, then x, y, z) to an untied cell or the
- * column's first cell, then replays the candidate chain forward.  The walk is bounded by the column. */
-template <bool FM, int DIM>
-__device__ int cell_chunk(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
-                          const MgTreeNode *__restrict__ tree, int qx, int qy, int qz) {
-    const int qmin = W.min_y >> 2, qh = W.height >> 2;
-    qy = qy < qmin ? qmin : (qy > qmin + qh - 1 ? qmin + qh - 1 : qy);
-    const int bx = qx & ~3, bz = qz & ~3, ly = qy - qmin;
-    const int idx0 = (ly >> 2) * 64 + (qx & 3) * 16 + (ly & 3) * 4 + (qz & 3);
-    int32_t tg[6];
-    uint64_t d;
-    int idx = idx0, leaf;
-    for (;;) {
-        int sec = idx >> 6, r = idx & 63;
-        cell_target<FM, DIM>(W, S, T, bx + (r >> 4), qmin + sec * 4 + ((r >> 2) & 3), bz + (r & 3), tg);
-        leaf = tree_search(tree, tg, -1, d);
-        if (idx == 0 || tree_count_at(tree, tg, d) < 2) break;
-        idx--;
-    }
-    for (int k = idx + 1; k <= idx0; k++) { /* replay the chain forward */
-        int sec = k >> 6, r = k & 63;
-        cell_target<FM, DIM>(W, S, T, bx + (r >> 4), qmin + sec * 4 + ((r >> 2) & 3), bz + (r & 3), tg);
-        int l0 = tree_search(tree, tg, -1, d);
-        if (node_dist(tree[leaf], tg) != d) leaf = l0;
-    }
-    return tree[leaf].biome;
-}
 /* mcgen_biome_grid: out[iz*nx+ix] = biome_at(x0 + ix*step, y, z0 + iz*step) (libmcgen/src/region.c:86-108) */
 template <bool FM, int DIM>
 __global__ void __launch_bounds__(128) k_blockgrid(const __grid_constant__ MgWorldDesc W, const MgTreeNode *__restrict__ tree,

@@ -10,6 +10,7 @@
 namespace mg {
 
 long long launch_count();
+void count_launch_external(); /* for launchers outside kernels.cu */
 
 /* per-seed lattices: d_states[s * W.ntables + j] */
 int launch_setup(const MgWorldDesc &W, const int64_t *d_seeds, int ns, MgLattice *d_states, cudaStream_t st);
@@ -17,6 +18,14 @@ int launch_setup(const MgWorldDesc &W, const int64_t *d_seeds, int ns, MgLattice
 /* seeds x quart points, ENGINE rule (targets optional) */
 int launch_points(const MgWorldDesc &W, const MgTreeNode *tree, const MgLattice *states, int ns, const int32_t *pts,
                   int np, uint8_t *out, int32_t *targets, cudaStream_t st);
+
+/* seeds x points for the Overworld (fused.cu): lattices built and sampled in shared memory by one kernel,
+ * climate finish + R-tree by a second.  Scratch: fused_scratch_bytes(W, ns * np) (five noise values per
+ * sample).  fused_supported() tells whether a world's lattice count fits the kernel. */
+bool fused_supported(const MgWorldDesc &W);
+size_t fused_scratch_bytes(const MgWorldDesc &W, long long samples);
+int launch_ow_seed_points(const MgWorldDesc &W, const MgTreeNode *tree, const int64_t *seeds, int ns, const int32_t *pts,
+                          int np, uint8_t *out, int32_t *targets, void *scratch, cudaStream_t st);
 
 /* one seed's quart grid.  Scratch: chain_scratch_bytes(nx*nz) for GRID_CHAIN; for the End,
  * (nx/4 + 2) * (nz/4 + 2) bytes of chunk classes. */

@@ -29,7 +29,8 @@ typedef struct {
     int32_t first;      /* first octave */
     int32_t idx[MG_MAX_OCT];       /* amplitude index of level k */
     uint64_t hlo[MG_MAX_OCT], hhi[MG_MAX_OCT]; /* md5("octave_<n>") halves */
-    double freq[MG_MAX_OCT];       /* input factor of level k (a power of two) */
+    double freq[MG_MAX_OCT];       /* input factor of level k, 2^fexp[k] */
+    int32_t fexp[MG_MAX_OCT];      /* log2 of freq[k] */
     double amp_d[MG_MAX_OCT];      /* double branch: amplitude */
     double vf_d[MG_MAX_OCT];       /* double branch: value factor of the level */
     double vfac;                   /* double branch: NormalNoise value factor */
@@ -49,11 +50,14 @@ typedef struct __attribute__((aligned(16))) {
     float cval[MG_SPL_CONST];
 } MgSpline;
 
-/* R-tree node on the device: children of a subtree are contiguous [first, first+count);
- * a leaf has count == 0.  Bounds are quantised climate values (|v| <= 12000 in every table). */
-typedef struct {
-    int16_t lo[MG_TREE_DIMS];
-    int16_t hi[MG_TREE_DIMS];
+/* R-tree node on the device (32 bytes, two 16-byte loads): children of a subtree are contiguous
+ * [first, first+count); a leaf has count == 0.  Bounds of the six climate dimensions are quantised values
+ * (|v| <= 12000 in every table); the seventh dimension ("offset") always meets a target coordinate of 0, so
+ * its squared distance max(-hi, lo, 0)^2 is stored instead of its bounds. */
+typedef struct __attribute__((aligned(16))) {
+    int16_t lo[6];
+    int16_t hi[6];
+    uint32_t d7;
     uint16_t first;
     uint8_t count;
     uint8_t biome;

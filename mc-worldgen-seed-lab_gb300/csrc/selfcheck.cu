@@ -1,0 +1,85 @@
+/* selfcheck.cu -- on-device check that the exact integer coordinate split (split_fk / split_dk) equals the
+ * reference arithmetic (split_*_plain: (x * f) wrapped, + offset, floor, fraction, in double) bit for bit,
+ * on generated inputs that cover the ranges the biome path sees and the edges of the fast path:
+ * integer quart coordinates, coordinates plus a float shift, their products with the second-stack factor,
+ * tiny and huge values, values whose sum with the offset lands near an integer, in (-1, 0) or on 0, and
+ * offsets at 0, near 256 and on integers. */
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/mcgen.h"
+#include "device.cuh"
+
+using namespace mgd;
+
+namespace {
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+__global__ void k_check_split(long long n, uint64_t seed, unsigned long long *bad) {
+    unsigned long long bf = 0, bd = 0;
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
+        uint64_t r0 = mix64(seed ^ (uint64_t)g), r1 = mix64(r0), r2 = mix64(r1), r3 = mix64(r2);
+        const int k = (int)(r0 % 13) - 12;
+        const double f = ldexp(1.0, k);
+        double off;
+        switch ((r1 >> 8) % 8) {
+        case 0: off = 0.0; break;
+        case 1: off = 255.99999999999997; break;
+        case 2: off = (double)(r1 % 256); break;
+        case 3: off = 0.5; break;
+        default: off = (double)(r1 >> 11) * 0x1.0p-53 * 256.0; break;
+        }
+        double x;
+        const int64_t sr = (int64_t)r2;
+        switch (r0 >> 60) {
+        case 0: x = (double)(sr >> 39); break;                               /* |x| < 2^24, integer */
+        case 1: x = (double)(sr % 301); break;                               /* small integer */
+        case 2: x = (double)(sr % 40000) + (double)(float)((double)(int32_t)r3 * 0x1.0p-27); break; /* + float shift */
+        case 3: x = ((double)(sr % 3000000) + (double)(float)((double)(int32_t)r3 * 0x1.0p-28)) * MG_SECOND_STACK; break;
+        case 4: x = ldexp((double)(r3 >> 11), -(int)(r2 % 120) - 20) * ((r2 >> 63) ? -1.0 : 1.0); break; /* tiny */
+        case 5: { /* x * f + off near an integer, in (-1, 0) or on 0 */
+            const double target = (double)((int)(r3 % 11) - 5) + ((r3 >> 40) % 3 == 0 ? 0.0 : ldexp((double)(int64_t)(r2 >> 50) - 8192.0, -(int)((r3 >> 20) % 60)));
+            x = (target - off) / f;
+            break;
+        }
+        case 6: x = ldexp((double)(r3 >> 11) * 0x1.0p-53 + 1.0, 20 + (int)(r2 % 8)) * ((r2 >> 62) & 1 ? -1.0 : 1.0); break; /* huge */
+        case 7: x = -(double)(sr >> 40) - off / f; break;                     /* negative, sum near -integer */
+        case 8: x = (double)(sr >> 42) + 0.25 * (double)(r3 % 4); break;
+        default: x = ldexp((double)(int64_t)(r3 >> 10) * 0x1.0p-53, (int)(r2 % 56) - 30); break;
+        }
+        int ia, ib;
+        float fa, fb;
+        split_fk(x, f, k, off, ia, fa);
+        split_f_plain(x * f, off, ib, fb);
+        bf += (ia != ib) || (__float_as_uint(fa) != __float_as_uint(fb));
+        double da, db;
+        split_dk(x, f, k, off, ia, da);
+        split_d_plain(x * f, off, ib, db);
+        bd += (ia != ib) || (__double_as_longlong(da) != __double_as_longlong(db));
+    }
+    if (bf) atomicAdd(&bad[0], bf);
+    if (bd) atomicAdd(&bad[1], bd);
+}
+
+}  // namespace
+
+extern "C" MCGEN_API int mcgen_gb300_check_split(long long n, unsigned long long seed, long long *bad_f, long long *bad_d) {
+    if (n < 0 || !bad_f || !bad_d) return MCGEN_E_ARG;
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, 2 * sizeof(unsigned long long)) != cudaSuccess) return MCGEN_E_NOMEM;
+    cudaMemset(d, 0, 2 * sizeof(unsigned long long));
+    k_check_split<<<152 * 8, 256>>>(n, seed, d);
+    unsigned long long h[2] = {0, 0};
+    cudaError_t e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return MCGEN_E_INTERNAL;
+    *bad_f = (long long)h[0];
+    *bad_d = (long long)h[1];
+    return MCGEN_OK;
+}

@@ -162,6 +162,9 @@ struct NoiseParams {
 
 static void octave_seeds(MgNoise *s) {
     for (int k = 0; k < s->nlev; k++) {
+        int e = 0;
+        double mant = frexp(s->freq[k], &e); /* freq = 2^(first + index): mant is exactly 0.5 */
+        s->fexp[k] = mant == 0.5 ? e - 1 : 4096; /* 4096: not a power of two, the device multiplies */
         char nm[32];
         snprintf(nm, sizeof nm, "octave_%d", s->first + s->idx[k]);
         seed_from_name(nm, &s->hlo[k], &s->hhi[k]);
@@ -458,8 +461,13 @@ static int load_tree(const char *root, int version, int dim, std::vector<MgTreeN
                 *err = "biome parameter outside the 16-bit node range";
                 return MCGEN_E_DATA;
             }
-            o.lo[d] = (int16_t)lo;
-            o.hi[d] = (int16_t)hi;
+            if (d < 6) {
+                o.lo[d] = (int16_t)lo;
+                o.hi[d] = (int16_t)hi;
+            } else {
+                int64_t x = std::max(std::max(-hi, lo), (int64_t)0);
+                o.d7 = (uint32_t)(x * x);
+            }
         }
         if (b.kids.empty()) {
             o.biome = (uint8_t)b.biome;
