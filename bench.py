@@ -61,6 +61,29 @@ def config2_inputs(n_seeds: int = 65536):
     return seeds, pts
 
 
+C4_VERSIONS = ("26.1", "26.2", "26.3")
+C4_DIMS = ("minecraft:overworld",) * 6 + ("minecraft:the_nether",) * 2 + ("minecraft:the_end",) * 2
+
+
+def config4_requests(n: int = 10000, state: int = 3):
+    """The uneven mixed batch: n requests from SplitMix64(state), six draws each -- seed; version uniform over
+    26.1/26.2/26.3; dimension Overworld:Nether:End = 6:2:2; square side floor(16 * 32^u) quart cells (u uniform
+    in [0,1): log-uniform in [16, 512)); origin x, z uniform in [-30000, 30000] blocks (quart = block >> 2);
+    y = 64 (quart 16).  Returns (version, dimension, seed, qx0, qz0, side, qy) tuples."""
+    r = splitmix64(state, 6 * n).reshape(n, 6)
+    out = []
+    for i in range(n):
+        seed = int(r[i, 0].astype(np.int64))
+        version = C4_VERSIONS[int(r[i, 1] % np.uint64(3))]
+        dim = C4_DIMS[int(r[i, 2] % np.uint64(10))]
+        u = float(r[i, 3] >> np.uint64(11)) * 2.0 ** -53
+        side = int(16.0 * 32.0 ** u)
+        x = -30000 + int(r[i, 4] % np.uint64(60001))
+        z = -30000 + int(r[i, 5] % np.uint64(60001))
+        out.append((version, dim, seed, x >> 2, z >> 2, side, 16))
+    return out
+
+
 # ------------------------------------------------------------------------------------------ helpers
 def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
@@ -180,6 +203,8 @@ def run_gb300(args, rank, world, local_rank):
                               "(x,z in [-10000,10000], y in [-64,320]), ENGINE tie rule",
                   "seeds": int(seeds.size), "points_per_seed": int(len(pts)), "version": "26.3",
                   "dimension": "overworld", "l2": "working set > L2 (65536 x 46 lattices = 965 MB per step)"}
+    elif args.workload == "batch10k":
+        return run_batch(args, rank, world, local_rank, mg, ge)
     else:
         w = gen.world("minecraft:overworld", "normal", 12345)
         nx = nz = 256
@@ -297,6 +322,129 @@ def run_gb300(args, rank, world, local_rank):
         print(json.dumps(out), flush=True)
 
 
+def run_batch(args, rank, world, local_rank, mg, ge):
+    """Uneven mixed batch: 10,000 requests in one persistent launch (plan + CUDA graph), against the plain
+    form (one setup + one grid launch per request) on the same requests."""
+    import torch
+
+    dev = torch.device("cuda", local_rank)
+    reqs = config4_requests(args.requests)
+    gens = {v: mg.Generator.open(ge.data_root(), v) for v in C4_VERSIONS}
+    worlds = {(v, d): gens[v].world(d, "normal", 0) for v in C4_VERSIONS for d in set(C4_DIMS)}
+    plan = mg.Plan([(worlds[(v, d)], s, qx0, qz0, n, n, qy) for v, d, s, qx0, qz0, n, qy in reqs])
+    samples = plan.output_bytes
+    d_out = torch.empty(samples, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    tuned_ms = plan.autotune(d_out.data_ptr(), reps=1)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        plan.run_dev(d_out.data_ptr(), sh)
+    torch.cuda.synchronize(dev)
+    launches0 = mg.launch_count()
+    barrier()
+    with ClockSampler(local_rank) as clk:
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            plan.run_dev(d_out.data_ptr(), sh)
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = ev0.elapsed_time(ev1)
+    barrier()
+    graph_launches = mg.launch_count() - launches0  # graph replays are not counted by the library
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = samples * args.steps * world / (ms_max * 1e-3)
+    # per-kernel times: one run without the graph, under the library's event profiler
+    mg.profile(True)
+    plan.run_dev(d_out.data_ptr(), sh, graph=False)
+    torch.cuda.synchronize(dev)
+    mg.profile(False)
+    prof = mg.profile_read()
+    # plain form on the same requests
+    plain = torch.empty_like(d_out)
+    offs = [plan.offset(i) for i in range(len(reqs))]
+
+    def plain_step():
+        for i, (v, d, s, qx0, qz0, n, qy) in enumerate(reqs):
+            worlds[(v, d)].quart_grid_seed_dev(s, qx0, qz0, n, n, qy, 0, plain.data_ptr() + offs[i], sh)
+
+    plain_step()
+    torch.cuda.synchronize(dev)
+    pe0, pe1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    pe0.record(stream)
+    plain_step()
+    pe1.record(stream)
+    torch.cuda.synchronize(dev)
+    plain_wall = time.perf_counter() - t0
+    plain_ms = max(pe0.elapsed_time(pe1), plain_wall * 1e3)
+    same = bool(torch.equal(plain, d_out))
+    # end to end: host-buffer C ABI call (copies the ids to pinned host memory)
+    h_out = torch.empty(samples, dtype=torch.uint8).pin_memory()
+    hv = h_out.numpy()
+    plan.run(hv)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        plan.run(hv)
+    e2e_s = time.perf_counter() - t0
+    e2e = samples * args.steps * world / e2e_s
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32+f64+int64", "data": "synthetic (SplitMix64(3) requests)",
+           "config": {"workload": f"uneven mixed batch: {len(reqs)} SplitMix64(3) requests, versions 26.1/26.2/26.3, "
+                                  "Overworld:Nether:End 6:2:2, square side log-uniform in [16,512) quart cells, origin "
+                                  "uniform in [-30000,30000] blocks, y=64, ENGINE tie rule; one persistent launch "
+                                  "(CUDA graph) vs one plain launch pair per request",
+                      "requests": len(reqs), "samples_per_step": samples, "tile_shape": plan.shape,
+                      "autotune_ms": round(tuned_ms, 3), "l2": f"output {samples/1e6:.0f} MB per step > L2",
+                      "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+           "plain": {"value": samples * world / (plain_ms * 1e-3), "ms_per_step": plain_ms,
+                     "launches_per_step": 2 * len(reqs), "identical_output": same},
+           "batched_over_plain": (samples / (ms_max / args.steps)) / (samples / plain_ms),
+           "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(samples)},
+           "gpu_launches": int(graph_launches) + args.steps * (1 + sum(1 for _ in set(d for _, d, *_ in reqs)))}
+    if rank == 0:
+        out["kernels"] = {k: {"ms_total": round(v[0], 4), "launches": v[1], "avg_ms": round(v[0] / v[1], 5)}
+                          for k, v in prof.items()}
+        clocks = clk.summary()
+        if clocks:
+            out["clocks"] = clocks
+        if not args.skip_extras:
+            out["cpu_baseline"] = cpu_baseline_batch(reqs, args.cpu_sample_s)
+        print(json.dumps(out), flush=True)
+
+
+def cpu_baseline_batch(reqs, budget_s: float) -> dict:
+    """The reference algorithm on the host's cores over a prefix of the same requests (rows over threads)."""
+    import __graft_entry__ as ge
+    from oracle import oracle as O
+
+    cores = os.cpu_count() or 1
+    worlds = {}
+    done = cells = 0
+    t0 = time.perf_counter()
+    for v, d, s, qx0, qz0, n, qy in reqs:
+        key = (v, d)
+        if key not in worlds:
+            worlds[key] = O.World(ge.data_root(), v, d.split(":")[1])
+        worlds[key].quart_grid(s, qx0, qz0, n, n, qy, O.TIE_ENGINE, threads=cores)
+        done += 1
+        cells += n * n
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": cells / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"first {done} of {len(reqs)} requests ({cells} samples, {dt:.1f} s), rows over threads"}
+
+
 def cpu_baseline(workload: str, budget_s: float) -> dict:
     """The reference algorithm on this host's cores (CPU oracle, OpenMP over seeds or rows)."""
     import __graft_entry__ as ge
@@ -369,7 +517,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["seeds8", "grid256"], default="seeds8")
+    ap.add_argument("--workload", choices=["seeds8", "grid256", "batch10k"], default="seeds8")
+    ap.add_argument("--requests", type=int, default=10000, help="batch10k: number of requests")
     ap.add_argument("--cpu-sample-s", type=float, default=12.0)
     ap.add_argument("--seeds", type=int, default=65536, help="seeds8: number of seeds (65536 = the configuration)")
     ap.add_argument("--skip-extras", action="store_true",

@@ -52,6 +52,37 @@ MCGEN_API int mcgen_gb300_biome_grid_dev(const McWorld *w, int x0, int z0, int n
 MCGEN_API int mcgen_gb300_quart_grid_dev(const McWorld *w, int qx0, int qz0, int nx, int nz, int qy, int tie_rule,
                                          uint8_t *d_out, void *stream);
 
+/* One quart grid for an explicit seed (the world supplies version, dimension and preset), device output:
+ * the plain per-request form -- one setup launch and one grid launch per call. */
+MCGEN_API int mcgen_gb300_quart_grid_seed_dev(const McWorld *w, int64_t seed, int qx0, int qz0, int nx, int nz,
+                                              int qy, int tie_rule, uint8_t *d_out, void *stream);
+
+/* ---- batched form: many biome-map requests of uneven size in one persistent launch ----
+ * A request is a quart-resolution region (qx0.., qz0.., nx x nz at quart y) of one world (version,
+ * dimension, preset) and seed.  A plan freezes a request list: it builds every distinct (world, seed)'s
+ * noise lattices into a pool, splits requests into tiles that one persistent kernel takes from a device
+ * work queue, and lays outputs back to back (request i's nx*nz ids, row-major, at output offset i).
+ * Runs replay a CUDA graph of the setup and batch launches.  tie_rule: MCGEN_TIE_ENGINE or
+ * MCGEN_TIE_CHUNK_CELL (each cell resolved as the chunk that holds it stores it). */
+typedef struct McGb300Request {
+    const McWorld *world; /* version, dimension, preset; its own seed is ignored */
+    int64_t seed;
+    int32_t qx0, qz0, nx, nz, qy;
+} McGb300Request;
+typedef struct McGb300Plan McGb300Plan;
+MCGEN_API int mcgen_gb300_plan_new(const McGb300Request *reqs, int n, int tie_rule, McGb300Plan **out);
+MCGEN_API void mcgen_gb300_plan_free(McGb300Plan *p);
+MCGEN_API long long mcgen_gb300_plan_output_bytes(const McGb300Plan *p);
+MCGEN_API long long mcgen_gb300_plan_output_offset(const McGb300Plan *p, int i);
+/* the tile shape in use: 0 (32 x 4), 1 (16 x 8), 2 (64 x 2), 3 (8 x 16) */
+MCGEN_API int mcgen_gb300_plan_shape(const McGb300Plan *p);
+/* time the four tile shapes on this plan (reps runs each into d_out) and keep the fastest */
+MCGEN_API int mcgen_gb300_plan_autotune(McGb300Plan *p, uint8_t *d_out, int reps, double *best_ms);
+/* run into device memory on `stream` (graph replay) / without a graph / into host memory */
+MCGEN_API int mcgen_gb300_plan_run_dev(McGb300Plan *p, uint8_t *d_out, void *stream);
+MCGEN_API int mcgen_gb300_plan_run_dev_direct(McGb300Plan *p, uint8_t *d_out, void *stream);
+MCGEN_API int mcgen_gb300_plan_run(McGb300Plan *p, uint8_t *out);
+
 /* Allocation-free form of mcgen_gb300_seed_points_dev, for callers that cannot let a library allocate
  * device memory (their own memory arena, latency-critical loops, no allocation after set-up).  No
  * counterpart in the reference.  The per-seed noise lattices go to one fixed 16 MiB device array inside

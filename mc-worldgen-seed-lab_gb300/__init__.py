@@ -94,6 +94,26 @@ _PROTOS = {
                                           C.POINTER(C.c_longlong)]),
 }
 
+_PROTOS.update({
+    "mcgen_gb300_quart_grid_seed_dev": (C.c_int, [_P, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                                  _P, _P]),
+    "mcgen_gb300_plan_new": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(_P)]),
+    "mcgen_gb300_plan_free": (None, [_P]),
+    "mcgen_gb300_plan_output_bytes": (C.c_longlong, [_P]),
+    "mcgen_gb300_plan_output_offset": (C.c_longlong, [_P, C.c_int]),
+    "mcgen_gb300_plan_shape": (C.c_int, [_P]),
+    "mcgen_gb300_plan_autotune": (C.c_int, [_P, _P, C.c_int, C.POINTER(C.c_double)]),
+    "mcgen_gb300_plan_run_dev": (C.c_int, [_P, _P, _P]),
+    "mcgen_gb300_plan_run_dev_direct": (C.c_int, [_P, _P, _P]),
+    "mcgen_gb300_plan_run": (C.c_int, [_P, _P]),
+})
+
+
+class McGb300Request(C.Structure):
+    _fields_ = [("world", _P), ("seed", C.c_int64), ("qx0", C.c_int32), ("qz0", C.c_int32), ("nx", C.c_int32),
+                ("nz", C.c_int32), ("qy", C.c_int32)]
+
+
 _lib = None
 
 
@@ -333,6 +353,67 @@ class World:
         _check(load().mcgen_gb300_biome_grid_dev(self._h, x0, z0, nx, nz, step, y, d_out, stream or None),
                "mcgen_gb300_biome_grid_dev")
 
+    def quart_grid_seed_dev(self, seed, qx0, qz0, nx, nz, qy, tie_rule, d_out: int, stream: int = 0):
+        _check(load().mcgen_gb300_quart_grid_seed_dev(self._h, int(seed), qx0, qz0, nx, nz, qy, tie_rule, d_out,
+                                                      stream or None), "mcgen_gb300_quart_grid_seed_dev")
+
     def quart_grid_dev(self, qx0, qz0, nx, nz, qy, tie_rule, d_out: int, stream: int = 0):
         _check(load().mcgen_gb300_quart_grid_dev(self._h, qx0, qz0, nx, nz, qy, tie_rule, d_out, stream or None),
                "mcgen_gb300_quart_grid_dev")
+
+
+class Plan:
+    """A frozen batch of quart-grid requests (mcgen_gb300_plan_*): [(world, seed, qx0, qz0, nx, nz, qy), ...]."""
+
+    def __init__(self, requests, tie_rule: int = TIE_ENGINE):
+        L = load()
+        arr = (McGb300Request * len(requests))()
+        self._worlds = []
+        for i, (w, seed, qx0, qz0, nx, nz, qy) in enumerate(requests):
+            arr[i] = McGb300Request(w.handle, int(seed), qx0, qz0, nx, nz, qy)
+            self._worlds.append(w)
+        h = _P()
+        _check(L.mcgen_gb300_plan_new(arr, len(requests), tie_rule, C.byref(h)), "mcgen_gb300_plan_new")
+        self._h = h
+        self.n = len(requests)
+        self.shapes = [(r[4], r[5]) for r in requests]
+
+    def close(self):
+        if self._h:
+            load().mcgen_gb300_plan_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def output_bytes(self) -> int:
+        return load().mcgen_gb300_plan_output_bytes(self._h)
+
+    def offset(self, i: int) -> int:
+        return load().mcgen_gb300_plan_output_offset(self._h, i)
+
+    @property
+    def shape(self) -> int:
+        return load().mcgen_gb300_plan_shape(self._h)
+
+    def autotune(self, d_out: int, reps: int = 2) -> float:
+        ms = C.c_double()
+        _check(load().mcgen_gb300_plan_autotune(self._h, d_out, reps, C.byref(ms)), "mcgen_gb300_plan_autotune")
+        return ms.value
+
+    def run_dev(self, d_out: int, stream: int = 0, graph: bool = True):
+        f = load().mcgen_gb300_plan_run_dev if graph else load().mcgen_gb300_plan_run_dev_direct
+        _check(f(self._h, d_out, stream or None), "mcgen_gb300_plan_run_dev")
+
+    def run(self, out: np.ndarray | None = None) -> np.ndarray:
+        out = np.empty(self.output_bytes, np.uint8) if out is None else out
+        _check(load().mcgen_gb300_plan_run(self._h, _ptr(out)), "mcgen_gb300_plan_run")
+        return out
+
+    def split(self, flat: np.ndarray) -> list:
+        """Per-request (nz, nx) views of a flat output."""
+        return [flat[self.offset(i):self.offset(i) + nx * nz].reshape(nz, nx) for i, (nx, nz) in enumerate(self.shapes)]

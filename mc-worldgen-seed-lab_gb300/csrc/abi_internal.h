@@ -27,8 +27,15 @@ struct McWorld {
     MgLattice *d_state;
 };
 
+#include <cuda_runtime.h>
+
 namespace mg {
 std::mutex &abi_lock(); /* serialises GPU work of all entry points */
 int abi_device();       /* the device the library runs on */
+/* with abi_lock held: select and initialise the device (1 = ready), give the library's stream, put a
+ * world's tree and seed lattices on the device (MCGEN_OK or an error code) */
+int abi_device_ready();
+cudaStream_t abi_stream();
+int abi_world_device(McWorld *w);
 }  // namespace mg
 #endif

@@ -166,6 +166,9 @@ int block_biomes_dev(const McWorld *w, int x0, int z0, int nx, int nz, int step,
 namespace mg {
 std::mutex &abi_lock() { return g_lock; }
 int abi_device() { return g_device; }
+int abi_device_ready() { return device_ready_locked(); }
+cudaStream_t abi_stream() { return g_stream; }
+int abi_world_device(McWorld *w) { return world_device_locked(w); }
 }  // namespace mg
 
 /* ============================================================================ version, data */
@@ -541,6 +544,31 @@ MCGEN_API int mcgen_gb300_biome_grid_dev(const McWorld *w, int x0, int z0, int n
     int rc = world_device_locked(const_cast<McWorld *>(w));
     if (rc) return rc;
     return block_biomes_dev(w, x0, z0, nx, nz, step, y, nullptr, x0, x1, z0, z1, d_out, (cudaStream_t)stream);
+}
+
+/* One request the plain way: its seed's lattices into stream-ordered scratch, then one grid launch. */
+MCGEN_API int mcgen_gb300_quart_grid_seed_dev(const McWorld *w, int64_t seed, int qx0, int qz0, int nx, int nz, int qy,
+                                              int tie_rule, uint8_t *d_out, void *stream) {
+    if (!w || !d_out || nx <= 0 || nz <= 0) return MCGEN_E_ARG;
+    if (tie_rule != MCGEN_TIE_ENGINE && tie_rule != MCGEN_TIE_GRID_CHAIN) return MCGEN_E_ARG;
+    std::lock_guard<std::mutex> lk(g_lock);
+    if (!device_ready_locked()) return MCGEN_E_UNSUPPORTED;
+    int rc = world_device_locked(const_cast<McWorld *>(w));
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    DevBuf state(st), d_seed(st), scratch(st);
+    cudaError_t e;
+    if ((e = state.alloc(sizeof(MgLattice) * (size_t)w->desc.ntables)) || (e = d_seed.alloc(sizeof(int64_t))))
+        return cuda_code(e);
+    if ((e = cudaMemcpyAsync(d_seed.p, &seed, sizeof seed, cudaMemcpyHostToDevice, st))) return cuda_code(e);
+    if ((rc = mg::launch_setup(w->desc, (const int64_t *)d_seed.p, 1, (MgLattice *)state.p, st))) return cuda_code((cudaError_t)rc);
+    size_t sb = 0;
+    if (w->dim == MG_END) sb = (size_t)(nx / 4 + 3) * (size_t)(nz / 4 + 3);
+    else if (tie_rule == MCGEN_TIE_GRID_CHAIN) sb = mg::chain_scratch_bytes((long long)nx * nz);
+    if ((e = scratch.alloc(sb))) return cuda_code(e);
+    rc = mg::launch_quart_grid(w->desc, w->d_tree, (const MgLattice *)state.p, qx0, qz0, nx, nz, qy, tie_rule, d_out,
+                               scratch.p, st);
+    return rc ? cuda_code((cudaError_t)rc) : MCGEN_OK;
 }
 
 MCGEN_API long long mcgen_gb300_launch_count(void) { return mg::launch_count(); }

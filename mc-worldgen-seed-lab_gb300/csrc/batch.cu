@@ -1,0 +1,360 @@
+/* batch.cu -- many biome-map requests of uneven size in one persistent launch.
+ *
+ * A request is (world: version + dimension + preset, seed, quart region qx0..qx0+nx-1 x qz0..qz0+nz-1 at
+ * quart y, tie rule).  The host splits every request into tiles -- 128 quart cells (32 x 4, 16 x 8, 64 x 2
+ * or 8 x 16: the autotuner picks the shape) for Overworld and Nether, 8 x 8 chunks (32 x 32 quart cells)
+ * for the End -- and numbers them.  k_batch runs one CTA per
+ * SM slot for the whole batch; each CTA takes the next tile from a device counter (the work queue), finds
+ * its request by binary search over the requests' first-tile numbers, stages that request's seed lattices
+ * and its world's offset spline in shared memory when they differ from the previous tile's, and computes
+ * the tile.  Uneven requests therefore cost no idle SMs and no per-request launches.
+ *
+ * The seed lattices of every (world, seed) of the batch are built beforehand by k_setup_list_* into a
+ * state pool (the served form keeps that pool across batches as a device cache).
+ *
+ * End tiles: the class of chunk (cx, cz) needs the island noise over the 25 x 25 chunk cells around it
+ * (engine/mc_end.h:66-93).  An 8 x 8-chunk tile evaluates the (8+24)^2 simplex cells of its window once
+ * into shared memory (island flag and size) instead of 64 x 625 evaluations, then each chunk scans its
+ * window there.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "batch.h"
+#include "climate.cuh"
+#include "launch.h"
+#include "prof.h"
+
+namespace mg {
+
+#define BNT 128        /* threads per CTA: one quart cell per thread in Overworld / Nether tiles */
+#define END_TC 8       /* chunks per End tile side */
+#define END_WIN (END_TC + 24)
+
+/* ---------------------------------------------------------------- setup of a list of (world, seed) */
+#define LNT 128
+__device__ __forceinline__ void lst_swap(uint8_t *mine, int i, int j) {
+    uint8_t *a = mine + (i >> 2) * (4 * LNT) + (i & 3);
+    uint8_t *b = mine + (j >> 2) * (4 * LNT) + (j & 3);
+    uint8_t x = *a, y = *b;
+    *a = y;
+    *b = x;
+}
+__device__ __forceinline__ void lst_store(uint32_t (*perm)[LNT], int t, MgLattice &h, MgLattice *L) {
+    lattice_header(h);
+    const uint4 *src = reinterpret_cast<const uint4 *>(&h);
+    uint4 *dst = reinterpret_cast<uint4 *>(L);
+    for (int q = 0; q < 4; q++) dst[q] = src[q];
+    uint4 *dp = reinterpret_cast<uint4 *>(L->p);
+    for (int q = 0; q < 16; q++) dp[q] = make_uint4(perm[4 * q][t], perm[4 * q + 1][t], perm[4 * q + 2][t], perm[4 * q + 3][t]);
+}
+/* Overworld entries: one thread per (entry, lattice). */
+__global__ void __launch_bounds__(LNT) k_setup_list_xo(const MgWorldDesc *__restrict__ worlds, const MgSetupEntry *__restrict__ ent,
+                                                       int n, const int *__restrict__ first_lattice, long long total,
+                                                       MgLattice *__restrict__ pool) {
+    __shared__ uint32_t perm[64][LNT];
+    const int t = threadIdx.x;
+    const long long g = (long long)blockIdx.x * LNT + t;
+    if (g >= total) return;
+    int lo = 0, hi = n - 1; /* entry e with first_lattice[e] <= g < first_lattice[e+1] */
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (first_lattice[mid] <= g) lo = mid; else hi = mid - 1;
+    }
+    const MgSetupEntry &E = ent[lo];
+    const MgWorldDesc &W = worlds[E.world];
+    const int j = (int)(g - first_lattice[lo]);
+    int i = 0;
+    while (i < MG_OW_NOISES - 1 && j >= W.noise[i + 1].base) i++;
+    const MgNoise &N = W.noise[i];
+    const int r = j - N.base, st = r >= N.nlev, k = r - st * N.nlev;
+    Xo root = xo_from_seed(E.seed);
+    uint64_t plo = xo_next(root), phi = xo_next(root);
+    Xo nr = xo_make(W.nhl[i] ^ plo, W.nhh[i] ^ phi);
+    uint64_t a = xo_next(nr), b = xo_next(nr);
+    if (st) { a = xo_next(nr); b = xo_next(nr); }
+    Xo x = xo_make(N.hlo[k] ^ a, N.hhi[k] ^ b);
+    MgLattice h;
+    h.ox = xo_double(x) * 256.0;
+    h.oy = xo_double(x) * 256.0;
+    h.oz = xo_double(x) * 256.0;
+    for (int w = 0; w < 64; w++) perm[w][t] = 0x03020100u + 0x04040404u * (uint32_t)w;
+    uint8_t *mine = reinterpret_cast<uint8_t *>(&perm[0][t]);
+    for (int q = 0; q < 256; q++) lst_swap(mine, q, q + xo_int(x, 256u - (uint32_t)q));
+    lst_store(perm, t, h, pool + E.slot + j);
+}
+/* Nether entries: one thread per (entry, noise); End entries: one thread per entry. */
+__device__ __forceinline__ void lst_legacy(uint64_t &s, uint32_t (*perm)[LNT], int t, MgLattice *L) {
+    MgLattice h;
+    h.ox = lcg_double(s) * 256.0;
+    h.oy = lcg_double(s) * 256.0;
+    h.oz = lcg_double(s) * 256.0;
+    for (int w = 0; w < 64; w++) perm[w][t] = 0x03020100u + 0x04040404u * (uint32_t)w;
+    uint8_t *mine = reinterpret_cast<uint8_t *>(&perm[0][t]);
+    for (int q = 0; q < 256; q++) lst_swap(mine, q, q + lcg_int(s, 256 - q));
+    if (L) lst_store(perm, t, h, L);
+}
+__global__ void __launch_bounds__(LNT) k_setup_list_legacy(const MgWorldDesc *__restrict__ worlds,
+                                                           const MgSetupEntry *__restrict__ ent, int n,
+                                                           MgLattice *__restrict__ pool) {
+    __shared__ uint32_t perm[64][LNT];
+    const int t = threadIdx.x;
+    const long long g = (long long)blockIdx.x * LNT + t;
+    if (g >= 2LL * n) return;
+    const MgSetupEntry &E = ent[g >> 1];
+    const MgWorldDesc &W = worlds[E.world];
+    const int nz = (int)(g & 1);
+    const MgNoise &N = W.nether[nz];
+    uint64_t st = lcg_init((int64_t)((uint64_t)E.seed + (uint64_t)nz));
+    MgLattice *T = pool + E.slot + N.base;
+    int slot[MG_MAX_OCT];
+    for (int q = 0; q < MG_MAX_OCT; q++) slot[q] = -1;
+    for (int k = 0; k < N.nlev; k++) slot[N.idx[k]] = k;
+    const int zero = -N.first;
+    for (int stack = 0; stack < 2; stack++) {
+        MgLattice *S = T + stack * N.nlev;
+        const bool keep_zero = zero >= 0 && zero < N.octs && slot[zero] >= 0;
+        lst_legacy(st, perm, t, keep_zero ? S + slot[zero] : nullptr);
+        for (int q = zero - 1; q >= 0; q--) {
+            if (q < N.octs && slot[q] >= 0) lst_legacy(st, perm, t, S + slot[q]);
+            else st = lcg_jump(st, 262);
+        }
+    }
+}
+__global__ void __launch_bounds__(LNT) k_setup_list_end(const MgSetupEntry *__restrict__ ent, int n, MgLattice *__restrict__ pool) {
+    __shared__ uint32_t perm[64][LNT];
+    const long long g = (long long)blockIdx.x * LNT + threadIdx.x;
+    if (g >= n) return;
+    uint64_t st = lcg_jump(lcg_init(ent[g].seed), 17292);
+    lst_legacy(st, perm, threadIdx.x, pool + ent[g].slot);
+}
+
+/* ---------------------------------------------------------------- the persistent batch kernel */
+struct BatchSmem {
+    MgSpline spline;
+    MgLattice lat[MG_MAX_TABLES];
+    uint8_t endp[256];
+    uint8_t island[END_WIN * END_WIN]; /* 0: no island, else (float) size in sz[] */
+    float isize[END_WIN * END_WIN];
+    uint8_t cls[END_TC * END_TC];
+    int tile, req, state, world;
+};
+
+template <bool FM, int DIM, int TILE_W>
+__device__ __forceinline__ void batch_cells(const MgWorldDesc &W, const MgSpline &S, const MgLattice *T,
+                                            const MgTreeNode *tree, const MgBatchReq &R, int tx0, int tz0,
+                                            uint8_t *out) {
+    const int ix = tx0 + (threadIdx.x % TILE_W), iz = tz0 + (threadIdx.x / TILE_W);
+    if (ix >= R.nx || iz >= R.nz) return;
+    const int qx = R.qx0 + ix, qz = R.qz0 + iz;
+    uint8_t b;
+    if (R.tie == MG_TIE_CHUNK_CELL) {
+        b = (uint8_t)cell_chunk<FM, DIM>(W, S, T, tree, qx, R.qy, qz);
+    } else {
+        int32_t tg[6];
+        cell_target<FM, DIM>(W, S, T, qx, R.qy, qz, tg);
+        uint64_t d;
+        b = tree[tree_search(tree, tg, -1, d)].biome;
+    }
+    out[R.out_off + (size_t)iz * R.nx + ix] = b;
+}
+
+/* End tile: chunks [cx0, cx0 + END_TC) x [cz0, cz0 + END_TC) counted from the chunk of the request's
+ * first cell; the tile writes the request's cells that lie in those chunks. */
+template <bool FM>
+__device__ __forceinline__ void batch_end(const MgWorldDesc &W, BatchSmem &sm, const MgBatchReq &R, int tcx, int tcz,
+                                          uint8_t *out) {
+    const int cx0 = (R.qx0 >> 2) + tcx * END_TC, cz0 = (R.qz0 >> 2) + tcz * END_TC;
+    /* chunk c's height reads chunk cells c' + d, d in [-12, 12], with c' = (2c+1)/2 in Java int division
+     * (c for c >= 0, c + 1 for c < 0): a window of at most END_TC - 1 + 25 cells per axis */
+    const int wx0 = (cx0 * 2 + 1) / 2 - 12, wz0 = (cz0 * 2 + 1) / 2 - 12;
+    for (int i = threadIdx.x; i < END_WIN * END_WIN; i += blockDim.x) {
+        const long long tx = (long long)wx0 + i % END_WIN, tz = (long long)wz0 + i / END_WIN;
+        uint8_t isl = 0;
+        float size = 0.0f;
+        if (tx * tx + tz * tz > 4096LL) {
+            const double nv = simplex2(sm.endp, (double)tx, (double)tz, W.end_f2, W.end_g2);
+            isl = FM ? ((float)nv < -0.9f) : (nv < (double)-0.9f);
+            if (isl) size = fmodf(fabsf((float)tx) * 3439.0f + fabsf((float)tz) * 147.0f, 13.0f) + 9.0f;
+        }
+        sm.island[i] = isl;
+        sm.isize[i] = size;
+    }
+    __syncthreads();
+    if (threadIdx.x < END_TC * END_TC) {
+        const int cx = cx0 + threadIdx.x % END_TC, cz = cz0 + threadIdx.x / END_TC;
+        int cls = 0;
+        if ((long long)cx * cx + (long long)cz * cz > 4096LL) {
+            const int bx = (cx * 2 + 1) * 8, bz = (cz * 2 + 1) * 8;
+            const int sx = bx / 8, sz = bz / 8;
+            const int ccx = sx / 2, ccz = sz / 2, ox = sx % 2, oz = sz % 2;
+            float best;
+            if (!FM) {
+                int32_t sq = (int32_t)((uint32_t)sx * (uint32_t)sx + (uint32_t)sz * (uint32_t)sz);
+                float len = (float)sqrt((double)(float)sq);
+                best = clampf(100.0f - len * 8.0f, -100.0f, 80.0f);
+            } else best = -100.0f;
+            for (int dx = -12; dx <= 12; dx++)
+                for (int dz = -12; dz <= 12; dz++) {
+                    const int wi = (ccz + dz - wz0) * END_WIN + (ccx + dx - wx0);
+                    if (!sm.island[wi]) continue;
+                    const float xd = (float)(ox - dx * 2), zd = (float)(oz - dz * 2);
+                    const float h = clampf(100.0f - (float)sqrt((double)(xd * xd + zd * zd)) * sm.isize[wi], -100.0f, 80.0f);
+                    best = best > h ? best : h;
+                }
+            double e;
+            if (!FM) e = ((double)best - 8.0) / 128.0;
+            else {
+                const float ddx = (float)(0 - bx), ddz = (float)(0 - bz);
+                const float len = (float)sqrt((double)(ddx * ddx + 0.0f * 0.0f + ddz * ddz));
+                const float c = (clampf(100.0f - len, -100.0f, 80.0f) - 8.0f) * 0.0078125f;
+                const float o = (best - 8.0f) / 128.0f;
+                e = (double)(c > o ? c : o);
+            }
+            cls = e > 0.25 ? 1 : (e >= -0.0625 ? 2 : (e < -0.21875 ? 3 : 4));
+        }
+        sm.cls[threadIdx.x] = (uint8_t)cls;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 16 * END_TC * END_TC; i += blockDim.x) {
+        const int qx = 4 * cx0 + i % (4 * END_TC), qz = 4 * cz0 + i / (4 * END_TC);
+        const int ix = qx - R.qx0, iz = qz - R.qz0;
+        if (ix < 0 || iz < 0 || ix >= R.nx || iz >= R.nz) continue;
+        out[R.out_off + (size_t)iz * R.nx + ix] = (uint8_t)W.end_ids[sm.cls[(i / (16 * END_TC)) * END_TC + (i % (4 * END_TC)) / 4]];
+    }
+}
+
+template <int TILE_W>
+__global__ void __launch_bounds__(BNT) k_batch(const MgWorldDesc *__restrict__ worlds, const MgTreeNode *const *__restrict__ trees,
+                                               const MgBatchReq *__restrict__ reqs, int nreq, long long ntiles,
+                                               const MgLattice *__restrict__ pool, unsigned long long *__restrict__ counter,
+                                               uint8_t *__restrict__ out) {
+    extern __shared__ uint4 smem_raw[];
+    BatchSmem &sm = *reinterpret_cast<BatchSmem *>(smem_raw);
+    if (threadIdx.x == 0) { sm.state = -1; sm.world = -1; }
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            long long tile = (long long)atomicAdd(counter, 1ULL);
+            int r = -1;
+            if (tile < ntiles) {
+                int lo = 0, hi = nreq - 1;
+                while (lo < hi) {
+                    int mid = (lo + hi + 1) >> 1;
+                    if (reqs[mid].tile0 <= tile) lo = mid; else hi = mid - 1;
+                }
+                r = lo;
+            }
+            sm.tile = (int)(tile < ntiles ? tile - reqs[r < 0 ? 0 : r].tile0 : -1);
+            sm.req = r;
+        }
+        __syncthreads();
+        const int r = sm.req;
+        if (r < 0) return;
+        const MgBatchReq R = reqs[r];
+        const MgWorldDesc &W = worlds[R.world];
+        /* stage the world's spline and the request's lattices when they change */
+        const bool new_world = R.world != sm.world, new_state = R.state != sm.state;
+        if (new_world && W.dim == MG_OVERWORLD) {
+            const uint4 *c = reinterpret_cast<const uint4 *>(&W.spline);
+            uint4 *d = reinterpret_cast<uint4 *>(&sm.spline);
+            for (int i = threadIdx.x; i < (int)(sizeof(MgSpline) / 16); i += BNT) d[i] = c[i];
+        }
+        if (new_state) {
+            if (W.dim == MG_END) {
+                for (int i = threadIdx.x; i < 256; i += BNT) sm.endp[i] = pool[R.state].p[i];
+            } else {
+                const uint4 *a = reinterpret_cast<const uint4 *>(pool + R.state);
+                uint4 *b = reinterpret_cast<uint4 *>(sm.lat);
+                for (int i = threadIdx.x; i < W.ntables * (int)(sizeof(MgLattice) / 16); i += BNT) b[i] = a[i];
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) { sm.world = R.world; sm.state = R.state; }
+        const int tile = sm.tile;
+        if (W.dim == MG_END) {
+            const int ncx = ((R.qx0 + R.nx - 1) >> 2) - (R.qx0 >> 2) + 1;
+            const int tw = (ncx + END_TC - 1) / END_TC;
+            if (W.fmode) batch_end<true>(W, sm, R, tile % tw, tile / tw, out);
+            else batch_end<false>(W, sm, R, tile % tw, tile / tw, out);
+            continue;
+        }
+        constexpr int TILE_H = BNT / TILE_W;
+        const int tw = (R.nx + TILE_W - 1) / TILE_W;
+        const int tx0 = (tile % tw) * TILE_W, tz0 = (tile / tw) * TILE_H;
+        const MgTreeNode *tree = trees[R.world];
+        if (W.fmode) {
+            if (W.dim == MG_OVERWORLD) batch_cells<true, MG_OVERWORLD, TILE_W>(W, sm.spline, sm.lat, tree, R, tx0, tz0, out);
+            else batch_cells<true, MG_NETHER, TILE_W>(W, sm.spline, sm.lat, tree, R, tx0, tz0, out);
+        } else {
+            if (W.dim == MG_OVERWORLD) batch_cells<false, MG_OVERWORLD, TILE_W>(W, sm.spline, sm.lat, tree, R, tx0, tz0, out);
+            else batch_cells<false, MG_NETHER, TILE_W>(W, sm.spline, sm.lat, tree, R, tx0, tz0, out);
+        }
+    }
+}
+
+/* ---------------------------------------------------------------- host side */
+const int kBatchTileWidths[BATCH_SHAPES] = {32, 16, 64, 8};
+
+long long batch_tiles(int dim, int qx0, int qz0, int nx, int nz, int shape) {
+    if (dim == MG_END) {
+        const long long ncx = ((qx0 + nx - 1) >> 2) - (qx0 >> 2) + 1, ncz = ((qz0 + nz - 1) >> 2) - (qz0 >> 2) + 1;
+        return ((ncx + END_TC - 1) / END_TC) * ((ncz + END_TC - 1) / END_TC);
+    }
+    const int tw = kBatchTileWidths[shape], th = BNT / tw;
+    return (long long)((nx + tw - 1) / tw) * ((nz + th - 1) / th);
+}
+
+int launch_setup_list(const MgWorldDesc *d_worlds, int dim, const MgSetupEntry *d_ent, int n, const int *d_first,
+                      long long total_lattices, MgLattice *d_pool, cudaStream_t st) {
+    if (n <= 0) return 0;
+    if (dim == MG_OVERWORLD) {
+        ProfScope ps_(K_SETUP_XO, st);
+        k_setup_list_xo<<<(unsigned)((total_lattices + LNT - 1) / LNT), LNT, 0, st>>>(d_worlds, d_ent, n, d_first, total_lattices, d_pool);
+    } else if (dim == MG_NETHER) {
+        ProfScope ps_(K_SETUP_LEGACY, st);
+        k_setup_list_legacy<<<(unsigned)((2LL * n + LNT - 1) / LNT), LNT, 0, st>>>(d_worlds, d_ent, n, d_pool);
+    } else {
+        ProfScope ps_(K_SETUP_END, st);
+        k_setup_list_end<<<(unsigned)((n + LNT - 1) / LNT), LNT, 0, st>>>(d_ent, n, d_pool);
+    }
+    count_launch_external();
+    return (int)cudaGetLastError();
+}
+
+template <int TW>
+static int prepare_t() {
+    return (int)cudaFuncSetAttribute(k_batch<TW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BatchSmem));
+}
+/* kernel attributes (before any capture) and resident CTAs per SM */
+int batch_prepare(int *ctas_per_sm) {
+    int rc = prepare_t<32>();
+    if (!rc) rc = prepare_t<16>();
+    if (!rc) rc = prepare_t<64>();
+    if (!rc) rc = prepare_t<8>();
+    int n = 0;
+    if (!rc) rc = (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<32>, BNT, sizeof(BatchSmem));
+    if (ctas_per_sm) *ctas_per_sm = n > 0 ? n : 1;
+    return rc;
+}
+
+int launch_batch(const MgWorldDesc *d_worlds, const MgTreeNode *const *d_trees, const MgBatchReq *d_reqs, int nreq,
+                 long long ntiles, const MgLattice *d_pool, unsigned long long *d_counter, uint8_t *d_out, int ctas,
+                 int shape, cudaStream_t st) {
+    if (ntiles <= 0) return 0;
+    cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st);
+    if (e) return (int)e;
+    if ((long long)ctas > ntiles) ctas = (int)ntiles;
+    ProfScope ps_(K_BATCH, st);
+    const size_t sm = sizeof(BatchSmem);
+    switch (shape) {
+    case 1: k_batch<16><<<ctas, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
+    case 2: k_batch<64><<<ctas, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
+    case 3: k_batch<8><<<ctas, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
+    default: k_batch<32><<<ctas, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
+    }
+    count_launch_external();
+    return (int)cudaGetLastError();
+}
+
+}  // namespace mg

@@ -1,0 +1,273 @@
+/* plan.cpp -- the batched form's host side: McGb300Plan (mcgen_gb300_plan_*).
+ *
+ * A plan freezes a list of requests: it uploads the distinct worlds (descriptions and R-tree pointers),
+ * assigns every distinct (world, seed) a slot in a lattice pool, numbers the tiles of every request
+ * (batch.cu), and lays the outputs out back to back.  Running it enqueues the per-seed setup launches (one
+ * per dimension present) and the persistent k_batch launch.  The first run on a stream captures those
+ * launches into a CUDA graph on a private stream and later runs replay it; the tile shape is chosen by
+ * timing the four shapes on the plan itself (mcgen_gb300_plan_autotune).
+ */
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "../../include/mcgen_gb300.h"
+#include "abi_internal.h"
+#include "batch.h"
+#include "launch.h"
+
+struct McGb300Plan {
+    int nreq = 0;
+    long long ntiles[BATCH_SHAPES] = {0, 0, 0, 0};
+    long long out_bytes = 0;
+    std::vector<long long> out_off;
+    std::vector<long long> cells;
+    int shape = 0;
+    int ctas = 0;
+    /* device */
+    MgWorldDesc *d_worlds = nullptr;
+    const MgTreeNode **d_trees = nullptr;
+    MgBatchReq *d_reqs[BATCH_SHAPES] = {nullptr, nullptr, nullptr, nullptr};
+    MgSetupEntry *d_ent[3] = {nullptr, nullptr, nullptr};
+    int nent[3] = {0, 0, 0};
+    int *d_first = nullptr; /* Overworld: first lattice of each entry, relative to the Overworld list */
+    long long ow_lattices = 0;
+    MgLattice *d_pool = nullptr;
+    unsigned long long *d_counter = nullptr;
+    /* graph of one run */
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint8_t *graph_out = nullptr;
+    int graph_shape = -1;
+};
+
+namespace {
+
+int cuda_rc(cudaError_t e) { return e == cudaSuccess ? MCGEN_OK : e == cudaErrorMemoryAllocation ? MCGEN_E_NOMEM : MCGEN_E_INTERNAL; }
+
+int enqueue(McGb300Plan *p, uint8_t *d_out, int shape, cudaStream_t st) {
+    for (int d = 0; d < 3; d++) {
+        if (!p->nent[d]) continue;
+        int rc = mg::launch_setup_list(p->d_worlds, d, p->d_ent[d], p->nent[d], p->d_first, p->ow_lattices, p->d_pool, st);
+        if (rc) return rc;
+    }
+    return mg::launch_batch(p->d_worlds, p->d_trees, p->d_reqs[shape], p->nreq, p->ntiles[shape], p->d_pool,
+                            p->d_counter, d_out, p->ctas, shape, st);
+}
+
+void free_plan(McGb300Plan *p) {
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->cap) cudaStreamDestroy(p->cap);
+    cudaFree(p->d_worlds);
+    cudaFree((void *)p->d_trees);
+    for (auto *r : p->d_reqs) cudaFree(r);
+    for (auto *e : p->d_ent) cudaFree(e);
+    cudaFree(p->d_first);
+    cudaFree(p->d_pool);
+    cudaFree(p->d_counter);
+    delete p;
+}
+
+}  // namespace
+
+extern "C" {
+
+MCGEN_API int mcgen_gb300_plan_new(const McGb300Request *reqs, int n, int tie_rule, McGb300Plan **out) {
+    if (!out || n < 0 || (n > 0 && !reqs)) return MCGEN_E_ARG;
+    if (tie_rule != MCGEN_TIE_ENGINE && tie_rule != MCGEN_TIE_CHUNK_CELL) return MCGEN_E_ARG;
+    *out = nullptr;
+    for (int i = 0; i < n; i++) {
+        const McGb300Request &r = reqs[i];
+        if (!r.world || r.nx <= 0 || r.nz <= 0 || (long long)r.nx * r.nz > (1LL << 31)) return MCGEN_E_ARG;
+        if ((long long)r.qx0 + r.nx > INT32_MAX || (long long)r.qz0 + r.nz > INT32_MAX) return MCGEN_E_ARG;
+    }
+    std::lock_guard<std::mutex> lk(mg::abi_lock());
+    if (!mg::abi_device_ready()) return MCGEN_E_UNSUPPORTED;
+    McGb300Plan *p = new McGb300Plan();
+    p->nreq = n;
+    /* distinct worlds; each must have its device copy (tree) */
+    std::map<const McWorld *, int> widx;
+    std::vector<const McWorld *> worlds;
+    for (int i = 0; i < n; i++)
+        if (!widx.count(reqs[i].world)) { widx[reqs[i].world] = (int)worlds.size(); worlds.push_back(reqs[i].world); }
+    for (auto *w : worlds) {
+        int rc = mg::abi_world_device(const_cast<McWorld *>(w));
+        if (rc) { free_plan(p); return rc; }
+    }
+    /* distinct (world, seed) -> pool slots, grouped by dimension */
+    std::map<std::pair<int, int64_t>, int> slot_of;
+    std::vector<MgSetupEntry> ent[3];
+    std::vector<int> first;
+    long long pool = 0, ow = 0;
+    for (int i = 0; i < n; i++) {
+        const int wi = widx[reqs[i].world];
+        auto key = std::make_pair(wi, (int64_t)reqs[i].seed);
+        if (slot_of.count(key)) continue;
+        const MgWorldDesc &W = worlds[(size_t)wi]->desc;
+        MgSetupEntry e;
+        e.seed = reqs[i].seed;
+        e.world = wi;
+        e.slot = (int32_t)pool;
+        slot_of[key] = (int)pool;
+        if (W.dim == MG_OVERWORLD) { first.push_back((int)ow); ow += W.ntables; }
+        ent[W.dim].push_back(e);
+        pool += W.ntables;
+        if (pool > INT32_MAX) { free_plan(p); return MCGEN_E_ARG; }
+    }
+    p->ow_lattices = ow;
+    /* requests and tiles for every shape; outputs back to back */
+    std::vector<MgBatchReq> rq[BATCH_SHAPES];
+    p->out_off.resize((size_t)n);
+    p->cells.resize((size_t)n);
+    long long off = 0;
+    for (int i = 0; i < n; i++) {
+        p->out_off[(size_t)i] = off;
+        p->cells[(size_t)i] = (long long)reqs[i].nx * reqs[i].nz;
+        off += p->cells[(size_t)i];
+    }
+    p->out_bytes = off;
+    for (int s = 0; s < BATCH_SHAPES; s++) {
+        long long tiles = 0;
+        for (int i = 0; i < n; i++) {
+            const McGb300Request &r = reqs[i];
+            const int wi = widx[r.world];
+            MgBatchReq b;
+            b.world = wi;
+            b.state = slot_of[std::make_pair(wi, (int64_t)r.seed)];
+            b.qx0 = r.qx0; b.qz0 = r.qz0; b.nx = r.nx; b.nz = r.nz; b.qy = r.qy;
+            b.tie = worlds[(size_t)wi]->desc.dim == MG_END ? MG_TIE_ENGINE : tie_rule;
+            b.tile0 = tiles;
+            b.out_off = p->out_off[(size_t)i];
+            tiles += mg::batch_tiles(worlds[(size_t)wi]->desc.dim, r.qx0, r.qz0, r.nx, r.nz, s);
+            rq[s].push_back(b);
+        }
+        p->ntiles[s] = tiles;
+    }
+    /* device copies */
+    cudaError_t e = cudaSuccess;
+    std::vector<MgWorldDesc> wd;
+    std::vector<const MgTreeNode *> tp;
+    for (auto *w : worlds) { wd.push_back(w->desc); tp.push_back(w->d_tree); }
+    auto up = [&](void **dst, const void *src, size_t bytes) {
+        if (e || !bytes) return;
+        if ((e = cudaMalloc(dst, bytes)) == cudaSuccess) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+    };
+    up((void **)&p->d_worlds, wd.data(), sizeof(MgWorldDesc) * wd.size());
+    up((void **)&p->d_trees, tp.data(), sizeof(void *) * tp.size());
+    for (int s = 0; s < BATCH_SHAPES; s++) up((void **)&p->d_reqs[s], rq[s].data(), sizeof(MgBatchReq) * rq[s].size());
+    for (int d = 0; d < 3; d++) {
+        p->nent[d] = (int)ent[d].size();
+        up((void **)&p->d_ent[d], ent[d].data(), sizeof(MgSetupEntry) * ent[d].size());
+    }
+    up((void **)&p->d_first, first.data(), sizeof(int) * first.size());
+    if (!e && pool) e = cudaMalloc(&p->d_pool, sizeof(MgLattice) * (size_t)pool);
+    if (!e) e = cudaMalloc(&p->d_counter, sizeof(unsigned long long));
+    int cps = 1;
+    if (!e) e = (cudaError_t)mg::batch_prepare(&cps);
+    if (e) {
+        free_plan(p);
+        return cuda_rc(e);
+    }
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    p->ctas = sms * cps;
+    *out = p;
+    return MCGEN_OK;
+}
+
+MCGEN_API void mcgen_gb300_plan_free(McGb300Plan *p) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(mg::abi_lock());
+    free_plan(p);
+}
+
+MCGEN_API long long mcgen_gb300_plan_output_bytes(const McGb300Plan *p) { return p ? p->out_bytes : -1; }
+MCGEN_API long long mcgen_gb300_plan_output_offset(const McGb300Plan *p, int i) {
+    return (p && i >= 0 && i < p->nreq) ? p->out_off[(size_t)i] : -1;
+}
+MCGEN_API int mcgen_gb300_plan_shape(const McGb300Plan *p) { return p ? p->shape : -1; }
+
+/* Run into device memory (plan_output_bytes bytes at d_out) on `stream`, through the plan's CUDA graph. */
+MCGEN_API int mcgen_gb300_plan_run_dev(McGb300Plan *p, uint8_t *d_out, void *stream) {
+    if (!p || (!d_out && p->out_bytes)) return MCGEN_E_ARG;
+    if (!p->nreq) return MCGEN_OK;
+    std::lock_guard<std::mutex> lk(mg::abi_lock());
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e;
+    if (!p->exec || p->graph_out != d_out || p->graph_shape != p->shape) {
+        if (p->exec) { cudaGraphExecDestroy(p->exec); p->exec = nullptr; }
+        if (!p->cap && (e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking))) return cuda_rc(e);
+        if ((e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal))) return cuda_rc(e);
+        int rc = enqueue(p, d_out, p->shape, p->cap);
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(p->cap, &g);
+        if (rc || e) { if (g) cudaGraphDestroy(g); return rc ? MCGEN_E_INTERNAL : cuda_rc(e); }
+        e = cudaGraphInstantiate(&p->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e) { p->exec = nullptr; return cuda_rc(e); }
+        p->graph_out = d_out;
+        p->graph_shape = p->shape;
+    }
+    return cuda_rc(cudaGraphLaunch(p->exec, st));
+}
+
+/* The same without a graph (each launch visible to the library's per-kernel profiler). */
+MCGEN_API int mcgen_gb300_plan_run_dev_direct(McGb300Plan *p, uint8_t *d_out, void *stream) {
+    if (!p || (!d_out && p->out_bytes)) return MCGEN_E_ARG;
+    std::lock_guard<std::mutex> lk(mg::abi_lock());
+    int rc = enqueue(p, d_out, p->shape, (cudaStream_t)stream);
+    return rc ? MCGEN_E_INTERNAL : MCGEN_OK;
+}
+
+/* Time every tile shape on the plan itself (reps runs each, after one warm-up) and keep the fastest.
+ * d_out: a device buffer of plan_output_bytes. */
+MCGEN_API int mcgen_gb300_plan_autotune(McGb300Plan *p, uint8_t *d_out, int reps, double *best_ms) {
+    if (!p || (!d_out && p->out_bytes) || reps <= 0) return MCGEN_E_ARG;
+    std::lock_guard<std::mutex> lk(mg::abi_lock());
+    cudaStream_t st;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) return MCGEN_E_INTERNAL;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    double best = 1e30;
+    int best_s = 0, rc = 0;
+    for (int s = 0; s < BATCH_SHAPES && !rc; s++) {
+        rc = enqueue(p, d_out, s, st);
+        cudaEventRecord(a, st);
+        for (int r = 0; r < reps && !rc; r++) rc = enqueue(p, d_out, s, st);
+        cudaEventRecord(b, st);
+        if (cudaEventSynchronize(b)) rc = MCGEN_E_INTERNAL;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (!rc && ms / reps < best) { best = ms / reps; best_s = s; }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaStreamDestroy(st);
+    if (rc) return MCGEN_E_INTERNAL;
+    p->shape = best_s;
+    if (best_ms) *best_ms = best;
+    return MCGEN_OK;
+}
+
+/* Host-buffer form: runs the plan and copies the outputs to `out` (plan_output_bytes bytes). */
+MCGEN_API int mcgen_gb300_plan_run(McGb300Plan *p, uint8_t *out) {
+    if (!p || (!out && p->out_bytes)) return MCGEN_E_ARG;
+    if (!p->nreq) return MCGEN_OK;
+    uint8_t *d_out = nullptr;
+    cudaStream_t st = mg::abi_stream();
+    cudaError_t e = cudaMallocAsync((void **)&d_out, (size_t)p->out_bytes, st);
+    if (e) return cuda_rc(e);
+    int rc = mcgen_gb300_plan_run_dev(p, d_out, st);
+    if (!rc) rc = cuda_rc(cudaMemcpyAsync(out, d_out, (size_t)p->out_bytes, cudaMemcpyDeviceToHost, st));
+    cudaFreeAsync(d_out, st);
+    cudaError_t e2 = cudaStreamSynchronize(st);
+    return rc ? rc : cuda_rc(e2);
+}
+
+}  // extern "C"

@@ -22,7 +22,7 @@ const size_t kPool = 1 << 14;
 const char *kernel_name(int kid) {
     static const char *const n[K_NUM_KERNELS] = {"k_setup_xo", "k_setup_legacy", "k_setup_end", "k_points", "k_grid",
                                                  "k_chain_resolve", "k_blockgrid", "k_end_chunks", "k_end_lookup",
-                                                 "k_ow_seed_climate", "k_ow_finish_tree"};
+                                                 "k_ow_seed_climate", "k_ow_finish_tree", "k_batch"};
     return (kid >= 0 && kid < K_NUM_KERNELS) ? n[kid] : "?";
 }
 
@@ -40,6 +40,8 @@ static void drain_locked() {
 
 void prof_mark(int kid, cudaStream_t st, bool end) {
     if (!enabled.load(std::memory_order_relaxed)) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return; /* graphs: not timed */
     std::lock_guard<std::mutex> lk(m);
     if (!end) {
         if (next_event + 2 > pool.size()) drain_locked();

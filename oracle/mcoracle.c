@@ -1471,3 +1471,17 @@ uint64_t or_fnv1a64_names(const uint8_t *ids, size_t n) {
     }
     return h;
 }
+
+/* Quart grid where every cell takes the biome its chunk stores (chunk-cell tie chain,
+ * libmcgen/src/biome.c:87-114): out[iz*nx+ix] for (qx0+ix, qy, qz0+iz). */
+void or_chunk_grid(const OrWorld *w, int64_t seed, int qx0, int qz0, int nx, int nz, int qy, uint8_t *out, int threads) {
+#pragma omp parallel num_threads(nthreads(threads))
+    {
+        SeedState *st = (SeedState *)malloc(sizeof(SeedState));
+        seed_init(w, seed, st);
+#pragma omp for schedule(dynamic, 1)
+        for (int iz = 0; iz < nz; iz++)
+            for (int ix = 0; ix < nx; ix++) out[(size_t)iz * nx + ix] = (u8)cell_chunk(w, st, qx0 + ix, qy, qz0 + iz);
+        free(st);
+    }
+}

@@ -84,6 +84,8 @@ int or_biome_at(const OrWorld *w, int64_t seed, int x, int y, int z);
  * (libmcgen/src/region.c:86-122).  Parallel over rows. */
 void or_biome_grid(const OrWorld *w, int64_t seed, int x0, int z0, int nx, int nz, int step, int y,
                    uint8_t *out, int threads);
+/* Quart grid with the chunk-cell tie chain per cell (no zoom). */
+void or_chunk_grid(const OrWorld *w, int64_t seed, int qx0, int qz0, int nx, int nz, int qy, uint8_t *out, int threads);
 /* mcgen_gpu_biome_points semantics: block points xyz[3n]. */
 void or_block_points(const OrWorld *w, int64_t seed, int n, const int32_t *xyz, uint8_t *out, int threads);
 

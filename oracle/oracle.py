@@ -53,6 +53,7 @@ def lib():
         L.or_leaf_biome.restype = i32
         L.or_leaf_biome.argtypes = [vp, i32]
         L.or_points_work.argtypes = [vp, i64, i32p, i32, C.c_void_p]
+        L.or_chunk_grid.argtypes = [vp, i64, i32, i32, i32, i32, i32, u8p, i32]
         L.or_fnv1a64_names.restype = C.c_uint64
         L.or_fnv1a64_names.argtypes = [u8p, C.c_size_t]
         _lib = L
@@ -119,6 +120,11 @@ class World:
                    threads: int = 0) -> np.ndarray:
         out = np.zeros((nz, nx), dtype=np.uint8)
         lib().or_quart_grid(self._h, seed, qx0, qz0, nx, nz, qy, rule, _ptr(out), threads)
+        return out
+
+    def chunk_grid(self, seed: int, qx0: int, qz0: int, nx: int, nz: int, qy: int, threads: int = 0) -> np.ndarray:
+        out = np.zeros((nz, nx), dtype=np.uint8)
+        lib().or_chunk_grid(self._h, seed, qx0, qz0, nx, nz, qy, _ptr(out), threads)
         return out
 
     def biome_at(self, seed: int, x: int, y: int, z: int) -> int:

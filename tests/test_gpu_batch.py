@@ -1,0 +1,99 @@
+"""The batched form (one persistent launch over many uneven requests) against the oracle and against the
+plain one-request-per-launch form: bit-exact per request, for every version and dimension mixed in one
+batch, both tie rules, graph replays, every tile shape of the autotuner."""
+import numpy as np
+import pytest
+
+import __graft_entry__ as ge
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+VERSIONS = ["26.1", "26.2", "26.3", "26.4-snapshot-2"]
+DIMS = ["minecraft:overworld", "minecraft:the_nether", "minecraft:the_end"]
+
+
+@pytest.fixture(scope="module")
+def env():
+    mg = ge.package()
+    mg.load()
+    if mg.device_count() < 1:
+        pytest.fail("no CUDA device")
+    gens = {v: mg.Generator.open(ge.data_root(), v) for v in VERSIONS}
+    worlds = {(v, d): gens[v].world(d, "normal", 0) for v in VERSIONS for d in DIMS}
+    return mg, gens, worlds
+
+
+def mixed_requests(worlds, n=48, seed=9):
+    rng = np.random.default_rng(seed)
+    keys = list(worlds)
+    reqs = []
+    shapes = [(1, 1), (1, 37), (37, 1), (33, 5), (64, 64), (17, 129), (130, 3), (48, 48)]
+    for i in range(n):
+        v, d = keys[i % len(keys)]
+        nx, nz = shapes[i % len(shapes)]
+        qx0 = int(rng.integers(-9000, 9000)) if i % 5 else -nx // 2  # some straddle the origin (End disc)
+        qz0 = int(rng.integers(-9000, 9000)) if i % 5 else -nz // 2
+        seed_i = int(rng.integers(-2**63, 2**63 - 1))
+        reqs.append(((v, d), seed_i, qx0, qz0, nx, nz, 16))
+    return reqs
+
+
+def oracle_grid(v, d, seed, qx0, qz0, nx, nz, qy, rule):
+    w = O.World(ge.data_root(), v, d.split(":")[1])
+    if rule == 2 and not d.endswith("the_end"):
+        return w.chunk_grid(seed, qx0, qz0, nx, nz, qy)
+    return w.quart_grid(seed, qx0, qz0, nx, nz, qy, O.TIE_ENGINE)
+
+
+@pytest.mark.parametrize("rule", [0, 2])
+def test_batch_matches_oracle(env, rule):
+    mg, gens, worlds = env
+    reqs = mixed_requests(worlds)
+    plan = mg.Plan([(worlds[k], s, qx0, qz0, nx, nz, qy) for k, s, qx0, qz0, nx, nz, qy in reqs], tie_rule=rule)
+    out = plan.split(plan.run())
+    for (k, s, qx0, qz0, nx, nz, qy), got in zip(reqs, out):
+        exp = oracle_grid(k[0], k[1], s, qx0, qz0, nx, nz, qy, rule)
+        assert np.array_equal(got, exp), (k, s, qx0, qz0, nx, nz)
+
+
+def test_batch_equals_plain_and_replays(env):
+    torch = pytest.importorskip("torch")
+    mg, gens, worlds = env
+    reqs = mixed_requests(worlds, n=36, seed=4)
+    plan = mg.Plan([(worlds[k], s, qx0, qz0, nx, nz, qy) for k, s, qx0, qz0, nx, nz, qy in reqs])
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    d_out = torch.zeros(plan.output_bytes, dtype=torch.uint8, device=dev)
+    plan.run_dev(d_out.data_ptr(), stream)
+    first = d_out.cpu().numpy().copy()
+    for _ in range(2):  # graph replays overwrite the same bytes with the same values
+        d_out.fill_(0xEE)
+        plan.run_dev(d_out.data_ptr(), stream)
+        assert np.array_equal(d_out.cpu().numpy(), first)
+    d_out.fill_(0xEE)
+    plan.run_dev(d_out.data_ptr(), stream, graph=False)
+    assert np.array_equal(d_out.cpu().numpy(), first)
+    # the plain form: one setup + one grid launch per request
+    plain = torch.full_like(d_out, 0xEE)
+    for i, (k, s, qx0, qz0, nx, nz, qy) in enumerate(reqs):
+        worlds[k].quart_grid_seed_dev(s, qx0, qz0, nx, nz, qy, 0, plain.data_ptr() + plan.offset(i), stream)
+    assert np.array_equal(plain.cpu().numpy(), first)
+    # every tile shape the autotuner tries gives the same ids
+    ms = plan.autotune(d_out.data_ptr(), reps=1)
+    assert ms > 0 and 0 <= plan.shape < 4
+    plan.run_dev(d_out.data_ptr(), stream)
+    assert np.array_equal(d_out.cpu().numpy(), first)
+
+
+def test_batch_config4_sample(env):
+    """A 200-request prefix of the uneven mixed batch workload (SplitMix64(3)), checked against the oracle."""
+    import bench
+
+    mg, gens, worlds = env
+    reqs = bench.config4_requests(200)
+    plan = mg.Plan([(worlds[(v, d)], s, qx0, qz0, n, n, qy) for v, d, s, qx0, qz0, n, qy in reqs])
+    out = plan.split(plan.run())
+    for i in range(0, 200, 7):
+        v, d, s, qx0, qz0, n, qy = reqs[i]
+        exp = O.World(ge.data_root(), v, d.split(":")[1]).quart_grid(s, qx0, qz0, n, n, qy, O.TIE_ENGINE)
+        assert np.array_equal(out[i], exp), reqs[i]
