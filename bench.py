@@ -205,6 +205,8 @@ def run_gb300(args, rank, world, local_rank):
                   "dimension": "overworld", "l2": "working set > L2 (65536 x 46 lattices = 965 MB per step)"}
     elif args.workload == "batch10k":
         return run_batch(args, rank, world, local_rank, mg, ge)
+    elif args.workload == "serve":
+        return run_serve(args, rank, world, local_rank, mg, ge)
     else:
         w = gen.world("minecraft:overworld", "normal", 12345)
         nx = nz = 256
@@ -445,6 +447,117 @@ def cpu_baseline_batch(reqs, budget_s: float) -> dict:
             "sample": f"first {done} of {len(reqs)} requests ({cells} samples, {dt:.1f} s), rows over threads"}
 
 
+def zipf_table(n: int = 50000, s: float = 1.1) -> np.ndarray:
+    w = np.arange(1, n + 1, dtype=np.float64) ** -s
+    return np.cumsum(w) / w.sum()
+
+
+def config5_stream(rate: float, duration: float, state: int = 4, nseeds: int = 50000):
+    """Open-loop Poisson arrivals at `rate` per second for `duration` s (SplitMix64(state), seven draws per
+    request: exponential gap, Zipf(1.1) rank over nseeds seeds (drawn from SplitMix64(state + 100)), then
+    version, dimension, side, x, z as in the uneven batch).  Returns (arrival time, request) pairs."""
+    seeds = splitmix64(state + 100, nseeds).view(np.int64)
+    cdf = zipf_table(nseeds)
+    est = int(rate * duration * 1.2) + 64
+    r = splitmix64(state, 7 * est).reshape(est, 7)
+    t = 0.0
+    out = []
+    for i in range(est):
+        u = float(r[i, 0] >> np.uint64(11)) * 2.0 ** -53
+        t += -np.log1p(-u) / rate
+        if t >= duration:
+            break
+        rank = int(np.searchsorted(cdf, float(r[i, 1] >> np.uint64(11)) * 2.0 ** -53, side="right"))
+        seed = int(seeds[min(rank, nseeds - 1)])
+        version = C4_VERSIONS[int(r[i, 2] % np.uint64(3))]
+        dim = C4_DIMS[int(r[i, 3] % np.uint64(10))]
+        side = int(16.0 * 32.0 ** (float(r[i, 4] >> np.uint64(11)) * 2.0 ** -53))
+        x = -30000 + int(r[i, 5] % np.uint64(60001))
+        z = -30000 + int(r[i, 6] % np.uint64(60001))
+        out.append((t, (version, dim, seed, x >> 2, z >> 2, side, 16)))
+    return out
+
+
+def serve_run(mg, worlds, stream, budget: int, max_inflight: int = 2):
+    """Replay an arrival stream against a server: a submitter keeps the schedule, a collector waits."""
+    import threading
+
+    srv = mg.Server(hbm_budget_bytes=budget, max_inflight=max_inflight)
+    tickets = []
+    lat = []
+    samples = 0
+    done = threading.Event()
+
+    def collector():
+        i = 0
+        while True:
+            while i >= len(tickets):
+                if done.is_set() and i >= len(tickets):
+                    return
+                time.sleep(0.0002)
+            ids, ms = srv.wait(tickets[i])
+            lat.append(ms)
+            i += 1
+
+    col = threading.Thread(target=collector)
+    col.start()
+    t0 = time.perf_counter()
+    for at, (v, d, s, qx0, qz0, n, qy) in stream:
+        now = time.perf_counter() - t0
+        if at > now:
+            time.sleep(at - now)
+        tickets.append(srv.submit(worlds[(v, d)], s, qx0, qz0, n, n, qy))
+        samples += n * n
+    done.set()
+    col.join()
+    elapsed = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    lat_a = np.array(lat)
+    looks = st["cache_hits"] + st["cache_misses"]
+    return {"requests": len(stream), "elapsed_s": round(elapsed, 3), "achieved_rps": round(len(stream) / elapsed, 1),
+            "samples_per_s": samples / elapsed, "p50_ms": round(float(np.percentile(lat_a, 50)), 3),
+            "p99_ms": round(float(np.percentile(lat_a, 99)), 3), "max_ms": round(float(lat_a.max()), 3),
+            "cache_hit_rate": round(st["cache_hits"] / max(1, looks), 4), "cache_evictions": st["cache_evictions"],
+            "batches": st["batches"], "mean_batch": round(st["requests_admitted"] / max(1, st["batches"]), 2)}
+
+
+def run_serve(args, rank, world, local_rank, mg, ge):
+    """Serving: open-loop Poisson streams at several rates, continuous batching, 8 GB noise-state cache."""
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    gens = {v: mg.Generator.open(ge.data_root(), v) for v in C4_VERSIONS}
+    worlds = {(v, d): gens[v].world(d, "normal", 0) for v in C4_VERSIONS for d in set(C4_DIMS)}
+    warm = config5_stream(200.0, 1.0, state=99)
+    serve_run(mg, worlds, warm, 8 << 30)
+    rates = [float(x) for x in args.rates.split(",")]
+    runs = {}
+    with ClockSampler(local_rank) as clk:
+        for rate in rates:
+            runs[str(int(rate))] = serve_run(mg, worlds, config5_stream(rate, args.duration), 8 << 30)
+        small = serve_run(mg, worlds, config5_stream(rates[len(rates) // 2], args.duration / 2), 64 << 20)
+    top = runs[str(int(rates[-1]))]
+    out = {"metric": METRIC + " (served)", "value": top["samples_per_s"], "unit": UNIT, "n_gpus": world,
+           "steps": len(rates), "warmup": 1, "ms_per_step": top["elapsed_s"] * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64+int64",
+           "data": "synthetic (SplitMix64(4) Poisson stream, Zipf(1.1) over 50,000 seeds)",
+           "config": {"workload": f"served: open-loop Poisson arrivals at {args.rates} req/s for {args.duration} s each, "
+                                  "requests from the uneven-batch distribution, seeds Zipf(1.1) over 50,000; "
+                                  "continuous batching on 2 streams, 8 GB noise-state cache (LRU)",
+                      "rates": rates, "duration_s": args.duration,
+                      "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+           "served": runs, "small_budget_64MB": small,
+           "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
+           "e2e": {"value": top["samples_per_s"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": int(top["samples_per_s"] * top["elapsed_s"])}}
+    clocks = clk.summary()
+    if clocks:
+        out["clocks"] = clocks
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 def cpu_baseline(workload: str, budget_s: float) -> dict:
     """The reference algorithm on this host's cores (CPU oracle, OpenMP over seeds or rows)."""
     import __graft_entry__ as ge
@@ -517,7 +630,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["seeds8", "grid256", "batch10k"], default="seeds8")
+    ap.add_argument("--workload", choices=["seeds8", "grid256", "batch10k", "serve"], default="seeds8")
+    ap.add_argument("--rates", default="500,1000,2000", help="serve: arrival rates (requests/s)")
+    ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds per rate (60 = the configuration)")
     ap.add_argument("--requests", type=int, default=10000, help="batch10k: number of requests")
     ap.add_argument("--cpu-sample-s", type=float, default=12.0)
     ap.add_argument("--seeds", type=int, default=65536, help="seeds8: number of seeds (65536 = the configuration)")

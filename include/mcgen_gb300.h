@@ -83,6 +83,28 @@ MCGEN_API int mcgen_gb300_plan_run_dev(McGb300Plan *p, uint8_t *d_out, void *str
 MCGEN_API int mcgen_gb300_plan_run_dev_direct(McGb300Plan *p, uint8_t *d_out, void *stream);
 MCGEN_API int mcgen_gb300_plan_run(McGb300Plan *p, uint8_t *out);
 
+/* ---- served form: continuous batching with a device noise-state cache ----
+ * Submit requests from any thread at any time; a worker admits every pending request into the next batch
+ * as soon as one of `max_inflight` streams is free, so requests that arrive while others run are batched
+ * and overlap with them on the GPU.  Each (world, seed)'s lattices stay resident in an HBM cache of
+ * `hbm_budget_bytes` (LRU among entries no running batch uses).  `out` receives nx*nz ids (row-major) and
+ * must stay valid until mcgen_gb300_server_wait returns for the ticket.  Results equal the batched and
+ * plain forms bit for bit (ENGINE tie rule). */
+typedef struct McGb300Server McGb300Server;
+typedef struct McGb300ServerStats {
+    long long requests_submitted, requests_admitted, batches, samples_done;
+    long long cache_hits, cache_misses, cache_evictions, cache_entries, pending;
+    long long cache_slots[3]; /* Overworld, Nether, End */
+} McGb300ServerStats;
+MCGEN_API int mcgen_gb300_server_new(long long hbm_budget_bytes, int max_inflight, int max_batch_requests,
+                                     McGb300Server **out);
+MCGEN_API void mcgen_gb300_server_free(McGb300Server *s); /* drains pending work first */
+MCGEN_API int mcgen_gb300_server_submit(McGb300Server *s, const McGb300Request *req, uint8_t *out, long long *ticket);
+/* wait for a ticket (timeout_ms < 0: no limit; MCGEN_E_CANCEL on timeout, the ticket stays valid);
+ * latency_ms: submit to completion.  A ticket can be waited for once. */
+MCGEN_API int mcgen_gb300_server_wait(McGb300Server *s, long long ticket, int timeout_ms, double *latency_ms);
+MCGEN_API int mcgen_gb300_server_stats(McGb300Server *s, McGb300ServerStats *out);
+
 /* Allocation-free form of mcgen_gb300_seed_points_dev, for callers that cannot let a library allocate
  * device memory (their own memory arena, latency-critical loops, no allocation after set-up).  No
  * counterpart in the reference.  The per-seed noise lattices go to one fixed 16 MiB device array inside

@@ -106,7 +106,19 @@ _PROTOS.update({
     "mcgen_gb300_plan_run_dev": (C.c_int, [_P, _P, _P]),
     "mcgen_gb300_plan_run_dev_direct": (C.c_int, [_P, _P, _P]),
     "mcgen_gb300_plan_run": (C.c_int, [_P, _P]),
+    "mcgen_gb300_server_new": (C.c_int, [C.c_longlong, C.c_int, C.c_int, C.POINTER(_P)]),
+    "mcgen_gb300_server_free": (None, [_P]),
+    "mcgen_gb300_server_submit": (C.c_int, [_P, _P, _P, C.POINTER(C.c_longlong)]),
+    "mcgen_gb300_server_wait": (C.c_int, [_P, C.c_longlong, C.c_int, C.POINTER(C.c_double)]),
+    "mcgen_gb300_server_stats": (C.c_int, [_P, _P]),
+    "mcgen_gb300_seed_points_noalloc": (C.c_int, [_P, _P, C.c_int, _P, C.c_int, _P, _P, _P]),
 })
+
+
+class McGb300ServerStats(C.Structure):
+    _fields_ = [(n, C.c_longlong) for n in ("requests_submitted", "requests_admitted", "batches", "samples_done",
+                                            "cache_hits", "cache_misses", "cache_evictions", "cache_entries",
+                                            "pending")] + [("cache_slots", C.c_longlong * 3)]
 
 
 class McGb300Request(C.Structure):
@@ -417,3 +429,48 @@ class Plan:
     def split(self, flat: np.ndarray) -> list:
         """Per-request (nz, nx) views of a flat output."""
         return [flat[self.offset(i):self.offset(i) + nx * nz].reshape(nz, nx) for i, (nx, nz) in enumerate(self.shapes)]
+
+
+class Server:
+    """The served form (mcgen_gb300_server_*): continuous batching with a device noise-state cache."""
+
+    def __init__(self, hbm_budget_bytes: int = 8 << 30, max_inflight: int = 2, max_batch: int = 4096):
+        h = _P()
+        _check(load().mcgen_gb300_server_new(hbm_budget_bytes, max_inflight, max_batch, C.byref(h)),
+               "mcgen_gb300_server_new")
+        self._h = h
+        self._keep = {}
+
+    def close(self):
+        if self._h:
+            load().mcgen_gb300_server_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, world: "World", seed: int, qx0: int, qz0: int, nx: int, nz: int, qy: int = 16,
+               out: np.ndarray | None = None) -> int:
+        out = np.empty((nz, nx), np.uint8) if out is None else out
+        req = McGb300Request(world.handle, int(seed), qx0, qz0, nx, nz, qy)
+        t = C.c_longlong()
+        _check(load().mcgen_gb300_server_submit(self._h, C.byref(req), _ptr(out), C.byref(t)),
+               "mcgen_gb300_server_submit")
+        self._keep[t.value] = out
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        """(ids, latency in ms) of a ticket."""
+        lat = C.c_double()
+        _check(load().mcgen_gb300_server_wait(self._h, ticket, timeout_ms, C.byref(lat)), "mcgen_gb300_server_wait")
+        return self._keep.pop(ticket), lat.value
+
+    def stats(self) -> dict:
+        st = McGb300ServerStats()
+        _check(load().mcgen_gb300_server_stats(self._h, C.byref(st)), "mcgen_gb300_server_stats")
+        d = {n: getattr(st, n) for n, _ in st._fields_ if n != "cache_slots"}
+        d["cache_slots"] = list(st.cache_slots)
+        return d

@@ -1,0 +1,471 @@
+/* server.cpp -- the served form: continuous batching of biome-map requests (mcgen_gb300_server_*).
+ *
+ * Callers submit requests (world, seed, quart region) from any thread at any time and get a ticket.  A
+ * worker thread admits every pending request into the next batch as soon as one of the server's streams
+ * is free (up to `max_inflight` batches run at once, so a batch that forms while another is on the GPU
+ * starts right away and the two overlap on the device), makes sure each request's seed lattices are
+ * resident in the device noise-state cache, enqueues the setup launches for the cache misses and one
+ * persistent k_batch launch, and copies the ids back.  When a batch's event completes the worker hands
+ * every request its ids and wakes its waiters.
+ *
+ * Noise-state cache: per dimension a pool of fixed-size slots (46 lattices of 320 B for the Overworld, 8 for
+ * the Nether, 1 for the End) carved from one HBM budget, keyed by (world, seed), evicted least recently
+ * used among slots that no in-flight batch references.
+ */
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <list>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/mcgen_gb300.h"
+#include "abi_internal.h"
+#include "batch.h"
+#include "launch.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Pool { /* one dimension's slots */
+    int lattices_per_slot = 0;
+    int nslots = 0;
+    MgLattice *base = nullptr;
+    std::vector<int> free_slots;
+    std::list<std::pair<const McWorld *, int64_t>> lru; /* front = most recent */
+    /* builder: the batch slot whose setup launch is still filling this entry, -1 once it is complete */
+    struct Entry { int slot; int refs; int builder; std::list<std::pair<const McWorld *, int64_t>>::iterator it; };
+    std::map<std::pair<const McWorld *, int64_t>, Entry> map;
+};
+
+struct Ticket {
+    McGb300Request req;
+    uint8_t *out;
+    Clock::time_point t_submit, t_done;
+    int state = 0; /* 0 pending, 1 running, 2 done, 3 failed */
+    int err = 0;
+};
+
+struct Batch {
+    cudaStream_t st = nullptr;
+    cudaEvent_t done = nullptr;
+    cudaEvent_t setup_done = nullptr; /* after this batch's setup launches */
+    bool busy = false;
+    std::vector<long long> tickets;
+    std::vector<std::pair<int, std::pair<const McWorld *, int64_t>>> held; /* (dim, key) references */
+    /* device and pinned staging, grown as needed */
+    MgBatchReq *d_reqs = nullptr; size_t cap_reqs = 0;
+    MgSetupEntry *d_ent = nullptr; size_t cap_ent = 0;
+    int *d_first = nullptr; size_t cap_first = 0;
+    MgWorldDesc *d_worlds = nullptr; size_t cap_worlds = 0;
+    const MgTreeNode **d_trees = nullptr;
+    uint8_t *d_out = nullptr; size_t cap_out = 0;
+    uint8_t *h_out = nullptr; size_t cap_hout = 0;
+    unsigned long long *d_counter = nullptr;
+    std::vector<long long> out_off;
+};
+
+}  // namespace
+
+struct McGb300Server {
+    std::mutex m;
+    std::condition_variable cv_work, cv_done;
+    std::thread worker;
+    bool stop = false;
+    int max_batch = 4096;
+    int ctas = 0;
+    Pool pool[3];
+    std::vector<Batch> batches;
+    std::deque<long long> pending;
+    std::unordered_map<long long, Ticket> tickets;
+    long long next_ticket = 1;
+    McGb300ServerStats stats;
+    int fatal = 0;
+};
+
+namespace {
+
+int crc(cudaError_t e) { return e == cudaSuccess ? 0 : e == cudaErrorMemoryAllocation ? MCGEN_E_NOMEM : MCGEN_E_INTERNAL; }
+
+template <typename T>
+cudaError_t grow_dev(T **p, size_t *cap, size_t n) {
+    if (n <= *cap) return cudaSuccess;
+    size_t c = n + n / 2 + 16;
+    cudaFree((void *)*p);
+    *p = nullptr;
+    cudaError_t e = cudaMalloc((void **)p, sizeof(T) * c);
+    *cap = e ? 0 : c;
+    return e;
+}
+
+/* Reserve a cache slot for key in pool P (caller holds the server lock); -1 if every slot is in use.
+ * *builder: the batch still building a hit entry (-1 when complete); a miss is built by batch `me`. */
+int cache_acquire(McGb300Server *s, Pool &P, const std::pair<const McWorld *, int64_t> &key, int me, bool *miss,
+                  int *builder) {
+    auto it = P.map.find(key);
+    if (it != P.map.end()) {
+        it->second.refs++;
+        P.lru.erase(it->second.it);
+        P.lru.push_front(key);
+        it->second.it = P.lru.begin();
+        *miss = false;
+        *builder = it->second.builder;
+        s->stats.cache_hits++;
+        return it->second.slot;
+    }
+    int slot = -1;
+    if (!P.free_slots.empty()) {
+        slot = P.free_slots.back();
+        P.free_slots.pop_back();
+    } else {
+        for (auto r = P.lru.rbegin(); r != P.lru.rend(); ++r) { /* least recently used, unreferenced */
+            auto e = P.map.find(*r);
+            if (e->second.refs == 0) {
+                slot = e->second.slot;
+                P.lru.erase(std::next(r).base());
+                P.map.erase(e);
+                s->stats.cache_evictions++;
+                break;
+            }
+        }
+        if (slot < 0) return -1;
+    }
+    P.lru.push_front(key);
+    P.map[key] = Pool::Entry{slot, 1, me, P.lru.begin()};
+    *miss = true;
+    *builder = -1;
+    s->stats.cache_misses++;
+    return slot;
+}
+void cache_release(Pool &P, const std::pair<const McWorld *, int64_t> &key, int me) {
+    auto it = P.map.find(key);
+    if (it == P.map.end()) return;
+    if (it->second.refs > 0) it->second.refs--;
+    if (it->second.builder == me) it->second.builder = -1; /* its batch has completed */
+}
+
+/* Form and launch one batch from pending requests on batch slot b (server lock held). */
+int launch_batch(McGb300Server *s, Batch &b) {
+    const int me = (int)(&b - s->batches.data());
+    std::vector<int> wait_on;
+    std::vector<const McWorld *> worlds;
+    std::map<const McWorld *, int> widx;
+    std::vector<MgBatchReq> reqs;
+    std::vector<MgSetupEntry> ent[3];
+    std::vector<int> first;
+    long long tiles = 0, out = 0, ow = 0;
+    b.tickets.clear();
+    b.held.clear();
+    b.out_off.clear();
+    while (!s->pending.empty() && (int)b.tickets.size() < s->max_batch) {
+        const long long id = s->pending.front();
+        Ticket &T = s->tickets[id];
+        const McWorld *w = T.req.world;
+        const int dim = w->desc.dim;
+        auto key = std::make_pair(w, (int64_t)T.req.seed);
+        Pool &P = s->pool[dim];
+        if (w->desc.ntables > P.lattices_per_slot) { /* cannot happen with the shipped tables */
+            s->pending.pop_front();
+            T.state = 3;
+            T.err = MCGEN_E_DATA;
+            T.t_done = Clock::now();
+            continue;
+        }
+        bool miss = false;
+        int builder = -1;
+        /* the same key twice in one batch is one reference per request */
+        const int slot = cache_acquire(s, P, key, me, &miss, &builder);
+        if (slot < 0) break; /* cache full of in-flight states: wait for a batch to finish */
+        if (builder >= 0 && builder != me) wait_on.push_back(builder);
+        s->pending.pop_front();
+        b.held.push_back(std::make_pair(dim, key));
+        if (!widx.count(w)) { widx[w] = (int)worlds.size(); worlds.push_back(w); }
+        const int lat = (int)((P.base - s->pool[0].base) + (long long)slot * P.lattices_per_slot);
+        if (miss) {
+            MgSetupEntry e;
+            e.seed = T.req.seed;
+            e.world = widx[w];
+            e.slot = lat;
+            if (dim == MG_OVERWORLD) { first.push_back((int)ow); ow += w->desc.ntables; }
+            ent[dim].push_back(e);
+        }
+        MgBatchReq r;
+        r.world = widx[w];
+        r.state = lat;
+        r.qx0 = T.req.qx0; r.qz0 = T.req.qz0; r.nx = T.req.nx; r.nz = T.req.nz; r.qy = T.req.qy;
+        r.tie = MG_TIE_ENGINE;
+        r.tile0 = tiles;
+        r.out_off = out;
+        tiles += mg::batch_tiles(dim, r.qx0, r.qz0, r.nx, r.nz, 0);
+        b.out_off.push_back(out);
+        out += (long long)r.nx * r.nz;
+        reqs.push_back(r);
+        b.tickets.push_back(id);
+        T.state = 1;
+    }
+    if (b.tickets.empty()) return 0;
+    cudaError_t e = cudaSuccess;
+    std::vector<MgWorldDesc> wd;
+    std::vector<const MgTreeNode *> tp;
+    for (auto *w : worlds) { wd.push_back(w->desc); tp.push_back(w->d_tree); }
+    size_t ntrees_cap = b.cap_worlds;
+    if (!e) e = grow_dev(&b.d_worlds, &b.cap_worlds, wd.size());
+    if (!e && b.cap_worlds != ntrees_cap) {
+        cudaFree((void *)b.d_trees);
+        b.d_trees = nullptr;
+        e = cudaMalloc((void **)&b.d_trees, sizeof(void *) * b.cap_worlds);
+    }
+    size_t ent_n = ent[0].size() + ent[1].size() + ent[2].size();
+    if (!e) e = grow_dev(&b.d_reqs, &b.cap_reqs, reqs.size());
+    if (!e) e = grow_dev(&b.d_ent, &b.cap_ent, ent_n ? ent_n : 1);
+    if (!e) e = grow_dev(&b.d_first, &b.cap_first, first.size() ? first.size() : 1);
+    if (!e) e = grow_dev(&b.d_out, &b.cap_out, (size_t)out);
+    if (!e && (size_t)out > b.cap_hout) {
+        cudaFreeHost(b.h_out);
+        b.h_out = nullptr;
+        size_t c = (size_t)out + (size_t)out / 2;
+        e = cudaMallocHost((void **)&b.h_out, c);
+        b.cap_hout = e ? 0 : c;
+    }
+    if (!e && !b.d_counter) e = cudaMalloc(&b.d_counter, sizeof(unsigned long long));
+    if (e) return crc(e);
+    /* small host->device copies of this batch's descriptors (pageable sources: staged by the driver) */
+    cudaStream_t st = b.st;
+    e = cudaMemcpyAsync(b.d_worlds, wd.data(), sizeof(MgWorldDesc) * wd.size(), cudaMemcpyHostToDevice, st);
+    if (!e) e = cudaMemcpyAsync((void *)b.d_trees, tp.data(), sizeof(void *) * tp.size(), cudaMemcpyHostToDevice, st);
+    if (!e) e = cudaMemcpyAsync(b.d_reqs, reqs.data(), sizeof(MgBatchReq) * reqs.size(), cudaMemcpyHostToDevice, st);
+    size_t eo = 0;
+    for (int d = 0; d < 3 && !e; d++) {
+        if (ent[d].empty()) continue;
+        e = cudaMemcpyAsync(b.d_ent + eo, ent[d].data(), sizeof(MgSetupEntry) * ent[d].size(), cudaMemcpyHostToDevice, st);
+        eo += ent[d].size();
+    }
+    if (!e && !first.empty()) e = cudaMemcpyAsync(b.d_first, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice, st);
+    if (e) return crc(e);
+    eo = 0;
+    for (int d = 0; d < 3; d++) {
+        if (ent[d].empty()) continue;
+        int rc = mg::launch_setup_list(b.d_worlds, d, b.d_ent + eo, (int)ent[d].size(), b.d_first, ow, s->pool[0].base, st);
+        if (rc) return MCGEN_E_INTERNAL;
+        eo += ent[d].size();
+    }
+    if ((e = cudaEventRecord(b.setup_done, st))) return crc(e);
+    /* hits on states another in-flight batch is still building: order after that batch's setup */
+    for (int k : wait_on)
+        if ((e = cudaStreamWaitEvent(st, s->batches[(size_t)k].setup_done, 0))) return crc(e);
+    int rc = mg::launch_batch(b.d_worlds, b.d_trees, b.d_reqs, (int)reqs.size(), tiles, s->pool[0].base, b.d_counter,
+                              b.d_out, s->ctas, 0, st);
+    if (rc) return MCGEN_E_INTERNAL;
+    if ((e = cudaMemcpyAsync(b.h_out, b.d_out, (size_t)out, cudaMemcpyDeviceToHost, st))) return crc(e);
+    if ((e = cudaEventRecord(b.done, st))) return crc(e);
+    b.busy = true;
+    s->stats.batches++;
+    s->stats.requests_admitted += (long long)b.tickets.size();
+    return 0;
+}
+
+/* Hand a finished batch's ids to its requests (server lock held). */
+void finish_batch(McGb300Server *s, Batch &b, int err) {
+    const auto now = Clock::now();
+    for (size_t i = 0; i < b.tickets.size(); i++) {
+        auto it = s->tickets.find(b.tickets[i]);
+        if (it == s->tickets.end()) continue;
+        Ticket &T = it->second;
+        if (!err && T.out) memcpy(T.out, b.h_out + b.out_off[i], (size_t)T.req.nx * (size_t)T.req.nz);
+        T.state = err ? 3 : 2;
+        T.err = err;
+        T.t_done = now;
+        s->stats.samples_done += (long long)T.req.nx * T.req.nz;
+    }
+    const int me = (int)(&b - s->batches.data());
+    for (auto &h : b.held) cache_release(s->pool[h.first], h.second, me);
+    b.tickets.clear();
+    b.held.clear();
+    b.busy = false;
+    s->cv_done.notify_all();
+}
+
+void worker_loop(McGb300Server *s) {
+    std::unique_lock<std::mutex> lk(s->m);
+    for (;;) {
+        bool progressed = false;
+        /* completions */
+        for (auto &b : s->batches) {
+            if (!b.busy) continue;
+            cudaError_t q = cudaEventQuery(b.done);
+            if (q == cudaErrorNotReady) continue;
+            finish_batch(s, b, q == cudaSuccess ? 0 : MCGEN_E_INTERNAL);
+            progressed = true;
+        }
+        /* admissions: every free stream takes the pending requests */
+        for (auto &b : s->batches) {
+            if (b.busy || s->pending.empty()) continue;
+            std::lock_guard<std::mutex> glk(mg::abi_lock());
+            int rc = launch_batch(s, b);
+            if (rc) { /* fail the requests of this batch loudly */
+                finish_batch(s, b, rc);
+                s->fatal = rc;
+                progressed = true;
+            } else if (b.busy) {
+                progressed = true;
+            }
+            /* not busy and no error: the cache is full of states that running batches use; wait for one */
+        }
+        if (s->stop && s->pending.empty()) {
+            bool any = false;
+            for (auto &b : s->batches) any |= b.busy;
+            if (!any) return;
+        }
+        bool busy = false;
+        for (auto &b : s->batches) busy |= b.busy;
+        if (!progressed) {
+            if (busy) { /* poll the running batches; new requests also wake us */
+                s->cv_work.wait_for(lk, std::chrono::microseconds(50));
+            } else {
+                s->cv_work.wait(lk, [s] { return s->stop || !s->pending.empty(); });
+            }
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+MCGEN_API int mcgen_gb300_server_new(long long hbm_budget_bytes, int max_inflight, int max_batch_requests,
+                                     McGb300Server **out) {
+    if (!out || hbm_budget_bytes < (long long)(64 * sizeof(MgLattice)) || max_inflight < 1 || max_inflight > 8)
+        return MCGEN_E_ARG;
+    *out = nullptr;
+    std::lock_guard<std::mutex> glk(mg::abi_lock());
+    if (!mg::abi_device_ready()) return MCGEN_E_UNSUPPORTED;
+    McGb300Server *s = new McGb300Server();
+    memset(&s->stats, 0, sizeof s->stats);
+    s->max_batch = max_batch_requests > 0 ? max_batch_requests : 4096;
+    /* budget split: Overworld 3/4, Nether 3/16, End 1/16 of the lattices */
+    const long long lat_total = hbm_budget_bytes / (long long)sizeof(MgLattice);
+    const int lps[3] = {48, 8, 1}; /* lattices per seed: Overworld 46, Nether 8, End 1 */
+    const long long share[3] = {lat_total * 12 / 16, lat_total * 3 / 16, lat_total / 16};
+    long long total = 0;
+    for (int d = 0; d < 3; d++) {
+        s->pool[d].lattices_per_slot = lps[d];
+        s->pool[d].nslots = (int)std::max(1LL, std::min(share[d] / lps[d], (long long)INT32_MAX / 64));
+        total += (long long)s->pool[d].nslots * lps[d];
+    }
+    if (total > INT32_MAX) { delete s; return MCGEN_E_ARG; }
+    MgLattice *base = nullptr;
+    cudaError_t e = cudaMalloc(&base, sizeof(MgLattice) * (size_t)total);
+    if (e) { delete s; return crc(e); }
+    long long at = 0;
+    for (int d = 0; d < 3; d++) {
+        s->pool[d].base = base + at;
+        at += (long long)s->pool[d].nslots * lps[d];
+        for (int i = s->pool[d].nslots - 1; i >= 0; i--) s->pool[d].free_slots.push_back(i);
+    }
+    s->stats.cache_slots[0] = s->pool[0].nslots;
+    s->stats.cache_slots[1] = s->pool[1].nslots;
+    s->stats.cache_slots[2] = s->pool[2].nslots;
+    int cps = 1, dev = 0, sms = 1;
+    mg::batch_prepare(&cps);
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    s->ctas = sms * cps;
+    s->batches.resize((size_t)max_inflight);
+    for (auto &b : s->batches) {
+        if ((e = cudaStreamCreateWithFlags(&b.st, cudaStreamNonBlocking)) ||
+            (e = cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming)) ||
+            (e = cudaEventCreateWithFlags(&b.setup_done, cudaEventDisableTiming))) {
+            cudaFree(base);
+            delete s;
+            return crc(e);
+        }
+    }
+    s->worker = std::thread(worker_loop, s);
+    *out = s;
+    return MCGEN_OK;
+}
+
+MCGEN_API void mcgen_gb300_server_free(McGb300Server *s) {
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->m);
+        s->stop = true;
+    }
+    s->cv_work.notify_all();
+    s->worker.join();
+    std::lock_guard<std::mutex> glk(mg::abi_lock());
+    for (auto &b : s->batches) {
+        cudaStreamSynchronize(b.st);
+        cudaStreamDestroy(b.st);
+        cudaEventDestroy(b.done);
+        cudaEventDestroy(b.setup_done);
+        cudaFree(b.d_reqs);
+        cudaFree(b.d_ent);
+        cudaFree(b.d_first);
+        cudaFree(b.d_worlds);
+        cudaFree((void *)b.d_trees);
+        cudaFree(b.d_out);
+        cudaFreeHost(b.h_out);
+        cudaFree(b.d_counter);
+    }
+    cudaFree(s->pool[0].base);
+    delete s;
+}
+
+MCGEN_API int mcgen_gb300_server_submit(McGb300Server *s, const McGb300Request *req, uint8_t *out, long long *ticket) {
+    if (!s || !req || !req->world || !ticket || req->nx <= 0 || req->nz <= 0 || (long long)req->nx * req->nz > (1LL << 28))
+        return MCGEN_E_ARG;
+    {
+        /* the world's tree must be on the device before the worker references it */
+        std::lock_guard<std::mutex> glk(mg::abi_lock());
+        int rc = mg::abi_world_device(const_cast<McWorld *>(req->world));
+        if (rc) return rc;
+    }
+    std::lock_guard<std::mutex> lk(s->m);
+    if (s->fatal) return s->fatal;
+    const long long id = s->next_ticket++;
+    Ticket &T = s->tickets[id];
+    T.req = *req;
+    T.out = out;
+    T.t_submit = Clock::now();
+    s->pending.push_back(id);
+    *ticket = id;
+    s->stats.requests_submitted++;
+    s->cv_work.notify_one();
+    return MCGEN_OK;
+}
+
+MCGEN_API int mcgen_gb300_server_wait(McGb300Server *s, long long ticket, int timeout_ms, double *latency_ms) {
+    if (!s) return MCGEN_E_ARG;
+    std::unique_lock<std::mutex> lk(s->m);
+    auto it = s->tickets.find(ticket);
+    if (it == s->tickets.end()) return MCGEN_E_ARG;
+    auto done = [&] { return it->second.state >= 2; };
+    if (timeout_ms < 0) s->cv_done.wait(lk, done);
+    else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), done)) return MCGEN_E_CANCEL;
+    const Ticket &T = it->second;
+    if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(T.t_done - T.t_submit).count();
+    const int err = T.state == 3 ? (T.err ? T.err : MCGEN_E_INTERNAL) : MCGEN_OK;
+    s->tickets.erase(it);
+    return err;
+}
+
+MCGEN_API int mcgen_gb300_server_stats(McGb300Server *s, McGb300ServerStats *out) {
+    if (!s || !out) return MCGEN_E_ARG;
+    std::lock_guard<std::mutex> lk(s->m);
+    *out = s->stats;
+    out->pending = (long long)s->pending.size();
+    long long used = 0;
+    for (int d = 0; d < 3; d++) used += (long long)s->pool[d].map.size();
+    out->cache_entries = used;
+    return MCGEN_OK;
+}
+
+}  // extern "C"

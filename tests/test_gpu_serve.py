@@ -1,0 +1,92 @@
+"""The served form: continuous batching with a device noise-state cache.
+
+Each request's ids must be the same whether it is served alone or mixed with concurrent requests from
+several threads (different versions, dimensions, sizes, repeated seeds), and equal to the oracle; a small
+HBM budget must evict (LRU) without changing any result."""
+import threading
+
+import numpy as np
+import pytest
+
+import __graft_entry__ as ge
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+VERSIONS = ["26.1", "26.2", "26.3"]
+DIMS = ["minecraft:overworld", "minecraft:the_nether", "minecraft:the_end"]
+
+
+@pytest.fixture(scope="module")
+def env():
+    mg = ge.package()
+    mg.load()
+    if mg.device_count() < 1:
+        pytest.fail("no CUDA device")
+    gens = {v: mg.Generator.open(ge.data_root(), v) for v in VERSIONS}
+    worlds = {(v, d): gens[v].world(d, "normal", 0) for v in VERSIONS for d in DIMS}
+    return mg, gens, worlds
+
+
+def requests(worlds, n, seed):
+    rng = np.random.default_rng(seed)
+    keys = sorted(worlds)
+    seeds = [int(x) for x in rng.integers(-2**63, 2**63 - 1, 7)]  # few seeds: cache hits and in-flight sharing
+    out = []
+    for i in range(n):
+        k = keys[int(rng.integers(len(keys)))]
+        side = int(rng.integers(1, 90))
+        out.append((k, seeds[int(rng.integers(len(seeds)))], int(rng.integers(-5000, 5000)),
+                    int(rng.integers(-5000, 5000)), side, max(1, side // 2 + int(rng.integers(0, 9))), 16))
+    return out
+
+
+def test_alone_equals_mixed(env):
+    mg, gens, worlds = env
+    reqs = requests(worlds, 120, 1)
+    srv = mg.Server(hbm_budget_bytes=256 << 20, max_inflight=3)
+    alone = []
+    for k, s, qx0, qz0, nx, nz, qy in reqs:  # one at a time
+        ids, _ = srv.wait(srv.submit(worlds[k], s, qx0, qz0, nx, nz, qy))
+        alone.append(ids.copy())
+    mixed = [None] * len(reqs)
+
+    def client(part):
+        tickets = [(i, srv.submit(worlds[reqs[i][0]], *reqs[i][1:])) for i in part]
+        for i, t in tickets:
+            mixed[i] = srv.wait(t)[0]
+
+    threads = [threading.Thread(target=client, args=(list(range(j, len(reqs), 4)),)) for j in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    st = srv.stats()
+    srv.close()
+    for i, (a, b) in enumerate(zip(alone, mixed)):
+        assert np.array_equal(a, b), reqs[i]
+    for i in range(0, len(reqs), 9):
+        (v, d), s, qx0, qz0, nx, nz, qy = reqs[i]
+        exp = O.World(ge.data_root(), v, d.split(":")[1]).quart_grid(s, qx0, qz0, nx, nz, qy, O.TIE_ENGINE)
+        assert np.array_equal(alone[i], exp), reqs[i]
+    assert st["batches"] < 2 * len(reqs)  # the mixed phase was batched
+    assert st["cache_hits"] > 0
+
+
+def test_small_budget_evicts(env):
+    """A budget of a few Overworld slots forces LRU eviction; every result is still exact."""
+    mg, gens, worlds = env
+    srv = mg.Server(hbm_budget_bytes=4 * 48 * 320 * 16 // 12 + 64 * 320, max_inflight=2, max_batch=3)
+    rng = np.random.default_rng(7)
+    w = worlds[("26.3", "minecraft:overworld")]
+    ow = O.World(ge.data_root(), "26.3", "overworld")
+    tickets = []
+    for i in range(24):
+        s = int(rng.integers(-2**62, 2**62))
+        tickets.append((s, srv.submit(w, s, -40, 30, 24, 16, 16)))
+    for s, t in tickets:
+        ids, lat = srv.wait(t)
+        assert np.array_equal(ids, ow.quart_grid(s, -40, 30, 24, 16, 16, O.TIE_ENGINE))
+        assert lat >= 0
+    st = srv.stats()
+    srv.close()
+    assert st["cache_evictions"] > 0
