@@ -7,6 +7,13 @@ Workloads (synthetic inputs with the shapes of the published configurations):
            per-seed noise setup + climate + R-tree, ENGINE tie rule.  [65536, 8] biome ids.
   grid256  Overworld 26.3, seed 12345, mcgen_biome_grid 256 x 256 cells, x,z in [-512, 512) step 4,
            y = 64 (BiomeManager zoom + chunk-cell ties).  65,536 samples per step.
+  dims4096 Nether 26.3 and End 26.3: 4,096 SplitMix64(2) seeds x a 64 x 64 quart grid at y = 64 each, one
+           batched launch per dimension.
+  batch10k the uneven mixed batch: 10,000 SplitMix64(3) requests (versions 26.1/26.2/26.3, Overworld:Nether:
+           End 6:2:2, side log-uniform in [16, 512) quart cells), one persistent launch, against the plain
+           form (one setup + one grid launch per request).
+  serve    open-loop Poisson streams at 500/1000/2000 requests/s (SplitMix64(4), Zipf(1.1) over 50,000
+           seeds) against the continuous-batching server; p50/p99 latency, cache hit rate.
 
 A step is one pass of the workload.  `value` times steps with inputs resident in HBM through the
 device-pointer entry points; `e2e` times the same work through the host-buffer C ABI calls
@@ -150,11 +157,27 @@ class ClockSampler:
 def gpu_peaks(mg) -> dict:
     """Measured pipe rates (Gop/s) on this device; the host file gives only HBM and bf16 GEMM."""
     return {k: round(mg.pipe_rate(k), 1) for k in ("fp32_fma", "fp64_fma", "fp64_add", "int32_mad",
-                                                   "cvt_f64_floor_s32", "cvt_s32_f64", "cvt_f64_f32", "int64_mad")}
+                                                   "cvt_f64_floor_s32", "cvt_s32_f64", "cvt_f64_f32", "int64_mad",
+                                                   "cvt_s64_f64", "cvt_f32_f64")}
 
 
-# Algorithmic work per launch of each kernel (what the reference algorithm must do, counted from its
-# source; see DESIGN.md "Roofline"): (work units per launch, unit name, pipe peak key).
+# Lattice (octave) samples per biome sample: 52 in the Overworld (six NormalNoises, two stacks each, with
+# the shift noise sampled twice), 8 in the Nether; the oracle's work counter pins both numbers.
+OCTAVES_PER_SAMPLE = {"minecraft:overworld": 52, "minecraft:the_nether": 8, "minecraft:the_end": 0}
+# FP64 operations of one octave sample as the kernels compute it: the double branch (26.1/26.2) does the
+# two rounded coordinate adds, fx - 1, eight gradient sums, two smoothsteps (7 each), the other fraction
+# minus one, seven lerps (3 each) and the amplitude product and sum (3): 50.  The float branch (26.3) does
+# only the two coordinate adds in FP64.  Smaller per-sample terms (shift coordinates, End simplex) are left
+# out, so the model is a lower bound.
+FP64_PER_OCTAVE = {"26.1": 50, "26.2": 50, "26.3": 2, "26.4-snapshot-2": 2}
+
+
+def batch_fp64_ops(reqs) -> float:
+    return float(sum(n * n * OCTAVES_PER_SAMPLE[d] * FP64_PER_OCTAVE[v] for v, d, s, qx0, qz0, n, qy in reqs))
+
+
+# Algorithmic work per launch of each kernel, counted from the reference algorithm:
+# (work units per launch, unit name, pipe peak key).
 def kernel_work(kernel: str, seeds8: bool, ns: int, np_: int, ntables: int) -> tuple[float, str, str] | None:
     if kernel == "k_setup_xo":
         # 256 Fisher-Yates steps per lattice, each one Xoroshiro128++ draw (9 64-bit ALU ops = 18 32-bit ops),
@@ -207,6 +230,8 @@ def run_gb300(args, rank, world, local_rank):
         return run_batch(args, rank, world, local_rank, mg, ge)
     elif args.workload == "serve":
         return run_serve(args, rank, world, local_rank, mg, ge)
+    elif args.workload == "dims4096":
+        return run_dims(args, rank, world, local_rank, mg, ge)
     else:
         w = gen.world("minecraft:overworld", "normal", 12345)
         nx = nz = 256
@@ -389,36 +414,46 @@ def run_batch(args, rank, world, local_rank, mg, ge):
     plain_wall = time.perf_counter() - t0
     plain_ms = max(pe0.elapsed_time(pe1), plain_wall * 1e3)
     same = bool(torch.equal(plain, d_out))
-    # end to end: host-buffer C ABI call (copies the ids to pinned host memory)
+    # end to end through the public API, every step: the request list goes in from the host (plan_new copies
+    # worlds, requests and setup lists to the device), the plan runs, the ids come back into pinned memory
     h_out = torch.empty(samples, dtype=torch.uint8).pin_memory()
     hv = h_out.numpy()
-    plan.run(hv)
+    shape = plan.shape
+    plan_args = [(worlds[(v, d)], s, qx0, qz0, n, n, qy) for v, d, s, qx0, qz0, n, qy in reqs]
+
+    def e2e_step():
+        p = mg.Plan(plan_args)
+        p.shape = shape
+        p.run(hv)
+        b = p.h2d_bytes
+        p.close()
+        return b
+
+    e2e_step()
+    e2e_steps = min(args.steps, 5)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        plan.run(hv)
+    h2d = 0
+    for _ in range(e2e_steps):
+        h2d = e2e_step()
     e2e_s = time.perf_counter() - t0
-    e2e = samples * args.steps * world / e2e_s
-    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f32+f64+int64", "data": "synthetic (SplitMix64(3) requests)",
-           "config": {"workload": f"uneven mixed batch: {len(reqs)} SplitMix64(3) requests, versions 26.1/26.2/26.3, "
-                                  "Overworld:Nether:End 6:2:2, square side log-uniform in [16,512) quart cells, origin "
-                                  "uniform in [-30000,30000] blocks, y=64, ENGINE tie rule; one persistent launch "
-                                  "(CUDA graph) vs one plain launch pair per request",
-                      "requests": len(reqs), "samples_per_step": samples, "tile_shape": plan.shape,
-                      "autotune_ms": round(tuned_ms, 3), "l2": f"output {samples/1e6:.0f} MB per step > L2",
-                      "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
-           "plain": {"value": samples * world / (plain_ms * 1e-3), "ms_per_step": plain_ms,
-                     "launches_per_step": 2 * len(reqs), "identical_output": same},
-           "batched_over_plain": (samples / (ms_max / args.steps)) / (samples / plain_ms),
-           "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(samples)},
-           "gpu_launches": int(graph_launches) + args.steps * (1 + sum(1 for _ in set(d for _, d, *_ in reqs)))}
+    e2e = samples * e2e_steps * world / e2e_s
+    per_step_launches = sum(v[1] for v in prof.values())
     if rank == 0:
         out["kernels"] = {k: {"ms_total": round(v[0], 4), "launches": v[1], "avg_ms": round(v[0] / v[1], 5)}
                           for k, v in prof.items()}
         clocks = clk.summary()
         if clocks:
             out["clocks"] = clocks
+        peaks = gpu_peaks(mg) if not args.skip_extras else {}
+        out["pipe_peaks_gops"] = peaks
+        if "k_batch" in prof and peaks:
+            ops = batch_fp64_ops(reqs)
+            avg_s = prof["k_batch"][0] / prof["k_batch"][1] * 1e-3
+            achieved = ops / avg_s / 1e9
+            out["roofline"] = {"kernel": "k_batch", "bound": "fp64", "achieved": round(achieved, 1),
+                               "peak": peaks["fp64_add"], "unit": "Gop/s", "frac": round(achieved / peaks["fp64_add"], 4),
+                               "traffic": None, "work": f"{ops:.4g} FP64 ops per launch (lattice model)",
+                               "peak_source": "measured in-run (FP64 add pipe microbenchmark)"}
         if not args.skip_extras:
             out["cpu_baseline"] = cpu_baseline_batch(reqs, args.cpu_sample_s)
         print(json.dumps(out), flush=True)
@@ -522,6 +557,57 @@ def serve_run(mg, worlds, stream, budget: int, max_inflight: int = 2):
             "batches": st["batches"], "mean_batch": round(st["requests_admitted"] / max(1, st["batches"]), 2)}
 
 
+def run_dims(args, rank, world, local_rank, mg, ge):
+    """Other dimensions: 4,096 SplitMix64(2) seeds, a 64 x 64 quart grid at y=64 per seed, Nether 26.3 and
+    End 26.3, each dimension one batched launch (plan + graph) of 4,096 requests."""
+    import torch
+
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    seeds = splitmix64(2, 4096).view(np.int64)
+    gen = mg.Generator.open(ge.data_root(), "26.3")
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    res = {}
+    total_samples, total_ms, kern = 0, 0.0, {}
+    with ClockSampler(local_rank) as clk:
+        for dim in ("minecraft:the_nether", "minecraft:the_end"):
+            w = gen.world(dim, "normal", 0)
+            plan = mg.Plan([(w, int(s), -32, -32, 64, 64, 16) for s in seeds])
+            d_out = torch.empty(plan.output_bytes, dtype=torch.uint8, device=dev)
+            plan.autotune(d_out.data_ptr(), reps=1)
+            for _ in range(args.warmup):
+                plan.run_dev(d_out.data_ptr(), sh)
+            torch.cuda.synchronize(dev)
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            for _ in range(args.steps):
+                plan.run_dev(d_out.data_ptr(), sh)
+            ev1.record(stream)
+            torch.cuda.synchronize(dev)
+            ms = ev0.elapsed_time(ev1) / args.steps
+            mg.profile(True)
+            plan.run_dev(d_out.data_ptr(), sh, graph=False)
+            torch.cuda.synchronize(dev)
+            mg.profile(False)
+            for k, v in mg.profile_read().items():
+                kern[f"{dim.split(':')[1]}:{k}"] = {"ms_total": round(v[0], 4), "launches": v[1]}
+            res[dim.split(":")[1]] = {"ms_per_step": round(ms, 4), "samples_per_s": plan.output_bytes / (ms * 1e-3)}
+            total_samples += plan.output_bytes
+            total_ms += ms
+    out = {"metric": METRIC, "value": total_samples * world / (total_ms * 1e-3), "unit": UNIT, "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (SplitMix64(2) seeds)",
+           "config": {"workload": "other dimensions 26.3: 4096 SplitMix64(2) seeds x 64x64 quart grid at y=64, "
+                                  "Nether and End, one batched launch per dimension", "per_dimension": res},
+           "kernels": kern, "gpu_launches": args.steps * 4}
+    clocks = clk.summary()
+    if clocks:
+        out["clocks"] = clocks
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 def run_serve(args, rank, world, local_rank, mg, ge):
     """Serving: open-loop Poisson streams at several rates, continuous batching, 8 GB noise-state cache."""
     import torch
@@ -536,7 +622,7 @@ def run_serve(args, rank, world, local_rank, mg, ge):
     with ClockSampler(local_rank) as clk:
         for rate in rates:
             runs[str(int(rate))] = serve_run(mg, worlds, config5_stream(rate, args.duration), 8 << 30)
-        small = serve_run(mg, worlds, config5_stream(rates[len(rates) // 2], args.duration / 2), 64 << 20)
+        small = serve_run(mg, worlds, config5_stream(rates[len(rates) // 2], args.duration / 2), 2 << 20)
     top = runs[str(int(rates[-1]))]
     out = {"metric": METRIC + " (served)", "value": top["samples_per_s"], "unit": UNIT, "n_gpus": world,
            "steps": len(rates), "warmup": 1, "ms_per_step": top["elapsed_s"] * 1e3, "higher_is_better": True,
@@ -547,7 +633,7 @@ def run_serve(args, rank, world, local_rank, mg, ge):
                                   "continuous batching on 2 streams, 8 GB noise-state cache (LRU)",
                       "rates": rates, "duration_s": args.duration,
                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
-           "served": runs, "small_budget_64MB": small,
+           "served": runs, "small_budget_2MB": small,
            "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
            "e2e": {"value": top["samples_per_s"], "unit": UNIT, "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": int(top["samples_per_s"] * top["elapsed_s"])}}
@@ -601,6 +687,38 @@ def run_reference(args, rank, world):
         sample = f"first {n} of the 65536 seeds x 8 points per step"
         config = {"workload": "Overworld 26.3 normal, 65536 SplitMix64(1) seeds x 8 fixed points, ENGINE tie rule",
                   "version": "26.3", "dimension": "overworld"}
+    elif args.workload in ("batch10k", "serve"):
+        reqs = config4_requests(args.requests)
+        nfirst = 256
+        wl = {}
+        for v, d, *_ in reqs[:nfirst]:
+            if (v, d) not in wl:
+                wl[(v, d)] = O.World(ge.data_root(), v, d.split(":")[1])
+
+        def per_step():
+            for v, d, s, qx0, qz0, n, qy in reqs[:nfirst]:
+                wl[(v, d)].quart_grid(s, qx0, qz0, n, n, qy, O.TIE_ENGINE, threads=cores)
+
+        samples = sum(n * n for *_, n, qy in reqs[:nfirst])
+        sample = f"first {nfirst} of the {len(reqs)} uneven-batch requests ({samples} samples) per step, rows over threads"
+        config = {"workload": f"uneven mixed batch: {len(reqs)} SplitMix64(3) requests, versions 26.1/26.2/26.3, "
+                              "Overworld:Nether:End 6:2:2, square side log-uniform in [16,512) quart cells, origin "
+                              "uniform in [-30000,30000] blocks, y=64, ENGINE tie rule", "requests": len(reqs)}
+    elif args.workload == "dims4096":
+        seeds = splitmix64(2, 4096).view(np.int64)
+        wn = O.World(ge.data_root(), "26.3", "the_nether")
+        we = O.World(ge.data_root(), "26.3", "the_end")
+        nfirst = 16
+
+        def per_step():
+            for sd in seeds[:nfirst]:
+                wn.quart_grid(int(sd), -32, -32, 64, 64, 16, O.TIE_ENGINE, threads=cores)
+                we.quart_grid(int(sd), -32, -32, 64, 64, 16, O.TIE_ENGINE, threads=cores)
+
+        samples = nfirst * 2 * 64 * 64
+        sample = f"first {nfirst} of the 4096 seeds, Nether and End 64x64 grids per step"
+        config = {"workload": "other dimensions 26.3: 4096 SplitMix64(2) seeds x 64x64 quart grid at y=64, "
+                              "Nether and End"}
     else:
         rows = 32
         per_step = lambda: w.biome_grid(12345, -512, -512, 256, rows, 4, 64, threads=cores)  # noqa: E731
@@ -630,7 +748,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["seeds8", "grid256", "batch10k", "serve"], default="seeds8")
+    ap.add_argument("--workload", choices=["seeds8", "grid256", "batch10k", "serve", "dims4096"], default="batch10k")
     ap.add_argument("--rates", default="500,1000,2000", help="serve: arrival rates (requests/s)")
     ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds per rate (60 = the configuration)")
     ap.add_argument("--requests", type=int, default=10000, help="batch10k: number of requests")

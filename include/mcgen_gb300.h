@@ -76,9 +76,13 @@ MCGEN_API long long mcgen_gb300_plan_output_bytes(const McGb300Plan *p);
 MCGEN_API long long mcgen_gb300_plan_output_offset(const McGb300Plan *p, int i);
 /* the tile shape in use: 0 (32 x 4), 1 (16 x 8), 2 (64 x 2), 3 (8 x 16) */
 MCGEN_API int mcgen_gb300_plan_shape(const McGb300Plan *p);
+MCGEN_API int mcgen_gb300_plan_set_shape(McGb300Plan *p, int shape);
+/* bytes plan_new copied to the device (worlds, request and setup lists) */
+MCGEN_API long long mcgen_gb300_plan_h2d_bytes(const McGb300Plan *p);
 /* time the four tile shapes on this plan (reps runs each into d_out) and keep the fastest */
 MCGEN_API int mcgen_gb300_plan_autotune(McGb300Plan *p, uint8_t *d_out, int reps, double *best_ms);
-/* run into device memory on `stream` (graph replay) / without a graph / into host memory */
+/* run into device memory on `stream` (graph replay) / without a graph / into host memory (direct launches,
+ * outputs copied back, synchronous) */
 MCGEN_API int mcgen_gb300_plan_run_dev(McGb300Plan *p, uint8_t *d_out, void *stream);
 MCGEN_API int mcgen_gb300_plan_run_dev_direct(McGb300Plan *p, uint8_t *d_out, void *stream);
 MCGEN_API int mcgen_gb300_plan_run(McGb300Plan *p, uint8_t *out);
@@ -108,8 +112,8 @@ MCGEN_API int mcgen_gb300_server_stats(McGb300Server *s, McGb300ServerStats *out
 /* Allocation-free form of mcgen_gb300_seed_points_dev, for callers that cannot let a library allocate
  * device memory (their own memory arena, latency-critical loops, no allocation after set-up).  No
  * counterpart in the reference.  The per-seed noise lattices go to one fixed 16 MiB device array inside
- * the library instead of per-call scratch, so ns * (lattices per seed) * 320 bytes must fit: at most 1,139
- * Overworld, 6,553 Nether or 52,428 End seeds per call; larger calls return MCGEN_E_ARG (split them).
+ * the library instead of per-call scratch, so ns * (lattices per seed) * 352 bytes must fit: at most 1,036
+ * Overworld, 5,957 Nether or 47,662 End seeds per call; larger calls return MCGEN_E_ARG (split them).
  * The caller passes device inputs and outputs as for _dev.  The world must already be on the device (any
  * earlier biome call on it puts it there), else MCGEN_E_ARG.  The first call on a device looks up the
  * array's address; make it before any stream capture.  Calls share the array: calls whose GPU work

@@ -24,7 +24,7 @@ MCGEN_E_NOMEM, MCGEN_E_CANCEL, MCGEN_E_UNSUPPORTED, MCGEN_E_INTERNAL = 5, 6, 7, 
 MCGEN_COMPUTE_CPU, MCGEN_COMPUTE_GPU, MCGEN_COMPUTE_AUTO = 0, 1, 2
 TIE_ENGINE, TIE_GRID_CHAIN, TIE_CHUNK_CELL = 0, 1, 2
 PIPES = {"fp32_fma": 0, "fp64_fma": 1, "fp64_add": 2, "int32_mad": 3, "cvt_f64_floor_s32": 4,
-         "cvt_s32_f64": 5, "cvt_f64_f32": 6, "int64_mad": 7}
+         "cvt_s32_f64": 5, "cvt_f64_f32": 6, "int64_mad": 7, "cvt_s64_f64": 8, "cvt_f32_f64": 9}
 ERR_BUF = 1024
 _P = C.c_void_p
 
@@ -102,6 +102,8 @@ _PROTOS.update({
     "mcgen_gb300_plan_output_bytes": (C.c_longlong, [_P]),
     "mcgen_gb300_plan_output_offset": (C.c_longlong, [_P, C.c_int]),
     "mcgen_gb300_plan_shape": (C.c_int, [_P]),
+    "mcgen_gb300_plan_set_shape": (C.c_int, [_P, C.c_int]),
+    "mcgen_gb300_plan_h2d_bytes": (C.c_longlong, [_P]),
     "mcgen_gb300_plan_autotune": (C.c_int, [_P, _P, C.c_int, C.POINTER(C.c_double)]),
     "mcgen_gb300_plan_run_dev": (C.c_int, [_P, _P, _P]),
     "mcgen_gb300_plan_run_dev_direct": (C.c_int, [_P, _P, _P]),
@@ -411,6 +413,14 @@ class Plan:
     @property
     def shape(self) -> int:
         return load().mcgen_gb300_plan_shape(self._h)
+
+    @shape.setter
+    def shape(self, s: int):
+        _check(load().mcgen_gb300_plan_set_shape(self._h, s), "mcgen_gb300_plan_set_shape")
+
+    @property
+    def h2d_bytes(self) -> int:
+        return load().mcgen_gb300_plan_h2d_bytes(self._h)
 
     def autotune(self, d_out: int, reps: int = 2) -> float:
         ms = C.c_double()

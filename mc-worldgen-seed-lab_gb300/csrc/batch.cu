@@ -44,7 +44,7 @@ __device__ __forceinline__ void lst_store(uint32_t (*perm)[LNT], int t, MgLattic
     lattice_header(h);
     const uint4 *src = reinterpret_cast<const uint4 *>(&h);
     uint4 *dst = reinterpret_cast<uint4 *>(L);
-    for (int q = 0; q < 4; q++) dst[q] = src[q];
+    for (int q = 0; q < MG_LAT_HDR_WORDS; q++) dst[q] = src[q];
     uint4 *dp = reinterpret_cast<uint4 *>(L->p);
     for (int q = 0; q < 16; q++) dp[q] = make_uint4(perm[4 * q][t], perm[4 * q + 1][t], perm[4 * q + 2][t], perm[4 * q + 3][t]);
 }

@@ -91,15 +91,27 @@ __device__ __forceinline__ int ifloor(double v) { return __double2int_rd(v); }
 __device__ __forceinline__ int64_t lfloor(double v) { return __double2ll_rd(v); }
 
 /* ------------------------------------------------------------------ lattice header */
-/* fill the y/z splits a zero input coordinate uses */
-__device__ __forceinline__ void lattice_header(MgLattice &L) {
+template <typename T>
+__device__ __forceinline__ T fade_h(T t) { return t * t * t * (t * (t * (T)6 - (T)15) + (T)10); }
+/* fill the y/z splits a zero input coordinate uses (the reference computes the same values per sample);
+ * H is MgLattice or any header with the same field names */
+template <typename H>
+__device__ __forceinline__ void lattice_header(H &L) {
     L.iy = ifloor(L.oy);
     L.iz = ifloor(L.oz);
     L.fyd = L.oy - (double)L.iy;
     L.fzd = L.oz - (double)L.iz;
+    L.gyd = L.fyd - 1.0;
+    L.gzd = L.fzd - 1.0;
+    L.uyd = fade_h<double>(L.fyd);
+    L.uzd = fade_h<double>(L.fzd);
     L.fy = (float)L.fyd;
     L.fz = (float)L.fzd;
+    L.uy = fade_h<float>(L.fy);
+    L.uz = fade_h<float>(L.fz);
 }
+/* the header's 16-byte words (the permutation follows them) */
+#define MG_LAT_HDR_WORDS ((int)(offsetof(MgLattice, p) / 16))
 
 /* ------------------------------------------------------------------ Perlin octave (shared lattice math) */
 /* gradient dot with SimplexNoise.GRADIENT[h & 15]: every vector has two +-1 components, so the dot is a
@@ -135,13 +147,15 @@ struct IlvPerm {
     }
 };
 
-/* ImprovedNoise.sampleAndLerp with split coordinates (engine/mc_noise.h:54-75 / 90-110). */
+/* ImprovedNoise.sampleAndLerp with split coordinates (engine/mc_noise.h:54-75 / 90-110); g* = f* - 1 and
+ * u, v, w = fade(fx), fade(fy), fade(fz) are passed in so that a coordinate split once per lattice (the
+ * zero input coordinate) is not recomputed per sample. */
 template <typename T, typename P>
-__device__ __forceinline__ T octave_p(const P &p, int ix, T fx, int iy, T fy, int iz, T fz) {
+__device__ __forceinline__ T octave_q(const P &p, int ix, T fx, int iy, T fy, T gy, T v, int iz, T fz, T gz, T w) {
     int a = p(ix), b = p(ix + 1);
     int aa = p(a + iy), ab = p(a + iy + 1);
     int ba = p(b + iy), bb = p(b + iy + 1);
-    T gx = fx - (T)1, gy = fy - (T)1, gz = fz - (T)1;
+    T gx = fx - (T)1;
     T c000 = gdot<T>(p(aa + iz), fx, fy, fz);
     T c100 = gdot<T>(p(ba + iz), gx, fy, fz);
     T c010 = gdot<T>(p(ab + iz), fx, gy, fz);
@@ -150,9 +164,41 @@ __device__ __forceinline__ T octave_p(const P &p, int ix, T fx, int iy, T fy, in
     T c101 = gdot<T>(p(ba + iz + 1), gx, fy, gz);
     T c011 = gdot<T>(p(ab + iz + 1), fx, gy, gz);
     T c111 = gdot<T>(p(bb + iz + 1), gx, gy, gz);
-    T u = fade<T>(fx), v = fade<T>(fy), w = fade<T>(fz);
+    T u = fade<T>(fx);
     return lerp<T>(w, lerp<T>(v, lerp<T>(u, c000, c100), lerp<T>(u, c010, c110)),
                    lerp<T>(v, lerp<T>(u, c001, c101), lerp<T>(u, c011, c111)));
+}
+template <typename T, typename P>
+__device__ __forceinline__ T octave_p(const P &p, int ix, T fx, int iy, T fy, int iz, T fz) {
+    return octave_q<T>(p, ix, fx, iy, fy, fy - (T)1, fade<T>(fy), iz, fz, fz - (T)1, fade<T>(fz));
+}
+/* input coordinate y (resp. z) zero: its split comes from the lattice header */
+template <typename T> struct Hdr;
+template <> struct Hdr<float> {
+    template <typename H> __device__ static float fy(const H &h) { return h.fy; }
+    template <typename H> __device__ static float fz(const H &h) { return h.fz; }
+    template <typename H> __device__ static float gy(const H &h) { return h.fy - 1.0f; }
+    template <typename H> __device__ static float gz(const H &h) { return h.fz - 1.0f; }
+    template <typename H> __device__ static float uy(const H &h) { return h.uy; }
+    template <typename H> __device__ static float uz(const H &h) { return h.uz; }
+};
+template <> struct Hdr<double> {
+    template <typename H> __device__ static double fy(const H &h) { return h.fyd; }
+    template <typename H> __device__ static double fz(const H &h) { return h.fzd; }
+    template <typename H> __device__ static double gy(const H &h) { return h.gyd; }
+    template <typename H> __device__ static double gz(const H &h) { return h.gzd; }
+    template <typename H> __device__ static double uy(const H &h) { return h.uyd; }
+    template <typename H> __device__ static double uz(const H &h) { return h.uzd; }
+};
+template <typename T, typename P, typename H>
+__device__ __forceinline__ T octave_y0(const P &p, const H &h, int ix, T fx, int iz, T fz) {
+    using Q = Hdr<T>;
+    return octave_q<T>(p, ix, fx, h.iy, Q::fy(h), Q::gy(h), Q::uy(h), iz, fz, fz - (T)1, fade<T>(fz));
+}
+template <typename T, typename P, typename H>
+__device__ __forceinline__ T octave_z0(const P &p, const H &h, int ix, T fx, int iy, T fy) {
+    using Q = Hdr<T>;
+    return octave_q<T>(p, ix, fx, iy, fy, fy - (T)1, fade<T>(fy), h.iz, Q::fz(h), Q::gz(h), Q::uz(h));
 }
 template <typename T>
 __device__ __forceinline__ T octave(const uint8_t *__restrict__ p, int ix, T fx, int iy, T fy, int iz, T fz) {
@@ -290,28 +336,28 @@ __device__ __forceinline__ float oct_f_y0(const MgLattice *__restrict__ L, doubl
     float fx, fz;
     split_fk(x, f, k, L->ox, ix, fx);
     split_fk(z, f, k, L->oz, iz, fz);
-    return octave<float>(L->p, ix, fx, L->iy, L->fy, iz, fz);
+    return octave_y0<float>(PlainPerm{L->p}, *L, ix, fx, iz, fz);
 }
 __device__ __forceinline__ float oct_f_z0(const MgLattice *__restrict__ L, double x, double y, double f, int k) {
     int ix, iy;
     float fx, fy;
     split_fk(x, f, k, L->ox, ix, fx);
     split_fk(y, f, k, L->oy, iy, fy);
-    return octave<float>(L->p, ix, fx, iy, fy, L->iz, L->fz);
+    return octave_z0<float>(PlainPerm{L->p}, *L, ix, fx, iy, fy);
 }
 __device__ __forceinline__ double oct_d_y0(const MgLattice *__restrict__ L, double x, double z, double f, int k) {
     int ix, iz;
     double fx, fz;
     split_dk(x, f, k, L->ox, ix, fx);
     split_dk(z, f, k, L->oz, iz, fz);
-    return octave<double>(L->p, ix, fx, L->iy, L->fyd, iz, fz);
+    return octave_y0<double>(PlainPerm{L->p}, *L, ix, fx, iz, fz);
 }
 __device__ __forceinline__ double oct_d_z0(const MgLattice *__restrict__ L, double x, double y, double f, int k) {
     int ix, iy;
     double fx, fy;
     split_dk(x, f, k, L->ox, ix, fx);
     split_dk(y, f, k, L->oy, iy, fy);
-    return octave<double>(L->p, ix, fx, iy, fy, L->iz, L->fzd);
+    return octave_z0<double>(PlainPerm{L->p}, *L, ix, fx, iy, fy);
 }
 
 /* ------------------------------------------------------------------ NormalNoise (engine/mc_noise.h:285-324)

@@ -35,9 +35,9 @@ namespace mg {
 
 /* header of an offset-noise lattice, shared so that any thread can sample it */
 struct OffHdr {
-    double ox, oy, oz, fyd, fzd;
+    double ox, oy, oz, fyd, fzd, gyd, gzd, uyd, uzd;
     int iy, iz;
-    float fy, fz;
+    float fy, fz, uy, uz;
 };
 
 template <typename V>
@@ -104,15 +104,10 @@ __global__ void __launch_bounds__(FNT) k_ow_seed_climate(const __grid_constant__
         }
     }
     /* split of the offsets used by a zero input coordinate */
-    const int iy = ifloor(oy), iz = ifloor(oz);
-    const double fyd = oy - (double)iy, fzd = oz - (double)iz;
-    const float fy = (float)fyd, fz = (float)fzd;
-    if (t < nown) {
-        OffHdr h;
-        h.ox = ox; h.oy = oy; h.oz = oz; h.fyd = fyd; h.fzd = fzd;
-        h.iy = iy; h.iz = iz; h.fy = fy; h.fz = fz;
-        sm.hdr[t] = h;
-    }
+    OffHdr h;
+    h.ox = ox; h.oy = oy; h.oz = oz;
+    lattice_header(h);
+    if (t < nown) sm.hdr[t] = h;
     const uint8_t *pbase = reinterpret_cast<const uint8_t *>(&sm.perm[0][0]);
     const MgNoise &N = W.noise[noise];
     const double f = N.freq[lev];
@@ -127,7 +122,7 @@ __global__ void __launch_bounds__(FNT) k_ow_seed_climate(const __grid_constant__
             const int oj = o / spc;
             const int ost = oj >= O.nlev, olev = oj - ost * O.nlev;
             if (s0 + o % spc >= ns) continue;
-            const OffHdr &h = sm.hdr[o];
+            const OffHdr &oh = sm.hdr[o];
             const IlvPerm<FNT> perm{pbase, o};
             double X = (double)pts[3 * (p0 + p)], Z = (double)pts[3 * (p0 + p) + 2];
             if (ost) { X = X * MG_SECOND_STACK; Z = Z * MG_SECOND_STACK; }
@@ -136,21 +131,21 @@ __global__ void __launch_bounds__(FNT) k_ow_seed_climate(const __grid_constant__
             if (FM) {
                 int ix, izz, iyy;
                 float fx, fzz, fyy;
-                split_fk(X, of, ok, h.ox, ix, fx);
-                split_fk(Z, of, ok, h.oz, izz, fzz);
-                sm.val[o][p] = (V)octave_p<float>(perm, ix, fx, h.iy, h.fy, izz, fzz);
-                split_fk(Z, of, ok, h.ox, ix, fx);
-                split_fk(X, of, ok, h.oy, iyy, fyy);
-                sm.valb[o][p] = (V)octave_p<float>(perm, ix, fx, iyy, fyy, h.iz, h.fz);
+                split_fk(X, of, ok, oh.ox, ix, fx);
+                split_fk(Z, of, ok, oh.oz, izz, fzz);
+                sm.val[o][p] = (V)octave_y0<float>(perm, oh, ix, fx, izz, fzz);
+                split_fk(Z, of, ok, oh.ox, ix, fx);
+                split_fk(X, of, ok, oh.oy, iyy, fyy);
+                sm.valb[o][p] = (V)octave_z0<float>(perm, oh, ix, fx, iyy, fyy);
             } else {
                 int ix, izz, iyy;
                 double fx, fzz, fyy;
-                split_dk(X, of, ok, h.ox, ix, fx);
-                split_dk(Z, of, ok, h.oz, izz, fzz);
-                sm.val[o][p] = (V)octave_p<double>(perm, ix, fx, h.iy, h.fyd, izz, fzz);
-                split_dk(Z, of, ok, h.ox, ix, fx);
-                split_dk(X, of, ok, h.oy, iyy, fyy);
-                sm.valb[o][p] = (V)octave_p<double>(perm, ix, fx, iyy, fyy, h.iz, h.fzd);
+                split_dk(X, of, ok, oh.ox, ix, fx);
+                split_dk(Z, of, ok, oh.oz, izz, fzz);
+                sm.val[o][p] = (V)octave_y0<double>(perm, oh, ix, fx, izz, fzz);
+                split_dk(Z, of, ok, oh.ox, ix, fx);
+                split_dk(X, of, ok, oh.oy, iyy, fyy);
+                sm.valb[o][p] = (V)octave_z0<double>(perm, oh, ix, fx, iyy, fyy);
             }
         }
         __syncthreads();
@@ -198,13 +193,13 @@ __global__ void __launch_bounds__(FNT) k_ow_seed_climate(const __grid_constant__
                     float fx, fzz;
                     split_fk(x, f, fk, ox, ix, fx);
                     split_fk(z, f, fk, oz, izz, fzz);
-                    sm.val[t][p] = (V)octave_p<float>(perm, ix, fx, iy, fy, izz, fzz);
+                    sm.val[t][p] = (V)octave_y0<float>(perm, h, ix, fx, izz, fzz);
                 } else {
                     int ix, izz;
                     double fx, fzz;
                     split_dk(x, f, fk, ox, ix, fx);
                     split_dk(z, f, fk, oz, izz, fzz);
-                    sm.val[t][p] = (V)octave_p<double>(perm, ix, fx, iy, fyd, izz, fzz);
+                    sm.val[t][p] = (V)octave_y0<double>(perm, h, ix, fx, izz, fzz);
                 }
             }
         }

@@ -59,7 +59,7 @@ __device__ __forceinline__ void header_store(MgLattice &h, MgLattice *L) {
     const uint4 *src = reinterpret_cast<const uint4 *>(&h);
     uint4 *dst = reinterpret_cast<uint4 *>(L);
 #pragma unroll
-    for (int q = 0; q < 4; q++) dst[q] = src[q];
+    for (int q = 0; q < MG_LAT_HDR_WORDS; q++) dst[q] = src[q];
 }
 
 /* Overworld: lattice j of seed s; table layout noise-major, then stack, then level

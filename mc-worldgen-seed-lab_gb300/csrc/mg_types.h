@@ -82,14 +82,17 @@ typedef struct {
     MgSpline spline;
 } MgWorldDesc;
 
-/* One Perlin octave of one seed: offsets, the y/z lattice split of the offsets (used whenever
- * that input coordinate is zero), and the permutation. 320 bytes, 16-byte aligned. */
+/* One Perlin octave of one seed: offsets, the lattice split of the y and z offsets (what a zero input
+ * coordinate uses: fraction, fraction - 1 and smoothstep of the fraction), and the permutation.
+ * 352 bytes, 16-byte aligned; the 96-byte header precedes the permutation. */
 typedef struct __attribute__((aligned(16))) {
     double ox, oy, oz;
     double fyd, fzd;   /* oy - floor(oy), oz - floor(oz) (double branch) */
+    double gyd, gzd;   /* fyd - 1.0, fzd - 1.0 */
+    double uyd, uzd;   /* smoothstep(fyd), smoothstep(fzd) */
     int32_t iy, iz;    /* floor(oy), floor(oz) */
-    float fy, fz;      /* (float)(oy - iy), (float)(oz - iz) (float branch) */
-    uint8_t pad[8];
+    float fy, fz;      /* (float)fyd, (float)fzd (float branch) */
+    float uy, uz;      /* smoothstep(fy), smoothstep(fz) in float */
     uint8_t p[256];
 } MgLattice;
 

@@ -40,18 +40,33 @@ __global__ void __launch_bounds__(256) k_pipe(int iters, unsigned long long *sin
             if (OP == 1) asm volatile("fma.rn.f64 %0, %0, %1, %2;" : "+d"(d[c]) : "d"(db), "d"(dc));
             if (OP == 2) asm volatile("add.rn.f64 %0, %0, %1;" : "+d"(d[c]) : "d"(dc));
             if (OP == 3) asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(u[c]) : "r"(0xDEECE66Du), "r"(11u));
+            /* conversions: each result feeds the next conversion of its chain through one integer op on
+             * its bits, so no conversion is loop-invariant or dead */
             if (OP == 4) {
                 int r;
                 asm volatile("cvt.rmi.s32.f64 %0, %1;" : "=r"(r) : "d"(d[c]));
-                acc += r;
+                d[c] = __hiloint2double(__double2hiint(d[c]), __double2loint(d[c]) ^ r);
             }
-            if (OP == 5) asm volatile("cvt.rn.f64.s32 %0, %1;" : "=d"(d[c]) : "r"((int)u[c] + it));
+            if (OP == 5) {
+                const int x = __double2loint(d[c]) + 1;
+                asm volatile("cvt.rn.f64.s32 %0, %1;" : "=d"(d[c]) : "r"(x));
+            }
             if (OP == 6) {
                 float r;
                 asm volatile("cvt.rn.f32.f64 %0, %1;" : "=f"(r) : "d"(d[c]));
-                f[c] += r;
+                d[c] = __hiloint2double(__double2hiint(d[c]), __double2loint(d[c]) ^ __float_as_int(r));
             }
             if (OP == 7) asm volatile("mad.lo.u64 %0, %0, %1, %2;" : "+l"(w[c]) : "l"(0x5DEECE66DULL), "l"(11ULL));
+            if (OP == 8) {
+                double r;
+                asm volatile("cvt.rn.f64.s64 %0, %1;" : "=d"(r) : "l"(w[c]));
+                w[c] = (uint64_t)__double_as_longlong(r) ^ 0x5DEEu;
+            }
+            if (OP == 9) {
+                double r;
+                asm volatile("cvt.f64.f32 %0, %1;" : "=d"(r) : "f"(f[c]));
+                f[c] = __int_as_float(__double2hiint(r) ^ 0x5DEE);
+            }
         }
     }
     unsigned long long h = (unsigned long long)acc;
@@ -71,7 +86,7 @@ static int run_pipe(double *gops) {
     cudaError_t e = cudaMalloc(&sink, sizeof(unsigned long long) * (size_t)nt * nb);
     if (e) return (int)e;
     /* FP64-class operations may be ~64x slower per SM than FP32: size each loop for tens of ms */
-    const bool slow = OP == 1 || OP == 2 || OP == 4 || OP == 5 || OP == 6 || OP == 7;
+    const bool slow = OP != 0 && OP != 3;
     const int iters = slow ? 8192 : 8192 * 4;
     cudaEvent_t a, b;
     cudaEventCreate(&a);
@@ -102,6 +117,8 @@ int pipe_rate(int pipe, double *gops) {
     case 5: return run_pipe<5>(gops);
     case 6: return run_pipe<6>(gops);
     case 7: return run_pipe<7>(gops);
+    case 8: return run_pipe<8>(gops);
+    case 9: return run_pipe<9>(gops);
     default: return (int)cudaErrorInvalidValue;
     }
 }

@@ -24,6 +24,7 @@ struct McGb300Plan {
     int nreq = 0;
     long long ntiles[BATCH_SHAPES] = {0, 0, 0, 0};
     long long out_bytes = 0;
+    long long h2d_bytes = 0; /* bytes copied to the device by plan_new */
     std::vector<long long> out_off;
     std::vector<long long> cells;
     int shape = 0;
@@ -155,6 +156,7 @@ MCGEN_API int mcgen_gb300_plan_new(const McGb300Request *reqs, int n, int tie_ru
     auto up = [&](void **dst, const void *src, size_t bytes) {
         if (e || !bytes) return;
         if ((e = cudaMalloc(dst, bytes)) == cudaSuccess) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+        p->h2d_bytes += (long long)bytes;
     };
     up((void **)&p->d_worlds, wd.data(), sizeof(MgWorldDesc) * wd.size());
     up((void **)&p->d_trees, tp.data(), sizeof(void *) * tp.size());
@@ -191,6 +193,12 @@ MCGEN_API long long mcgen_gb300_plan_output_offset(const McGb300Plan *p, int i) 
     return (p && i >= 0 && i < p->nreq) ? p->out_off[(size_t)i] : -1;
 }
 MCGEN_API int mcgen_gb300_plan_shape(const McGb300Plan *p) { return p ? p->shape : -1; }
+MCGEN_API long long mcgen_gb300_plan_h2d_bytes(const McGb300Plan *p) { return p ? p->h2d_bytes : -1; }
+MCGEN_API int mcgen_gb300_plan_set_shape(McGb300Plan *p, int shape) {
+    if (!p || shape < 0 || shape >= BATCH_SHAPES) return MCGEN_E_ARG;
+    p->shape = shape;
+    return MCGEN_OK;
+}
 
 /* Run into device memory (plan_output_bytes bytes at d_out) on `stream`, through the plan's CUDA graph. */
 MCGEN_API int mcgen_gb300_plan_run_dev(McGb300Plan *p, uint8_t *d_out, void *stream) {
@@ -255,7 +263,8 @@ MCGEN_API int mcgen_gb300_plan_autotune(McGb300Plan *p, uint8_t *d_out, int reps
     return MCGEN_OK;
 }
 
-/* Host-buffer form: runs the plan and copies the outputs to `out` (plan_output_bytes bytes). */
+/* Host-buffer form: runs the plan (direct launches: a one-off run gains nothing from a graph) and copies
+ * the outputs to `out` (plan_output_bytes bytes). */
 MCGEN_API int mcgen_gb300_plan_run(McGb300Plan *p, uint8_t *out) {
     if (!p || (!out && p->out_bytes)) return MCGEN_E_ARG;
     if (!p->nreq) return MCGEN_OK;
@@ -263,7 +272,7 @@ MCGEN_API int mcgen_gb300_plan_run(McGb300Plan *p, uint8_t *out) {
     cudaStream_t st = mg::abi_stream();
     cudaError_t e = cudaMallocAsync((void **)&d_out, (size_t)p->out_bytes, st);
     if (e) return cuda_rc(e);
-    int rc = mcgen_gb300_plan_run_dev(p, d_out, st);
+    int rc = mcgen_gb300_plan_run_dev_direct(p, d_out, st);
     if (!rc) rc = cuda_rc(cudaMemcpyAsync(out, d_out, (size_t)p->out_bytes, cudaMemcpyDeviceToHost, st));
     cudaFreeAsync(d_out, st);
     cudaError_t e2 = cudaStreamSynchronize(st);

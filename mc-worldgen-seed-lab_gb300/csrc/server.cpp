@@ -8,7 +8,7 @@
  * persistent k_batch launch, and copies the ids back.  When a batch's event completes the worker hands
  * every request its ids and wakes its waiters.
  *
- * Noise-state cache: per dimension a pool of fixed-size slots (46 lattices of 320 B for the Overworld, 8 for
+ * Noise-state cache: per dimension a pool of fixed-size slots (46 lattices of 352 B for the Overworld, 8 for
  * the Nether, 1 for the End) carved from one HBM budget, keyed by (world, seed), evicted least recently
  * used among slots that no in-flight batch references.
  */
