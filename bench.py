@@ -2,16 +2,17 @@
 """Benchmark of the bit-exact biome path on GB300 (one JSON line on rank 0).
 
 Workloads (synthetic inputs with the shapes of the published configurations):
-  seeds8   (default) Overworld 26.3, 65,536 SplitMix64(1) world seeds x the same 8 points
+  seeds8   Overworld 26.3, 65,536 SplitMix64(1) world seeds x the same 8 points
            (x, z uniform in [-10000, 10000] blocks, y uniform in [-64, 320]; quart cells = block >> 2):
            per-seed noise setup + climate + R-tree, ENGINE tie rule.  [65536, 8] biome ids.
   grid256  Overworld 26.3, seed 12345, mcgen_biome_grid 256 x 256 cells, x,z in [-512, 512) step 4,
            y = 64 (BiomeManager zoom + chunk-cell ties).  65,536 samples per step.
   dims4096 Nether 26.3 and End 26.3: 4,096 SplitMix64(2) seeds x a 64 x 64 quart grid at y = 64 each, one
            batched launch per dimension.
-  batch10k the uneven mixed batch: 10,000 SplitMix64(3) requests (versions 26.1/26.2/26.3, Overworld:Nether:
-           End 6:2:2, side log-uniform in [16, 512) quart cells), one persistent launch, against the plain
-           form (one setup + one grid launch per request).
+  batch10k (default) the uneven mixed batch: 10,000 SplitMix64(3) requests (versions 26.1/26.2/26.3,
+           Overworld:Nether:End 6:2:2, side log-uniform in [16, 512) quart cells), one persistent launch, against
+           the plain form (one setup + one grid launch per request).  e2e: per step a plan is built from the
+           host request list, run into pinned host memory and freed.
   serve    open-loop Poisson streams at 500/1000/2000 requests/s (SplitMix64(4), Zipf(1.1) over 50,000
            seeds) against the continuous-batching server; p50/p99 latency, cache hit rate.
 
@@ -66,6 +67,16 @@ def config2_inputs(n_seeds: int = 65536):
     z = -10000 + (r[16:24] % np.uint64(20001)).astype(np.int64)
     pts = np.stack([x >> 2, y >> 2, z >> 2], 1).astype(np.int32)
     return seeds, pts
+
+
+def config3_inputs(n_seeds: int = 4096):
+    """Other dimensions: 4,096 SplitMix64(2) seeds, each with a 64 x 64 quart grid at y=64 whose corner is drawn
+    from SplitMix64(102) uniformly in [-30000, 30000) blocks (quart = block >> 2), so that the End grids sample
+    the outer islands and not only the central island (|chunk| <= 64)."""
+    seeds = splitmix64(2, n_seeds).view(np.int64)
+    r = splitmix64(102, 2 * n_seeds).reshape(n_seeds, 2)
+    origins = ((-30000 + (r % np.uint64(60000)).astype(np.int64)) >> 2).astype(np.int32)
+    return seeds, origins
 
 
 C4_VERSIONS = ("26.1", "26.2", "26.3")
@@ -178,13 +189,19 @@ def batch_fp64_ops(reqs) -> float:
 
 # Algorithmic work per launch of each kernel, counted from the reference algorithm:
 # (work units per launch, unit name, pipe peak key).
+# DRAM bytes (read + write) per work unit of a launch, from one ncu capture each: k_batch per sample
+# (300-request prefix of the uneven batch), k_ow_seed_climate per seed (4,096 seeds x 8 points).
+DRAM_BYTES_PER_UNIT = {"k_batch": (4486912 + 955136) / 10987120, "k_ow_seed_climate": 98560 / 4096}
+
+
 def kernel_work(kernel: str, seeds8: bool, ns: int, np_: int, ntables: int) -> tuple[float, str, str] | None:
-    if kernel == "k_setup_xo":
-        # 256 Fisher-Yates steps per lattice, each one Xoroshiro128++ draw (9 64-bit ALU ops = 18 32-bit ops),
-        # a 32x32->64 multiply and compare (3 ops) and a swap (2 loads + 2 stores): 25 int32-pipe ops; plus
-        # 3 nextDouble draws (3 x 18 + 3 conversions) per lattice.
-        ops = ns * ntables * (256 * 25 + 3 * 21)
-        return ops, "Gop/s", "int32_mad"
+    # Integer ALU work of the per-seed setup, which bounds both kernels below (the fused kernel's ALU pipe
+    # is its busiest): per lattice 256 Fisher-Yates steps, each one Xoroshiro128++ draw (16 32-bit ALU ops:
+    # two 64-bit adds, three 64-bit rotates, a shift and two 3-input xors), the Lemire bound (3) and the
+    # swap addressing (2); plus three nextDouble draws (16 + 4 each).
+    per_lattice = 256 * (16 + 3 + 2) + 3 * 20
+    if kernel in ("k_setup_xo", "k_ow_seed_climate"):
+        return float(ns * ntables * per_lattice), "Gop/s", "int32_mad"
     return None
 
 
@@ -338,9 +355,11 @@ def run_gb300(args, rank, world, local_rank):
             if wk and peaks:
                 ops, unit, peak_key = wk
                 achieved = ops / avg_s / 1e9
+                per = DRAM_BYTES_PER_UNIT.get(top)
                 out["roofline"] = {"kernel": top, "bound": peak_key, "achieved": round(achieved, 1),
                                    "peak": peaks[peak_key], "unit": unit, "frac": round(achieved / peaks[peak_key], 4),
-                                   "traffic": None, "peak_source": "measured in-run (pipe microbenchmark)"}
+                                   "traffic": round(per * seeds.size) if per is not None else None,
+                                   "peak_source": "measured in-run (pipe microbenchmark)"}
             else:
                 out["roofline"] = {"kernel": top, "bound": None, "achieved": None, "peak": None, "unit": None,
                                    "frac": None, "traffic": None}
@@ -429,15 +448,30 @@ def run_batch(args, rank, world, local_rank, mg, ge):
         p.close()
         return b
 
-    e2e_step()
-    e2e_steps = min(args.steps, 5)
+    e2e_steps = 0 if args.skip_extras else min(args.steps, 5)
+    h2d = e2e_step() if e2e_steps else 0
     t0 = time.perf_counter()
-    h2d = 0
     for _ in range(e2e_steps):
         h2d = e2e_step()
     e2e_s = time.perf_counter() - t0
-    e2e = samples * e2e_steps * world / e2e_s
+    e2e = samples * e2e_steps * world / e2e_s if e2e_steps else None
     per_step_launches = sum(v[1] for v in prof.values())
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32+f64+int64", "data": "synthetic (SplitMix64(3) requests)",
+           "config": {"workload": f"uneven mixed batch: {len(reqs)} SplitMix64(3) requests, versions 26.1/26.2/26.3, "
+                                  "Overworld:Nether:End 6:2:2, square side log-uniform in [16,512) quart cells, origin "
+                                  "uniform in [-30000,30000] blocks, y=64, ENGINE tie rule; one persistent launch "
+                                  "(CUDA graph) vs one plain launch pair per request",
+                      "requests": len(reqs), "samples_per_step": samples, "tile_shape": plan.shape,
+                      "autotune_ms": round(tuned_ms, 3), "l2": f"output {samples/1e6:.0f} MB per step > L2",
+                      "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+           "plain": {"value": samples * world / (plain_ms * 1e-3), "ms_per_step": plain_ms,
+                     "launches_per_step": 2 * len(reqs), "identical_output": same},
+           "batched_over_plain": (samples / (ms_max / args.steps)) / (samples / plain_ms),
+           "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(samples),
+                   "steps": e2e_steps, "call": "Plan(requests) + plan_run(host buffer) + plan_free per step"},
+           "gpu_launches": int(graph_launches) + args.steps * per_step_launches}
     if rank == 0:
         out["kernels"] = {k: {"ms_total": round(v[0], 4), "launches": v[1], "avg_ms": round(v[0] / v[1], 5)}
                           for k, v in prof.items()}
@@ -452,7 +486,11 @@ def run_batch(args, rank, world, local_rank, mg, ge):
             achieved = ops / avg_s / 1e9
             out["roofline"] = {"kernel": "k_batch", "bound": "fp64", "achieved": round(achieved, 1),
                                "peak": peaks["fp64_add"], "unit": "Gop/s", "frac": round(achieved / peaks["fp64_add"], 4),
-                               "traffic": None, "work": f"{ops:.4g} FP64 ops per launch (lattice model)",
+                               "traffic": round(DRAM_BYTES_PER_UNIT["k_batch"] * samples),
+                               "traffic_note": "DRAM bytes per sample from the ncu capture of a 300-request launch "
+                                               "(profiles/k_batch_uneven_batch.md) x samples; a lower bound at full "
+                                               "size, where the output no longer fits L2",
+                               "work": f"{ops:.4g} FP64 ops per launch (lattice model)",
                                "peak_source": "measured in-run (FP64 add pipe microbenchmark)"}
         if not args.skip_extras:
             out["cpu_baseline"] = cpu_baseline_batch(reqs, args.cpu_sample_s)
@@ -564,7 +602,7 @@ def run_dims(args, rank, world, local_rank, mg, ge):
 
     dev = torch.device("cuda", local_rank)
     torch.cuda.set_device(dev)
-    seeds = splitmix64(2, 4096).view(np.int64)
+    seeds, origins = config3_inputs()
     gen = mg.Generator.open(ge.data_root(), "26.3")
     stream = torch.cuda.current_stream(dev)
     sh = stream.cuda_stream
@@ -573,7 +611,7 @@ def run_dims(args, rank, world, local_rank, mg, ge):
     with ClockSampler(local_rank) as clk:
         for dim in ("minecraft:the_nether", "minecraft:the_end"):
             w = gen.world(dim, "normal", 0)
-            plan = mg.Plan([(w, int(s), -32, -32, 64, 64, 16) for s in seeds])
+            plan = mg.Plan([(w, int(s), int(qx), int(qz), 64, 64, 16) for s, (qx, qz) in zip(seeds, origins)])
             d_out = torch.empty(plan.output_bytes, dtype=torch.uint8, device=dev)
             plan.autotune(d_out.data_ptr(), reps=1)
             for _ in range(args.warmup):
@@ -599,7 +637,8 @@ def run_dims(args, rank, world, local_rank, mg, ge):
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (SplitMix64(2) seeds)",
            "config": {"workload": "other dimensions 26.3: 4096 SplitMix64(2) seeds x 64x64 quart grid at y=64, "
-                                  "Nether and End, one batched launch per dimension", "per_dimension": res},
+                                  "corners SplitMix64(102) uniform in [-30000,30000) blocks, Nether and End, one "
+                                  "batched launch per dimension", "per_dimension": res},
            "kernels": kern, "gpu_launches": args.steps * 4}
     clocks = clk.summary()
     if clocks:
@@ -705,15 +744,15 @@ def run_reference(args, rank, world):
                               "Overworld:Nether:End 6:2:2, square side log-uniform in [16,512) quart cells, origin "
                               "uniform in [-30000,30000] blocks, y=64, ENGINE tie rule", "requests": len(reqs)}
     elif args.workload == "dims4096":
-        seeds = splitmix64(2, 4096).view(np.int64)
+        seeds, origins = config3_inputs()
         wn = O.World(ge.data_root(), "26.3", "the_nether")
         we = O.World(ge.data_root(), "26.3", "the_end")
         nfirst = 16
 
         def per_step():
-            for sd in seeds[:nfirst]:
-                wn.quart_grid(int(sd), -32, -32, 64, 64, 16, O.TIE_ENGINE, threads=cores)
-                we.quart_grid(int(sd), -32, -32, 64, 64, 16, O.TIE_ENGINE, threads=cores)
+            for sd, (qx, qz) in zip(seeds[:nfirst], origins[:nfirst]):
+                wn.quart_grid(int(sd), int(qx), int(qz), 64, 64, 16, O.TIE_ENGINE, threads=cores)
+                we.quart_grid(int(sd), int(qx), int(qz), 64, 64, 16, O.TIE_ENGINE, threads=cores)
 
         samples = nfirst * 2 * 64 * 64
         sample = f"first {nfirst} of the 4096 seeds, Nether and End 64x64 grids per step"

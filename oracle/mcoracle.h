@@ -15,7 +15,7 @@
  * Parity is pinned against the reference's golden vectors
  * (tests/vectors/<V>/ climate, noise and grid-hash tables, tests/unit/ref26{2,3}.txt) and, in the build
  * container, against the reference engine compiled from its own sources
- * (oracle/build_ref.sh).
+ * (oracle/build.py, build_reference).
  */
 #ifndef MCORACLE_H
 #define MCORACLE_H

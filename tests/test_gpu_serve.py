@@ -75,7 +75,7 @@ def test_alone_equals_mixed(env):
 def test_small_budget_evicts(env):
     """A budget of a few Overworld slots forces LRU eviction; every result is still exact."""
     mg, gens, worlds = env
-    srv = mg.Server(hbm_budget_bytes=4 * 48 * 320 * 16 // 12 + 64 * 320, max_inflight=2, max_batch=3)
+    srv = mg.Server(hbm_budget_bytes=4 * 48 * 352 * 16 // 12 + 64 * 352, max_inflight=2, max_batch=3)
     rng = np.random.default_rng(7)
     w = worlds[("26.3", "minecraft:overworld")]
     ow = O.World(ge.data_root(), "26.3", "overworld")
