@@ -74,7 +74,8 @@ MCGEN_API int mcgen_gb300_plan_new(const McGb300Request *reqs, int n, int tie_ru
 MCGEN_API void mcgen_gb300_plan_free(McGb300Plan *p);
 MCGEN_API long long mcgen_gb300_plan_output_bytes(const McGb300Plan *p);
 MCGEN_API long long mcgen_gb300_plan_output_offset(const McGb300Plan *p, int i);
-/* the tile shape in use: 0 (32 x 4), 1 (16 x 8), 2 (64 x 2), 3 (8 x 16) */
+/* the tile shape in use (cells x rows, resident CTAs per SM): 0 (32 x 4, 8), 1 (8 x 16, 4), 2 (8 x 16, 6),
+ * 3 (8 x 16, 8) */
 MCGEN_API int mcgen_gb300_plan_shape(const McGb300Plan *p);
 MCGEN_API int mcgen_gb300_plan_set_shape(McGb300Plan *p, int shape);
 /* bytes plan_new copied to the device (worlds, request and setup lists) */
@@ -109,6 +110,30 @@ MCGEN_API int mcgen_gb300_server_submit(McGb300Server *s, const McGb300Request *
 MCGEN_API int mcgen_gb300_server_wait(McGb300Server *s, long long ticket, int timeout_ms, double *latency_ms);
 MCGEN_API int mcgen_gb300_server_stats(McGb300Server *s, McGb300ServerStats *out);
 
+/* ---- biome seed search: which candidate seeds produce the observed biomes ----
+ * The reference's gb_search (crack/src/gpu_biomes/gpu_biomes.h:44-56, gpu_biomes.cu:245-278).  Candidates:
+ * MCGEN_SEEDS_LIST list[0..n), MCGEN_SEEDS_STRUCTURE base | i << 48 for i < 65536 (base: a 48-bit structure
+ * seed; n ignored), MCGEN_SEEDS_RANGE base + i for i < n.  Each candidate is checked against obs[0..nobs)
+ * in order and stops at the first observation it fails; reached[j] (nobs + 1 entries) counts candidates
+ * that passed exactly j observations.  Candidates passing all are written to found, sorted as unsigned, at
+ * most max_found (*n_found of them).  An observation (the reference's McgObs, engine/cuda/mc_gpu.cuh:47-54)
+ * is a quart cell, or with MCGEN_OBS_BLOCK in flags a block that BiomeManager's zoom resolves with the
+ * candidate's hashed seed, and the set of biome ids that satisfy it (mask bit id); flags' low byte is the
+ * End window half-width (12 in the game; mcgen_gb300_obs_end_radius gives the narrowest exact one).
+ * ties != 0: an Overworld/Nether observation is also met when any equal-fitness R-tree leaf's biome is in
+ * the mask (the game's choice between them is not deterministic).  *ms: device time of the search. */
+typedef struct McGb300Obs {
+    int32_t qx, qy, qz, flags;
+    uint64_t mask[2];
+} McGb300Obs;
+#define MCGEN_OBS_BLOCK 0x100
+enum { MCGEN_SEEDS_LIST = 0, MCGEN_SEEDS_STRUCTURE = 1, MCGEN_SEEDS_RANGE = 2 };
+MCGEN_API int mcgen_gb300_search(const McWorld *w, int kind, const int64_t *list, uint64_t base, uint64_t n,
+                                 const McGb300Obs *obs, int nobs, int ties, int64_t *found, uint32_t max_found,
+                                 uint32_t *n_found, uint64_t *reached, double *ms);
+/* End window half-width for an observation mask (engine/cuda/mc_gpu.cuh:640-652); -1 on bad arguments */
+MCGEN_API int mcgen_gb300_obs_end_radius(const McWorld *w, const uint64_t mask[2]);
+
 /* Allocation-free form of mcgen_gb300_seed_points_dev, for callers that cannot let a library allocate
  * device memory (their own memory arena, latency-critical loops, no allocation after set-up).  No
  * counterpart in the reference.  The per-seed noise lattices go to one fixed 16 MiB device array inside
@@ -138,8 +163,12 @@ MCGEN_API const char *mcgen_gb300_last_error(void);
  * inputs (quart coordinates, shifted and second-stack coordinates, tiny/huge values, sums landing on or
  * near integers and in (-1, 0), edge offsets) through both the fast split and the plain double arithmetic
  * of the reference; *bad_f / *bad_d count differing results of the float (26.3) and double (26.1/26.2)
- * branches.  Same seed, same inputs. */
+ * branches (the double branch also checks the fraction in units of 2^-52).  Same seed, same inputs. */
 MCGEN_API int mcgen_gb300_check_split(long long n, unsigned long long seed, long long *bad_f, long long *bad_d);
+/* Device self-check of the double branch's fixed-point octave (gradient sums and first lerp differences in
+ * units of 2^-52) against the plain double octave: n random (permutation, fractions) cases; *bad counts
+ * results that differ as doubles. */
+MCGEN_API int mcgen_gb300_check_octave(long long n, unsigned long long seed, long long *bad);
 
 /* Pipe microbenchmarks on the current device, in giga-operations per second:
  * 0 FP32 FMA, 1 FP64 FMA, 2 FP64 add, 3 int32 multiply-add, 4 double->int floor conversion,

@@ -90,6 +90,10 @@ _PROTOS = {
     "mcgen_gb300_profile_read": (C.c_int, [C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_double),
                                            C.POINTER(C.c_longlong)]),
     "mcgen_gb300_pipe_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+    "mcgen_gb300_check_octave": (C.c_int, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]),
+    "mcgen_gb300_search": (C.c_int, [_P, C.c_int, _P, C.c_uint64, C.c_uint64, _P, C.c_int, C.c_int, _P, C.c_uint32,
+                                     C.POINTER(C.c_uint32), _P, C.POINTER(C.c_double)]),
+    "mcgen_gb300_obs_end_radius": (C.c_int, [_P, _P]),
     "mcgen_gb300_check_split": (C.c_int, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong),
                                           C.POINTER(C.c_longlong)]),
 }
@@ -205,6 +209,13 @@ def check_split(n: int, seed: int = 1) -> tuple[int, int]:
     return bf.value, bd.value
 
 
+def check_octave(n: int, seed: int = 1) -> int:
+    """Mismatches of the double branch's fixed-point octave against the plain double octave."""
+    b = C.c_longlong()
+    _check(load().mcgen_gb300_check_octave(n, seed, C.byref(b)), "mcgen_gb300_check_octave")
+    return b.value
+
+
 def pipe_rate(pipe: str) -> float:
     """Measured throughput of one GPU pipe in giga-operations per second (see PIPES)."""
     g = C.c_double()
@@ -274,6 +285,23 @@ def _norm_seeds(seeds) -> McSeeds:
         return McSeeds(*[int(s) for s in seeds])
     s = int(seeds)
     return McSeeds(s, s, s, s)
+
+
+SEEDS_LIST, SEEDS_STRUCTURE, SEEDS_RANGE = 0, 1, 2
+OBS_BLOCK = 0x100
+# one search observation (McGb300Obs): quart or block cell, flags (OBS_BLOCK | End window half-width), mask
+OBS_DTYPE = np.dtype([("qx", "<i4"), ("qy", "<i4"), ("qz", "<i4"), ("flags", "<i4"), ("mask", "<u8", (2,))])
+
+
+def make_obs(rows, block: bool = False, rad: int = 12) -> np.ndarray:
+    """Observations from (x, y, z, [biome ids]) rows."""
+    a = np.zeros(len(rows), OBS_DTYPE)
+    for i, (x, y, z, ids) in enumerate(rows):
+        a[i]["qx"], a[i]["qy"], a[i]["qz"] = x, y, z
+        a[i]["flags"] = (OBS_BLOCK if block else 0) | rad
+        for b in ids:
+            a[i]["mask"][b >> 6] |= np.uint64(1) << np.uint64(b & 63)
+    return a
 
 
 class World:
@@ -356,6 +384,31 @@ class World:
         _check(load().mcgen_gb300_seed_points(self._h, _ptr(seeds), len(seeds), _ptr(qxyz), len(qxyz), _ptr(out),
                                               _ptr(tg) if tg is not None else None), "mcgen_gb300_seed_points")
         return (out, tg) if want_targets else out
+
+    def search(self, obs: np.ndarray, kind: int = None, base: int = 0, n: int = 0, seeds=None, ties: bool = True,
+               max_found: int = 1 << 16):
+        """Biome seed search (mcgen_gb300_search): (found seeds sorted as unsigned, reached[nobs + 1], device ms).
+        obs: an OBS_DTYPE array; kind: SEEDS_LIST (seeds), SEEDS_STRUCTURE (base, 2^16 candidates) or
+        SEEDS_RANGE (base + i, i < n)."""
+        obs = np.ascontiguousarray(obs, OBS_DTYPE)
+        if kind is None:
+            kind = SEEDS_LIST if seeds is not None else SEEDS_STRUCTURE
+        lst = None
+        if kind == SEEDS_LIST:
+            lst = np.ascontiguousarray(seeds, np.int64)
+            n = lst.size
+        reached = np.zeros(len(obs) + 1, np.uint64)
+        found = np.zeros(max(1, max_found), np.int64)
+        nf, ms = C.c_uint32(), C.c_double()
+        _check(load().mcgen_gb300_search(self._h, kind, _ptr(lst) if lst is not None else None,
+                                         C.c_uint64(base & (2**64 - 1)), C.c_uint64(n), obs.ctypes.data, len(obs),
+                                         int(ties), _ptr(found), max_found, C.byref(nf), reached.ctypes.data,
+                                         C.byref(ms)), "mcgen_gb300_search")
+        return found[:nf.value].copy(), reached, ms.value
+
+    def end_radius(self, mask) -> int:
+        m = np.ascontiguousarray(mask, np.uint64)
+        return load().mcgen_gb300_obs_end_radius(self._h, m.ctypes.data)
 
     # device-pointer forms: integer addresses of device buffers and a cudaStream_t handle
     def seed_points_dev(self, d_seeds: int, ns: int, d_qxyz: int, np_: int, d_out: int, d_targets: int = 0,

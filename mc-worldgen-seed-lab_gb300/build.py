@@ -21,7 +21,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
                   "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math,-O2", "-I", CSRC, "-I", INCLUDE]
-SOURCES = ["kernels.cu", "pipes.cu", "api.cpp", "world.cpp", "prof.cpp", "noalloc.cu", "fused.cu", "selfcheck.cu", "batch.cu", "plan.cpp", "server.cpp"]
+SOURCES = ["kernels.cu", "pipes.cu", "api.cpp", "world.cpp", "prof.cpp", "noalloc.cu", "fused.cu", "selfcheck.cu", "batch.cu",
+           "plan.cpp", "server.cpp", "search.cu"]
 
 
 def nvcc() -> str:

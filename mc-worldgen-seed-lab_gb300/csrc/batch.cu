@@ -130,13 +130,20 @@ __global__ void __launch_bounds__(LNT) k_setup_list_end(const MgSetupEntry *__re
 }
 
 /* ---------------------------------------------------------------- the persistent batch kernel */
-struct BatchSmem {
-    MgSpline spline;
-    MgLattice lat[MG_MAX_TABLES];
+/* The lattices of an Overworld/Nether request and the End's scratch are never live in the same tile, so
+ * they share storage: 24.6 KB per CTA, which leaves the register budget as the occupancy limit. */
+struct BatchEnd {
     uint8_t endp[256];
-    uint8_t island[END_WIN * END_WIN]; /* 0: no island, else (float) size in sz[] */
+    uint8_t island[END_WIN * END_WIN]; /* 0: no island, else its size in isize[] */
     float isize[END_WIN * END_WIN];
     uint8_t cls[END_TC * END_TC];
+};
+struct BatchSmem {
+    MgSpline spline;
+    union {
+        MgLattice lat[MG_MAX_TABLES];
+        BatchEnd end;
+    };
     int tile, req, state, world;
 };
 
@@ -173,12 +180,12 @@ __device__ __forceinline__ void batch_end(const MgWorldDesc &W, BatchSmem &sm, c
         uint8_t isl = 0;
         float size = 0.0f;
         if (tx * tx + tz * tz > 4096LL) {
-            const double nv = simplex2(sm.endp, (double)tx, (double)tz, W.end_f2, W.end_g2);
+            const double nv = simplex2(sm.end.endp, (double)tx, (double)tz, W.end_f2, W.end_g2);
             isl = FM ? ((float)nv < -0.9f) : (nv < (double)-0.9f);
             if (isl) size = fmodf(fabsf((float)tx) * 3439.0f + fabsf((float)tz) * 147.0f, 13.0f) + 9.0f;
         }
-        sm.island[i] = isl;
-        sm.isize[i] = size;
+        sm.end.island[i] = isl;
+        sm.end.isize[i] = size;
     }
     __syncthreads();
     if (threadIdx.x < END_TC * END_TC) {
@@ -197,9 +204,9 @@ __device__ __forceinline__ void batch_end(const MgWorldDesc &W, BatchSmem &sm, c
             for (int dx = -12; dx <= 12; dx++)
                 for (int dz = -12; dz <= 12; dz++) {
                     const int wi = (ccz + dz - wz0) * END_WIN + (ccx + dx - wx0);
-                    if (!sm.island[wi]) continue;
+                    if (!sm.end.island[wi]) continue;
                     const float xd = (float)(ox - dx * 2), zd = (float)(oz - dz * 2);
-                    const float h = clampf(100.0f - (float)sqrt((double)(xd * xd + zd * zd)) * sm.isize[wi], -100.0f, 80.0f);
+                    const float h = clampf(100.0f - (float)sqrt((double)(xd * xd + zd * zd)) * sm.end.isize[wi], -100.0f, 80.0f);
                     best = best > h ? best : h;
                 }
             double e;
@@ -213,19 +220,21 @@ __device__ __forceinline__ void batch_end(const MgWorldDesc &W, BatchSmem &sm, c
             }
             cls = e > 0.25 ? 1 : (e >= -0.0625 ? 2 : (e < -0.21875 ? 3 : 4));
         }
-        sm.cls[threadIdx.x] = (uint8_t)cls;
+        sm.end.cls[threadIdx.x] = (uint8_t)cls;
     }
     __syncthreads();
     for (int i = threadIdx.x; i < 16 * END_TC * END_TC; i += blockDim.x) {
         const int qx = 4 * cx0 + i % (4 * END_TC), qz = 4 * cz0 + i / (4 * END_TC);
         const int ix = qx - R.qx0, iz = qz - R.qz0;
         if (ix < 0 || iz < 0 || ix >= R.nx || iz >= R.nz) continue;
-        out[R.out_off + (size_t)iz * R.nx + ix] = (uint8_t)W.end_ids[sm.cls[(i / (16 * END_TC)) * END_TC + (i % (4 * END_TC)) / 4]];
+        out[R.out_off + (size_t)iz * R.nx + ix] = (uint8_t)W.end_ids[sm.end.cls[(i / (16 * END_TC)) * END_TC + (i % (4 * END_TC)) / 4]];
     }
 }
 
-template <int TILE_W>
-__global__ void __launch_bounds__(BNT) k_batch(const MgWorldDesc *__restrict__ worlds, const MgTreeNode *const *__restrict__ trees,
+/* TILE_W: tile width in cells (tiles are 128 cells); MINB: resident CTAs per SM the register allocation
+ * is sized for (4: 128 registers, 6: 80, 8: 64) */
+template <int TILE_W, int MINB>
+__global__ void __launch_bounds__(BNT, MINB) k_batch(const MgWorldDesc *__restrict__ worlds, const MgTreeNode *const *__restrict__ trees,
                                                const MgBatchReq *__restrict__ reqs, int nreq, long long ntiles,
                                                const MgLattice *__restrict__ pool, unsigned long long *__restrict__ counter,
                                                uint8_t *__restrict__ out) {
@@ -262,7 +271,7 @@ __global__ void __launch_bounds__(BNT) k_batch(const MgWorldDesc *__restrict__ w
         }
         if (new_state) {
             if (W.dim == MG_END) {
-                for (int i = threadIdx.x; i < 256; i += BNT) sm.endp[i] = pool[R.state].p[i];
+                for (int i = threadIdx.x; i < 256; i += BNT) sm.end.endp[i] = pool[R.state].p[i];
             } else {
                 const uint4 *a = reinterpret_cast<const uint4 *>(pool + R.state);
                 uint4 *b = reinterpret_cast<uint4 *>(sm.lat);
@@ -294,7 +303,10 @@ __global__ void __launch_bounds__(BNT) k_batch(const MgWorldDesc *__restrict__ w
 }
 
 /* ---------------------------------------------------------------- host side */
-const int kBatchTileWidths[BATCH_SHAPES] = {32, 16, 64, 8};
+/* tile shapes the autotuner chooses from: tile width, and the register budget (resident CTAs per SM: 8, 4,
+ * 6, 8) in k_batch's second template argument */
+const int kBatchTileWidths[BATCH_SHAPES] = {32, 8, 8, 8};
+static int g_resident[BATCH_SHAPES] = {0, 0, 0, 0}; /* CTAs per SM x SMs, per shape (batch_prepare) */
 
 long long batch_tiles(int dim, int qx0, int qz0, int nx, int nz, int shape) {
     if (dim == MG_END) {
@@ -322,36 +334,45 @@ int launch_setup_list(const MgWorldDesc *d_worlds, int dim, const MgSetupEntry *
     return (int)cudaGetLastError();
 }
 
-template <int TW>
-static int prepare_t() {
-    return (int)cudaFuncSetAttribute(k_batch<TW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BatchSmem));
-}
-/* kernel attributes (before any capture) and resident CTAs per SM */
-int batch_prepare(int *ctas_per_sm) {
-    int rc = prepare_t<32>();
-    if (!rc) rc = prepare_t<16>();
-    if (!rc) rc = prepare_t<64>();
-    if (!rc) rc = prepare_t<8>();
+template <int TW, int MB>
+static int prepare_t(int shape, int sms) {
+    int rc = (int)cudaFuncSetAttribute(k_batch<TW, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BatchSmem));
     int n = 0;
-    if (!rc) rc = (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<32>, BNT, sizeof(BatchSmem));
-    if (ctas_per_sm) *ctas_per_sm = n > 0 ? n : 1;
+    if (!rc) rc = (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<TW, MB>, BNT, sizeof(BatchSmem));
+    g_resident[shape] = (n > 0 ? n : 1) * sms;
+    return rc;
+}
+/* kernel attributes (before any capture) and resident CTAs per SM of shape 0 */
+int batch_prepare(int *ctas_per_sm) {
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int rc = prepare_t<32, 8>(0, sms);
+    if (!rc) rc = prepare_t<8, 4>(1, sms);
+    if (!rc) rc = prepare_t<8, 6>(2, sms);
+    if (!rc) rc = prepare_t<8, 8>(3, sms);
+    if (ctas_per_sm) *ctas_per_sm = g_resident[0] / (sms > 0 ? sms : 1);
     return rc;
 }
 
+/* ctas: upper bound on the persistent grid (0: every resident CTA of the shape) */
 int launch_batch(const MgWorldDesc *d_worlds, const MgTreeNode *const *d_trees, const MgBatchReq *d_reqs, int nreq,
                  long long ntiles, const MgLattice *d_pool, unsigned long long *d_counter, uint8_t *d_out, int ctas,
                  int shape, cudaStream_t st) {
     if (ntiles <= 0) return 0;
+    if (shape < 0 || shape >= BATCH_SHAPES || g_resident[shape] <= 0) return (int)cudaErrorInvalidValue;
     cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st);
     if (e) return (int)e;
-    if ((long long)ctas > ntiles) ctas = (int)ntiles;
+    int grid = g_resident[shape];
+    if (ctas > 0 && ctas < grid) grid = ctas;
+    if ((long long)grid > ntiles) grid = (int)ntiles;
     ProfScope ps_(K_BATCH, st);
     const size_t sm = sizeof(BatchSmem);
     switch (shape) {
-    case 1: k_batch<16><<<ctas, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
-    case 2: k_batch<64><<<ctas, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
-    case 3: k_batch<8><<<ctas, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
-    default: k_batch<32><<<ctas, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
+    case 1: k_batch<8, 4><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
+    case 2: k_batch<8, 6><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
+    case 3: k_batch<8, 8><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
+    default: k_batch<32, 8><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
     }
     count_launch_external();
     return (int)cudaGetLastError();

@@ -25,14 +25,17 @@ typedef struct {
 
 #define BATCH_SHAPES 4
 namespace mg {
-/* tile widths of the four Overworld/Nether tile shapes (128 cells each) */
+/* tile widths of the four Overworld/Nether tile shapes (128 cells each; the shapes also differ in the
+ * register budget: 8, 4, 6 and 8 resident CTAs per SM) */
 extern const int kBatchTileWidths[BATCH_SHAPES];
 /* tiles of a request: 128 quart cells of shape `shape` (Overworld, Nether) or 8 x 8 chunks (End) */
 long long batch_tiles(int dim, int qx0, int qz0, int nx, int nz, int shape);
 /* lattices of a list of entries of one dimension; Overworld needs the prefix sums of lattices per entry */
 int launch_setup_list(const MgWorldDesc *d_worlds, int dim, const MgSetupEntry *d_ent, int n, const int *d_first,
                       long long total_lattices, MgLattice *d_pool, cudaStream_t st);
+/* kernel attributes and resident grid sizes; call before any stream capture */
 int batch_prepare(int *ctas_per_sm);
+/* ctas: upper bound on the persistent grid, 0 = every resident CTA of the shape */
 int launch_batch(const MgWorldDesc *d_worlds, const MgTreeNode *const *d_trees, const MgBatchReq *d_reqs, int nreq,
                  long long ntiles, const MgLattice *d_pool, unsigned long long *d_counter, uint8_t *d_out, int ctas,
                  int shape, cudaStream_t st);

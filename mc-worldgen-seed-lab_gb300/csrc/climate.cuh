@@ -124,8 +124,10 @@ __device__ __forceinline__ double simplex2(const uint8_t *__restrict__ p, double
     return 70.0 * n;
 }
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return v < lo ? lo : (v < hi ? v : hi); }
-/* EndIslandDensityFunction.getHeightValue at (sx, sz) = (block / 8) */
-inline __device__ float end_height(const uint8_t *__restrict__ p, bool fm, int sx, int sz, double F2, double G2) {
+/* EndIslandDensityFunction.getHeightValue at (sx, sz) = (block / 8); rad: half-width of the island window in
+ * chunk cells (12 in the game; the seed search may narrow it, engine/cuda/mc_gpu.cuh:600-626, 640-652) */
+inline __device__ float end_height(const uint8_t *__restrict__ p, bool fm, int sx, int sz, double F2, double G2,
+                                   int rad = 12) {
     int cx = sx / 2, cz = sz / 2, ox = sx % 2, oz = sz % 2;
     float best;
     if (!fm) {
@@ -133,8 +135,8 @@ inline __device__ float end_height(const uint8_t *__restrict__ p, bool fm, int s
         float len = (float)sqrt((double)(float)sq);
         best = clampf(100.0f - len * 8.0f, -100.0f, 80.0f);
     } else best = -100.0f;
-    for (int dx = -12; dx <= 12; dx++)
-        for (int dz = -12; dz <= 12; dz++) {
+    for (int dx = -rad; dx <= rad; dx++)
+        for (int dz = -rad; dz <= rad; dz++) {
             long long tx = (long long)cx + dx, tz = (long long)cz + dz;
             if (tx * tx + tz * tz <= 4096LL) continue;
             double nv = simplex2(p, (double)tx, (double)tz, F2, G2);
@@ -148,10 +150,11 @@ inline __device__ float end_height(const uint8_t *__restrict__ p, bool fm, int s
     return best;
 }
 /* TheEndBiomeSource class of chunk (cx, cz): 0 the_end, 1 highlands, 2 midlands, 3 small islands, 4 barrens */
-inline __device__ int end_chunk_class(const uint8_t *__restrict__ p, bool fm, int cx, int cz, double F2, double G2) {
+inline __device__ int end_chunk_class(const uint8_t *__restrict__ p, bool fm, int cx, int cz, double F2, double G2,
+                                      int rad = 12) {
     if ((long long)cx * cx + (long long)cz * cz <= 4096LL) return 0;
     int bx = (cx * 2 + 1) * 8, bz = (cz * 2 + 1) * 8;
-    float h = end_height(p, fm, bx / 8, bz / 8, F2, G2);
+    float h = end_height(p, fm, bx / 8, bz / 8, F2, G2, rad);
     double e;
     if (!fm) e = ((double)h - 8.0) / 128.0;
     else {

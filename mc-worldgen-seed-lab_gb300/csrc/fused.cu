@@ -22,6 +22,7 @@
 
 #include "climate.cuh"
 #include "launch.h"
+#include "search.cuh"
 #include "prof.h"
 
 namespace mg {
@@ -35,7 +36,8 @@ namespace mg {
 
 /* header of an offset-noise lattice, shared so that any thread can sample it */
 struct OffHdr {
-    double ox, oy, oz, fyd, fzd, gyd, gzd, uyd, uzd;
+    double ox, oy, oz, fyd, fzd, uyd, uzd;
+    int64_t Fy, Fz;
     int iy, iz;
     float fy, fz, uy, uz;
 };
@@ -55,7 +57,7 @@ struct FusedSmem {
 template <bool FM>
 __global__ void __launch_bounds__(FNT) k_ow_seed_climate(const __grid_constant__ MgWorldDesc W,
                                                          const int64_t *__restrict__ seeds, int ns,
-                                                         const int32_t *__restrict__ pts, int np,
+                                                         const int32_t *__restrict__ pts, int np, int pstride,
                                                          typename std::conditional<FM, float, double>::type *__restrict__ clim) {
     typedef typename std::conditional<FM, float, double>::type V;
     extern __shared__ uint4 smem_raw[];
@@ -124,7 +126,8 @@ __global__ void __launch_bounds__(FNT) k_ow_seed_climate(const __grid_constant__
             if (s0 + o % spc >= ns) continue;
             const OffHdr &oh = sm.hdr[o];
             const IlvPerm<FNT> perm{pbase, o};
-            double X = (double)pts[3 * (p0 + p)], Z = (double)pts[3 * (p0 + p) + 2];
+            const int32_t *pp = pts + (size_t)(s0 + o % spc) * pstride + 3 * (p0 + p);
+            double X = (double)pp[0], Z = (double)pp[2];
             if (ost) { X = X * MG_SECOND_STACK; Z = Z * MG_SECOND_STACK; }
             const double of = O.freq[olev];
             const int ok = O.fexp[olev];
@@ -140,12 +143,13 @@ __global__ void __launch_bounds__(FNT) k_ow_seed_climate(const __grid_constant__
             } else {
                 int ix, izz, iyy;
                 double fx, fzz, fyy;
-                split_dk(X, of, ok, oh.ox, ix, fx);
-                split_dk(Z, of, ok, oh.oz, izz, fzz);
-                sm.val[o][p] = (V)octave_y0<double>(perm, oh, ix, fx, izz, fzz);
-                split_dk(Z, of, ok, oh.ox, ix, fx);
-                split_dk(X, of, ok, oh.oy, iyy, fyy);
-                sm.valb[o][p] = (V)octave_z0<double>(perm, oh, ix, fx, iyy, fyy);
+                int64_t FX, FZ, FY;
+                split_dk(X, of, ok, oh.ox, ix, fx, FX);
+                split_dk(Z, of, ok, oh.oz, izz, fzz, FZ);
+                sm.val[o][p] = (V)octave_d_y0(perm, oh, ix, fx, FX, izz, fzz, FZ);
+                split_dk(Z, of, ok, oh.ox, ix, fx, FX);
+                split_dk(X, of, ok, oh.oy, iyy, fyy, FY);
+                sm.valb[o][p] = (V)octave_d_z0(perm, oh, ix, fx, FX, iyy, fyy, FY);
             }
         }
         __syncthreads();
@@ -153,7 +157,8 @@ __global__ void __launch_bounds__(FNT) k_ow_seed_climate(const __grid_constant__
         if (t < spc * FNPC) {
             const int cs = t / FNPC, p = t % FNPC;
             if (p < npc && s0 + cs < ns) {
-                const double X = (double)pts[3 * (p0 + p)], Z = (double)pts[3 * (p0 + p) + 2];
+                const int32_t *pp = pts + (size_t)(s0 + cs) * pstride + 3 * (p0 + p);
+                const double X = (double)pp[0], Z = (double)pp[2];
                 double x, z;
                 if (FM) {
                     float sa = 0.0f, sb = 0.0f;
@@ -197,9 +202,10 @@ __global__ void __launch_bounds__(FNT) k_ow_seed_climate(const __grid_constant__
                 } else {
                     int ix, izz;
                     double fx, fzz;
-                    split_dk(x, f, fk, ox, ix, fx);
-                    split_dk(z, f, fk, oz, izz, fzz);
-                    sm.val[t][p] = (V)octave_y0<double>(perm, h, ix, fx, izz, fzz);
+                    int64_t FX, FZ;
+                    split_dk(x, f, fk, ox, ix, fx, FX);
+                    split_dk(z, f, fk, oz, izz, fzz, FZ);
+                    sm.val[t][p] = (V)octave_d_y0(perm, h, ix, fx, FX, izz, fzz, FZ);
                 }
             }
         }
@@ -236,7 +242,7 @@ template <bool FM>
 __global__ void __launch_bounds__(128) k_ow_finish_tree(const __grid_constant__ MgWorldDesc W,
                                                         const MgTreeNode *__restrict__ tree,
                                                         const typename std::conditional<FM, float, double>::type *__restrict__ clim,
-                                                        int ns, const int32_t *__restrict__ pts, int np,
+                                                        int ns, const int32_t *__restrict__ pts, int np, int pstride,
                                                         uint8_t *__restrict__ out, int32_t *__restrict__ targets) {
     __shared__ MgSpline S;
     {
@@ -248,7 +254,7 @@ __global__ void __launch_bounds__(128) k_ow_finish_tree(const __grid_constant__ 
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= (long long)ns * np) return;
     const int p = (int)(g % np);
-    const int by = pts[3 * p + 1] * 4;
+    const int by = pts[(size_t)(g / np) * pstride + 3 * p + 1] * 4;
     int32_t tg[6];
     const auto *v = clim + (size_t)g * 5;
     if (FM) climate_finish_f(W, S, (float)v[0], (float)v[1], (float)v[2], (float)v[3], (float)v[4], by, tg);
@@ -258,6 +264,72 @@ __global__ void __launch_bounds__(128) k_ow_finish_tree(const __grid_constant__ 
     out[g] = tree[leaf].biome;
     if (targets)
         for (int k = 0; k < 6; k++) targets[g * 6 + k] = tg[k];
+}
+
+/* Seed search, Overworld, first observation of every candidate: finish the climate at the candidate's own
+ * cell, check the observation (mask, or any equal-fitness leaf in ties mode); passing candidates are
+ * appended to `surv`, failures counted into *fail (engine/cuda/mc_gpu.cuh:476-493, stage [0]). */
+template <bool FM>
+__global__ void __launch_bounds__(128) k_ow_search_first(const __grid_constant__ MgWorldDesc W,
+                                                         const MgTreeNode *__restrict__ tree,
+                                                         const typename std::conditional<FM, float, double>::type *__restrict__ clim,
+                                                         int ns, const int64_t *__restrict__ seeds,
+                                                         const int32_t *__restrict__ pts, MgObs o, int ties,
+                                                         int64_t *__restrict__ surv, unsigned *__restrict__ nsurv,
+                                                         unsigned long long *__restrict__ fail) {
+    __shared__ MgSpline S;
+    {
+        const uint4 *c = reinterpret_cast<const uint4 *>(&W.spline);
+        uint4 *d = reinterpret_cast<uint4 *>(&S);
+        for (int i = threadIdx.x; i < (int)(sizeof(MgSpline) / 16); i += blockDim.x) d[i] = c[i];
+    }
+    __syncthreads();
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    bool failed = false;
+    if (g < ns) {
+        int32_t tg[6];
+        const auto *v = clim + (size_t)g * 5;
+        const int by = pts[3 * g + 1] * 4;
+        if (FM) climate_finish_f(W, S, (float)v[0], (float)v[1], (float)v[2], (float)v[3], (float)v[4], by, tg);
+        else climate_finish_d(W, S, (double)v[0], (double)v[1], (double)v[2], (double)v[3], (double)v[4], by, tg);
+        if (obs_accept(o, tree, tg, ties != 0)) surv[atomicAdd(nsurv, 1u)] = seeds[g];
+        else failed = true;
+    }
+    const int nf = __syncthreads_count(failed);
+    if (threadIdx.x == 0 && nf) atomicAdd(fail, (unsigned long long)nf);
+}
+
+template <bool FM>
+static int search_first_t(const MgWorldDesc &W, const MgTreeNode *tree, const int64_t *seeds, int ns, const int32_t *pts,
+                          const MgObs &o, int ties, void *scratch, int64_t *surv, unsigned *nsurv,
+                          unsigned long long *fail, cudaStream_t st) {
+    typedef typename std::conditional<FM, float, double>::type V;
+    const size_t sm = sizeof(FusedSmem<V>);
+    cudaError_t e = cudaFuncSetAttribute(k_ow_seed_climate<FM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e) return (int)e;
+    const int spc = FNT / W.ntables;
+    V *clim = (V *)scratch;
+    {
+        ProfScope ps_(K_OW_SEED_CLIMATE, st);
+        k_ow_seed_climate<FM><<<(unsigned)((ns + spc - 1) / spc), FNT, sm, st>>>(W, seeds, ns, pts, 1, 3, clim);
+    }
+    count_launch_external();
+    {
+        ProfScope ps_(K_SEARCH_FIRST, st);
+        k_ow_search_first<FM><<<(unsigned)((ns + 127) / 128), 128, 0, st>>>(W, tree, clim, ns, seeds, pts, o, ties, surv,
+                                                                             nsurv, fail);
+    }
+    count_launch_external();
+    return 0;
+}
+
+int launch_ow_search_first(const MgWorldDesc &W, const MgTreeNode *tree, const int64_t *seeds, int ns, const int32_t *pts,
+                           const MgObs &o, int ties, void *scratch, int64_t *surv, unsigned *nsurv,
+                           unsigned long long *fail, cudaStream_t st) {
+    if (ns <= 0) return 0;
+    int rc = W.fmode ? search_first_t<true>(W, tree, seeds, ns, pts, o, ties, scratch, surv, nsurv, fail, st)
+                     : search_first_t<false>(W, tree, seeds, ns, pts, o, ties, scratch, surv, nsurv, fail, st);
+    return rc ? rc : (int)cudaGetLastError();
 }
 
 bool fused_supported(const MgWorldDesc &W) {
@@ -280,13 +352,13 @@ static int fused_t(const MgWorldDesc &W, const MgTreeNode *tree, const int64_t *
     V *clim = (V *)scratch;
     {
         ProfScope ps_(K_OW_SEED_CLIMATE, st);
-        k_ow_seed_climate<FM><<<(unsigned)((ns + spc - 1) / spc), FNT, sm, st>>>(W, seeds, ns, pts, np, clim);
+        k_ow_seed_climate<FM><<<(unsigned)((ns + spc - 1) / spc), FNT, sm, st>>>(W, seeds, ns, pts, np, 0, clim);
     }
     count_launch_external();
     const long long n = (long long)ns * np;
     {
         ProfScope ps_(K_OW_FINISH_TREE, st);
-        k_ow_finish_tree<FM><<<(unsigned)((n + 127) / 128), 128, 0, st>>>(W, tree, clim, ns, pts, np, out, tg);
+        k_ow_finish_tree<FM><<<(unsigned)((n + 127) / 128), 128, 0, st>>>(W, tree, clim, ns, pts, np, 0, out, tg);
     }
     count_launch_external();
     return 0;

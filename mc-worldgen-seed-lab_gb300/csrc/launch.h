@@ -27,6 +27,12 @@ size_t fused_scratch_bytes(const MgWorldDesc &W, long long samples);
 int launch_ow_seed_points(const MgWorldDesc &W, const MgTreeNode *tree, const int64_t *seeds, int ns, const int32_t *pts,
                           int np, uint8_t *out, int32_t *targets, void *scratch, cudaStream_t st);
 
+/* seed search, Overworld, first observation (one quart cell per candidate at pts[3i..3i+2]): candidates
+ * that pass go to surv (count *nsurv), failures are added to *fail.  Scratch: fused_scratch_bytes(W, ns). */
+int launch_ow_search_first(const MgWorldDesc &W, const MgTreeNode *tree, const int64_t *seeds, int ns, const int32_t *pts,
+                           const MgObs &o, int ties, void *scratch, int64_t *surv, unsigned *nsurv,
+                           unsigned long long *fail, cudaStream_t st);
+
 /* one seed's quart grid.  Scratch: chain_scratch_bytes(nx*nz) for GRID_CHAIN; for the End,
  * (nx/4 + 2) * (nz/4 + 2) bytes of chunk classes. */
 size_t chain_scratch_bytes(long long ncells);

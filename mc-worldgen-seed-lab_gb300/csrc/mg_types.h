@@ -9,7 +9,7 @@
 
 #define MG_MAX_OCT 12        /* octaves per NormalNoise stack (continentalness has 9) */
 #define MG_OW_NOISES 6       /* offset (shift), temperature, vegetation, continentalness, erosion, ridge */
-#define MG_MAX_TABLES 64     /* lattices per seed: Overworld 46, Nether 8, End 1 */
+#define MG_MAX_TABLES 48     /* lattices per seed: Overworld 46, Nether 8, End 1 */
 #define MG_SPL_MP 128        /* offset-spline multipoint nodes (26.x: 53) */
 #define MG_SPL_PTS 512       /* offset-spline points (26.x: 253) */
 #define MG_SPL_CONST 512     /* offset-spline constant leaves (26.x: 201) */
@@ -83,17 +83,28 @@ typedef struct {
 } MgWorldDesc;
 
 /* One Perlin octave of one seed: offsets, the lattice split of the y and z offsets (what a zero input
- * coordinate uses: fraction, fraction - 1 and smoothstep of the fraction), and the permutation.
+ * coordinate uses: fraction and smoothstep of the fraction, and the fraction as a multiple of 2^-52 for
+ * the double branch's exact fixed-point gradient sums), and the permutation.
  * 352 bytes, 16-byte aligned; the 96-byte header precedes the permutation. */
 typedef struct __attribute__((aligned(16))) {
     double ox, oy, oz;
     double fyd, fzd;   /* oy - floor(oy), oz - floor(oz) (double branch) */
-    double gyd, gzd;   /* fyd - 1.0, fzd - 1.0 */
     double uyd, uzd;   /* smoothstep(fyd), smoothstep(fzd) */
+    int64_t Fy, Fz;    /* fyd, fzd in units of 2^-52, or -1 when not a multiple of 2^-52 */
     int32_t iy, iz;    /* floor(oy), floor(oz) */
     float fy, fz;      /* (float)fyd, (float)fzd (float branch) */
     float uy, uz;      /* smoothstep(fy), smoothstep(fz) in float */
     uint8_t p[256];
 } MgLattice;
+
+/* One seed-search observation (the reference's McgObs, engine/cuda/mc_gpu.cuh:47-54): a quart cell, or a
+ * block resolved through BiomeManager's zoom when flags has MG_OBS_BLOCK; flags' low byte is the End window
+ * half-width; the biomes that satisfy it as a 128-bit mask.  32 bytes. */
+typedef struct {
+    int32_t qx, qy, qz, flags;
+    uint64_t mask[2];
+} MgObs;
+#define MG_OBS_BLOCK 0x100
+#define MG_MAX_OBS 64
 
 #endif

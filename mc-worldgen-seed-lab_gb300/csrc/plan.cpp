@@ -131,9 +131,22 @@ MCGEN_API int mcgen_gb300_plan_new(const McGb300Request *reqs, int n, int tie_ru
         off += p->cells[(size_t)i];
     }
     p->out_bytes = off;
+    /* processing order: requests grouped by world, heaviest code path first (Overworld double branch, then
+     * float, Nether, End), so that the CTAs resident at any time run the same code (the kernel holds every
+     * dimension and branch; mixing them thrashes the instruction cache) and the light tiles come last */
+    std::vector<int> order((size_t)n);
+    for (int i = 0; i < n; i++) order[(size_t)i] = i;
+    auto weight = [&](int i) {
+        const MgWorldDesc &W = worlds[(size_t)widx[reqs[i].world]]->desc;
+        return W.dim * 2 + (W.fmode ? 1 : 0);
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        const int wa = weight(a), wb = weight(b);
+        return wa != wb ? wa < wb : widx[reqs[a].world] < widx[reqs[b].world];
+    });
     for (int s = 0; s < BATCH_SHAPES; s++) {
         long long tiles = 0;
-        for (int i = 0; i < n; i++) {
+        for (int i : order) {
             const McGb300Request &r = reqs[i];
             const int wi = widx[r.world];
             MgBatchReq b;
@@ -168,16 +181,12 @@ MCGEN_API int mcgen_gb300_plan_new(const McGb300Request *reqs, int n, int tie_ru
     up((void **)&p->d_first, first.data(), sizeof(int) * first.size());
     if (!e && pool) e = cudaMalloc(&p->d_pool, sizeof(MgLattice) * (size_t)pool);
     if (!e) e = cudaMalloc(&p->d_counter, sizeof(unsigned long long));
-    int cps = 1;
-    if (!e) e = (cudaError_t)mg::batch_prepare(&cps);
+    if (!e) e = (cudaError_t)mg::batch_prepare(nullptr);
     if (e) {
         free_plan(p);
         return cuda_rc(e);
     }
-    int dev = 0, sms = 1;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    p->ctas = sms * cps;
+    p->ctas = 0; /* each tile shape runs its own resident grid */
     *out = p;
     return MCGEN_OK;
 }

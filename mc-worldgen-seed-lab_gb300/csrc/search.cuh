@@ -1,0 +1,112 @@
+/* search.cuh -- device pieces of the biome seed search (crack/src/gpu_biomes/gpu_biomes.cu k_search,
+ * engine/cuda/mc_gpu.cuh:47-194): per-candidate BiomeManager seed (SHA-256), observation cells, biome
+ * masks and the equal-fitness leaf set used by the ties mode. */
+#ifndef MG_SEARCH_CUH
+#define MG_SEARCH_CUH
+
+#include "climate.cuh"
+
+namespace mg {
+
+/* FIPS 180-4 round constants */
+static __constant__ uint32_t kSha256K[64] = {
+    0x428a2f98, 0x71374491, 0xb5c0fbcf, 0xe9b5dba5, 0x3956c25b, 0x59f111f1, 0x923f82a4, 0xab1c5ed5,
+    0xd807aa98, 0x12835b01, 0x243185be, 0x550c7dc3, 0x72be5d74, 0x80deb1fe, 0x9bdc06a7, 0xc19bf174,
+    0xe49b69c1, 0xefbe4786, 0x0fc19dc6, 0x240ca1cc, 0x2de92c6f, 0x4a7484aa, 0x5cb0a9dc, 0x76f988da,
+    0x983e5152, 0xa831c66d, 0xb00327c8, 0xbf597fc7, 0xc6e00bf3, 0xd5a79147, 0x06ca6351, 0x14292967,
+    0x27b70a85, 0x2e1b2138, 0x4d2c6dfc, 0x53380d13, 0x650a7354, 0x766a0abb, 0x81c2c92e, 0x92722c85,
+    0xa2bfe8a1, 0xa81a664b, 0xc24b8b70, 0xc76c51a3, 0xd192e819, 0xd6990624, 0xf40e3585, 0x106aa070,
+    0x19a4c116, 0x1e376c08, 0x2748774c, 0x34b0bcb5, 0x391c0cb3, 0x4ed8aa4a, 0x5b9cca4f, 0x682e6ff3,
+    0x748f82ee, 0x78a5636f, 0x84c87814, 0x8cc70208, 0x90befffa, 0xa4506ceb, 0xbef9a3f7, 0xc67178f2};
+
+__device__ __forceinline__ uint32_t ror32(uint32_t x, int n) { return __funnelshift_r(x, x, n); }
+
+/* BiomeManager.obfuscateSeed: the first 8 bytes of SHA-256 over the seed's 8 little-endian bytes, read as
+ * a little-endian long (libmcgen/src/world.c:117-152).  One 64-byte block; the message schedule is kept
+ * as a 16-word ring. */
+__device__ __forceinline__ int64_t hashed_seed(int64_t seed) {
+    const uint64_t u = (uint64_t)seed;
+    uint32_t w[16];
+    w[0] = __byte_perm((uint32_t)u, 0, 0x0123);
+    w[1] = __byte_perm((uint32_t)(u >> 32), 0, 0x0123);
+    w[2] = 0x80000000u;
+#pragma unroll
+    for (int i = 3; i < 15; i++) w[i] = 0;
+    w[15] = 64;
+    uint32_t a = 0x6a09e667, b = 0xbb67ae85, c = 0x3c6ef372, d = 0xa54ff53a;
+    uint32_t e = 0x510e527f, f = 0x9b05688c, g = 0x1f83d9ab, h = 0x5be0cd19;
+#pragma unroll
+    for (int i = 0; i < 64; i++) {
+        uint32_t wi;
+        if (i < 16) {
+            wi = w[i];
+        } else {
+            const uint32_t w15 = w[(i - 15) & 15], w2 = w[(i - 2) & 15];
+            wi = w[i & 15] + (ror32(w15, 7) ^ ror32(w15, 18) ^ (w15 >> 3)) + w[(i - 7) & 15] +
+                 (ror32(w2, 17) ^ ror32(w2, 19) ^ (w2 >> 10));
+            w[i & 15] = wi;
+        }
+        const uint32_t t1 = h + (ror32(e, 6) ^ ror32(e, 11) ^ ror32(e, 25)) + ((e & f) ^ (~e & g)) + kSha256K[i] + wi;
+        const uint32_t t2 = (ror32(a, 2) ^ ror32(a, 13) ^ ror32(a, 22)) + ((a & b) ^ (a & c) ^ (b & c));
+        h = g; g = f; f = e; e = d + t1;
+        d = c; c = b; b = a; a = t1 + t2;
+    }
+    const uint32_t h0 = 0x6a09e667u + a, h1 = 0xbb67ae85u + b;
+    /* digest bytes 0..7 are h0, h1 big-endian; as a little-endian long */
+    return (int64_t)(((uint64_t)__byte_perm(h1, 0, 0x0123) << 32) | __byte_perm(h0, 0, 0x0123));
+}
+
+__device__ __forceinline__ bool obs_in(const MgObs &o, int b) { return (o.mask[b >> 6] >> (b & 63)) & 1ULL; }
+
+/* the observation's quart cell for this seed (engine/cuda/mc_gpu.cuh:120-124); the hashed seed is
+ * formed once per seed, at the first block observation */
+__device__ __forceinline__ void obs_cell(const MgObs &o, int64_t seed, int64_t &hs, bool &have, int &qx, int &qy, int &qz) {
+    if (!(o.flags & MG_OBS_BLOCK)) { qx = o.qx; qy = o.qy; qz = o.qz; return; }
+    if (!have) { hs = hashed_seed(seed); have = true; }
+    zoom_cell(hs, o.qx, o.qy, o.qz, qx, qy, qz);
+}
+
+/* biomes of every leaf at the minimum fitness (engine/cuda/mc_gpu.cuh:166-187): a child is visited iff its
+ * box distance is <= the best leaf distance so far; a closer leaf resets the set */
+__device__ __forceinline__ void tree_ties(const MgTreeNode *__restrict__ T, const int32_t *t, uint64_t m[2]) {
+    int stk_node[10], stk_next[10], sp = 1;
+    uint64_t best = ~0ULL;
+    m[0] = m[1] = 0;
+    stk_node[0] = 0;
+    stk_next[0] = 0;
+    while (sp > 0) {
+        const int nd = stk_node[sp - 1], c = stk_next[sp - 1];
+        if (c >= T[nd].count) { sp--; continue; }
+        stk_next[sp - 1] = c + 1;
+        const int ci = T[nd].first + c;
+        const uint64_t cd = node_dist(T[ci], t);
+        if (cd > best) continue;
+        if (T[ci].count == 0) {
+            if (cd < best) { best = cd; m[0] = m[1] = 0; }
+            const int b = T[ci].biome;
+            m[b >> 6] |= 1ULL << (b & 63);
+        } else if (sp < 10) {
+            stk_node[sp] = ci; stk_next[sp] = 0; sp++;
+        }
+    }
+}
+
+/* observation met by a target: its ENGINE biome is in the mask, or (ties) any equal-fitness leaf's is */
+__device__ __forceinline__ bool obs_accept(const MgObs &o, const MgTreeNode *__restrict__ T, const int32_t *tg, bool ties) {
+    uint64_t d;
+    if (obs_in(o, T[tree_search(T, tg, -1, d)].biome)) return true;
+    if (!ties) return false;
+    uint64_t m[2];
+    tree_ties(T, tg, m);
+    return ((m[0] & o.mask[0]) | (m[1] & o.mask[1])) != 0;
+}
+
+/* candidate i of a source: 0 list, 1 structure seed base | i << 48, 2 base + i */
+__device__ __forceinline__ int64_t search_seed(int kind, const int64_t *__restrict__ list, uint64_t base, uint64_t i) {
+    if (kind == 0) return list[i];
+    if (kind == 1) return (int64_t)(base | (i << 48));
+    return (int64_t)(base + i);
+}
+
+}  // namespace mg
+#endif

@@ -3,7 +3,8 @@
  * on generated inputs that cover the ranges the biome path sees and the edges of the fast path:
  * integer quart coordinates, coordinates plus a float shift, their products with the second-stack factor,
  * tiny and huge values, values whose sum with the offset lands near an integer, in (-1, 0) or on 0, and
- * offsets at 0, near 256 and on integers. */
+ * offsets at 0, near 256 and on integers.  Also: the double branch's fixed-point octave (octave_dfix)
+ * against the plain double octave on random permutations and fractions. */
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -59,15 +60,67 @@ __global__ void k_check_split(long long n, uint64_t seed, unsigned long long *ba
         split_f_plain(x * f, off, ib, fb);
         bf += (ia != ib) || (__float_as_uint(fa) != __float_as_uint(fb));
         double da, db;
-        split_dk(x, f, k, off, ia, da);
+        int64_t F;
+        split_dk(x, f, k, off, ia, da, F);
         split_d_plain(x * f, off, ib, db);
-        bd += (ia != ib) || (__double_as_longlong(da) != __double_as_longlong(db));
+        bd += (ia != ib) || (__double_as_longlong(da) != __double_as_longlong(db)) || F != fixed52(db);
     }
     if (bf) atomicAdd(&bad[0], bf);
     if (bd) atomicAdd(&bad[1], bd);
 }
 
+/* fixed-point double octave vs the plain double octave: random permutation per thread, fractions that are
+ * multiples of 2^-52 (any, near 0, near 1, on small dyadic grids); equal as doubles (the sign of an exact
+ * zero may differ, and is never observed downstream) */
+__global__ void k_check_octave(long long n, uint64_t seed, unsigned long long *bad) {
+    __shared__ uint8_t perm[128][256];
+    uint8_t *P = perm[threadIdx.x];
+    uint64_t r = mix64(seed ^ (0xC0FFEEULL + blockIdx.x * 977ULL + threadIdx.x));
+    for (int i = 0; i < 256; i++) P[i] = (uint8_t)i;
+    for (int i = 255; i > 0; i--) {
+        r = mix64(r);
+        const int j = (int)(r % (uint64_t)(i + 1));
+        const uint8_t t = P[i]; P[i] = P[j]; P[j] = t;
+    }
+    const PlainPerm pp{P};
+    unsigned long long b = 0;
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (long long)gridDim.x * blockDim.x) {
+        int64_t F[3];
+        for (int c = 0; c < 3; c++) {
+            r = mix64(r ^ (uint64_t)g);
+            switch (r >> 61) {
+            case 0: F[c] = 0; break;
+            case 1: F[c] = (int64_t)((r >> 8) & 0xFFF); break;                          /* near 0 */
+            case 2: F[c] = (1LL << 52) - 1 - (int64_t)((r >> 8) & 0xFFF); break;        /* near 1 */
+            case 3: F[c] = (int64_t)(((r >> 8) & 0xFF) << 44); break;                   /* dyadic grid */
+            default: F[c] = (int64_t)((r >> 8) & ((1ULL << 52) - 1)); break;
+            }
+        }
+        const int ix = (int)(r & 255) - 128, iy = (int)((r >> 8) & 255), iz = (int)((r >> 16) & 1023) - 512;
+        const double fx = (double)F[0] * 0x1.0p-52, fy = (double)F[1] * 0x1.0p-52, fz = (double)F[2] * 0x1.0p-52;
+        const double v = fade<double>(fy), w = fade<double>(fz);
+        const double a = octave_dfix(pp, ix, fx, F[0], iy, F[1], v, iz, F[2], w);
+        const double c = octave_q<double>(pp, ix, fx, iy, fy, fy - 1.0, v, iz, fz, fz - 1.0, w);
+        b += !(a == c);
+    }
+    if (b) atomicAdd(bad, b);
+}
+
 }  // namespace
+
+extern "C" MCGEN_API int mcgen_gb300_check_octave(long long n, unsigned long long seed, long long *bad) {
+    if (n < 0 || !bad) return MCGEN_E_ARG;
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, sizeof(unsigned long long)) != cudaSuccess) return MCGEN_E_NOMEM;
+    cudaMemset(d, 0, sizeof(unsigned long long));
+    k_check_octave<<<152 * 2, 128>>>(n, seed, d);
+    unsigned long long h = 0;
+    cudaError_t e = cudaMemcpy(&h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return MCGEN_E_INTERNAL;
+    *bad = (long long)h;
+    return MCGEN_OK;
+}
 
 extern "C" MCGEN_API int mcgen_gb300_check_split(long long n, unsigned long long seed, long long *bad_f, long long *bad_d) {
     if (n < 0 || !bad_f || !bad_d) return MCGEN_E_ARG;

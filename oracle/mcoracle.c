@@ -1144,7 +1144,7 @@ static double simplex2(const Lattice *L, double xin, double yin) {
     return 70.0 * (n[0] + n[1] + n[2]);
 }
 static inline float clampf(float v, float lo, float hi) { return v < lo ? lo : (v < hi ? v : hi); }
-static float end_height(const Lattice *L, int fmode, i32 sx, i32 sz) {
+static float end_height(const Lattice *L, int fmode, i32 sx, i32 sz, int rad) {
     i32 cx = sx / 2, cz = sz / 2, ox = sx % 2, oz = sz % 2;
     float best;
     if (!fmode) {
@@ -1152,8 +1152,8 @@ static float end_height(const Lattice *L, int fmode, i32 sx, i32 sz) {
         float len = (float)sqrt((double)(float)sq);
         best = clampf(100.0f - len * 8.0f, -100.0f, 80.0f);
     } else best = -100.0f;
-    for (i32 dx = -12; dx <= 12; dx++)
-        for (i32 dz = -12; dz <= 12; dz++) {
+    for (i32 dx = -rad; dx <= rad; dx++)
+        for (i32 dz = -rad; dz <= rad; dz++) {
             i64 tx = (i64)cx + dx, tz = (i64)cz + dz;
             if (tx * tx + tz * tz <= 4096) continue;
             double nv = simplex2(L, (double)tx, (double)tz);
@@ -1166,8 +1166,10 @@ static float end_height(const Lattice *L, int fmode, i32 sx, i32 sz) {
         }
     return best;
 }
-static double end_erosion(const Lattice *L, int fmode, i32 bx, i32 bz) {
-    float h = end_height(L, fmode, bx / 8, bz / 8);
+/* rad: half-width of the island window in chunk cells, 12 in the game; the seed search may pass less
+ * (engine/cuda/mc_gpu.cuh:600-626, 640-652) */
+static double end_erosion(const Lattice *L, int fmode, i32 bx, i32 bz, int rad) {
+    float h = end_height(L, fmode, bx / 8, bz / 8, rad);
     if (!fmode) return ((double)h - 8.0) / 128.0;
     float dx = (float)(0 - bx), dz = (float)(0 - bz);
     float len = (float)sqrt((double)(dx * dx + 0.0f * 0.0f + dz * dz));
@@ -1175,14 +1177,15 @@ static double end_erosion(const Lattice *L, int fmode, i32 bx, i32 bz) {
     float o = (h - 8.0f) / 128.0f;
     return (double)(c > o ? c : o);
 }
-static int end_class(const Lattice *L, int fmode, i32 qx, i32 qz) {
+static int end_class_r(const Lattice *L, int fmode, i32 qx, i32 qz, int rad) {
     i32 cx = (qx * 4) >> 4, cz = (qz * 4) >> 4;
     if ((i64)cx * cx + (i64)cz * cz <= 4096) return 0;
-    double h = end_erosion(L, fmode, (cx * 2 + 1) * 8, (cz * 2 + 1) * 8);
+    double h = end_erosion(L, fmode, (cx * 2 + 1) * 8, (cz * 2 + 1) * 8, rad);
     if (h > 0.25) return 1;
     if (h >= -0.0625) return 2;
     return h < -0.21875 ? 3 : 4;
 }
+static int end_class(const Lattice *L, int fmode, i32 qx, i32 qz) { return end_class_r(L, fmode, qx, qz, 12); }
 
 /* ------------------------------------------------------------------------------------------------
  * Cells and tie rules
@@ -1261,6 +1264,23 @@ static double zoom_dist(i64 seed, int x, int y, int z, double dx, double dy, dou
     r = zoom_step(r, seed);
     double jz = zoom_jitter(r);
     return (dz + jz) * (dz + jz) + (dy + jy) * (dy + jy) + (dx + jx) * (dx + jx);
+}
+/* the quart cell BiomeManager.getBiome picks for block (x, y, z) */
+static void zoom_quart(i64 zseed, int x, int y, int z, int *qx, int *qy, int *qz) {
+    int ax = x - 2, ay = y - 2, az = z - 2;
+    int px = ax >> 2, py = ay >> 2, pz = az >> 2;
+    double fx = (ax & 3) / 4.0, fy = (ay & 3) / 4.0, fz = (az & 3) / 4.0;
+    int best = 0;
+    double bd = INFINITY;
+    for (int i = 0; i < 8; i++) {
+        int ex = (i & 4) == 0, ey = (i & 2) == 0, ez = (i & 1) == 0;
+        double d = zoom_dist(zseed, ex ? px : px + 1, ey ? py : py + 1, ez ? pz : pz + 1, ex ? fx : fx - 1.0,
+                             ey ? fy : fy - 1.0, ez ? fz : fz - 1.0);
+        if (bd > d) { best = i; bd = d; }
+    }
+    *qx = (best & 4) == 0 ? px : px + 1;
+    *qy = (best & 2) == 0 ? py : py + 1;
+    *qz = (best & 1) == 0 ? pz : pz + 1;
 }
 static int block_biome(const OrWorld *w, const SeedState *st, int x, int y, int z) {
     int ax = x - 2, ay = y - 2, az = z - 2;
@@ -1416,7 +1436,7 @@ void or_cell_climate(const OrWorld *w, int64_t seed, int qx, int qy, int qz, flo
     float v[6] = {0, 0, 0, 0, 0, 0};
     if (w->dim == OR_OVERWORLD) climate_ow(w, st, qx * 4, qy * 4, qz * 4, v, NULL);
     else if (w->dim == OR_NETHER) climate_nether(w, st, qx * 4, qy * 4, qz * 4, v);
-    else v[0] = (float)end_erosion(&st->end, w->fmode, qx * 4, qz * 4);
+    else v[0] = (float)end_erosion(&st->end, w->fmode, qx * 4, qz * 4, 12);
     for (int k = 0; k < 6; k++) { raw[k] = v[k]; tg[k] = w->dim == OR_END ? 0 : quantize(v[k]); }
     free(st);
 }
@@ -1484,4 +1504,107 @@ void or_chunk_grid(const OrWorld *w, int64_t seed, int qx0, int qz0, int nx, int
             for (int ix = 0; ix < nx; ix++) out[(size_t)iz * nx + ix] = (u8)cell_chunk(w, st, qx0 + ix, qy, qz0 + iz);
         free(st);
     }
+}
+
+/* ------------------------------------------------------------------------------------------------
+ * Biome seed search (crack/src/gpu_biomes/gpu_biomes.cu:245-278 search_cpu_impl; per-seed checks
+ * engine/cuda/mc_gpu.cuh:476-493 Overworld, 552-561 Nether, 685-693 End)
+ * ---------------------------------------------------------------------------------------------- */
+/* all leaves at the minimum fitness -> mask of their biomes (mc_gpu.cuh:166-187) */
+static void tree_ties(const Tree *T, int ni, const i64 *t, i64 *best, u64 m[2]) {
+    const TNode *nd = &T->node[ni];
+    for (int c = 0; c < nd->count; c++) {
+        int ci = T->kid[nd->first + c];
+        const TNode *cn = &T->node[ci];
+        i64 cd = box_dist(cn, t);
+        if (cd > *best) continue;
+        if (cn->count == 0) {
+            if (cd < *best) { *best = cd; m[0] = m[1] = 0; }
+            m[cn->biome >> 6] |= 1ULL << (cn->biome & 63);
+        } else tree_ties(T, ci, t, best, m);
+    }
+}
+static int obs_in(const OrObs *o, int b) { return (int)((o->mask[b >> 6] >> (b & 63)) & 1u); }
+
+/* number of leading observations seed passes */
+static int search_check(const OrWorld *w, SeedState *st, i64 seed, const OrObs *obs, int nobs, int ties) {
+    seed_init(w, seed, st);
+    for (int j = 0; j < nobs; j++) {
+        const OrObs *o = &obs[j];
+        int qx = o->qx, qy = o->qy, qz = o->qz;
+        if (o->flags & OR_OBS_BLOCK) zoom_quart(st->zoom, o->qx, o->qy, o->qz, &qx, &qy, &qz);
+        if (w->dim == OR_END) {
+            if (!obs_in(o, w->end_ids[end_class_r(&st->end, w->fmode, qx, qz, o->flags & 0xFF)])) return j;
+            continue;
+        }
+        i64 tg[TDIM];
+        cell_target(w, st, qx, qy, qz, tg, NULL);
+        int b = w->tree.node[tree_search(&w->tree, w->tree.root, tg, -1, NULL)].biome;
+        if (obs_in(o, b)) continue;
+        if (!ties) return j;
+        i64 best = INT64_MAX;
+        u64 m[2] = {0, 0};
+        tree_ties(&w->tree, w->tree.root, tg, &best, m);
+        if (!((m[0] & o->mask[0]) | (m[1] & o->mask[1]))) return j;
+    }
+    return nobs;
+}
+
+static int cmp_u64(const void *a, const void *b) {
+    u64 x = *(const u64 *)a, y = *(const u64 *)b;
+    return x < y ? -1 : x > y;
+}
+
+void or_search(const OrWorld *w, int kind, const int64_t *list, uint64_t base, uint64_t n, const OrObs *obs, int nobs,
+               int ties, uint64_t *reached, int64_t *found, uint32_t max_found, uint32_t *n_found, int threads) {
+    u64 total = kind == OR_SEEDS_STRUCTURE ? 65536u : n;
+    for (int j = 0; j <= nobs; j++) reached[j] = 0;
+    u64 *all = (u64 *)malloc(sizeof(u64) * (total ? total : 1));
+    u64 nall = 0;
+#pragma omp parallel num_threads(nthreads(threads))
+    {
+        SeedState *st = (SeedState *)malloc(sizeof(SeedState));
+        u64 *lh = (u64 *)calloc((size_t)nobs + 1, sizeof(u64));
+#pragma omp for schedule(dynamic, 64)
+        for (long long i = 0; i < (long long)total; i++) {
+            i64 seed = kind == OR_SEEDS_LIST ? list[i]
+                     : kind == OR_SEEDS_STRUCTURE ? (i64)(base | ((u64)i << 48)) : (i64)(base + (u64)i);
+            int j = search_check(w, st, seed, obs, nobs, ties);
+            lh[j]++;
+            if (j == nobs) {
+                u64 k;
+#pragma omp atomic capture
+                k = nall++;
+                all[k] = (u64)seed;
+            }
+        }
+#pragma omp critical
+        for (int j = 0; j <= nobs; j++) reached[j] += lh[j];
+        free(lh);
+        free(st);
+    }
+    qsort(all, (size_t)nall, sizeof(u64), cmp_u64);
+    u32 nf = nall < max_found ? (u32)nall : max_found;
+    for (u32 k = 0; k < nf; k++) found[k] = (i64)all[k];
+    *n_found = nf;
+    free(all);
+}
+
+/* half-width of the End window that decides membership in mask (engine/cuda/mc_gpu.cuh:640-652): the
+ * smallest class threshold at which membership changes bounds the islands that can matter */
+int or_obs_end_radius(const OrWorld *w, const uint64_t mask[2]) {
+    static const int order[4] = {3, 4, 2, 1}; /* small islands, barrens, midlands, highlands */
+    static const int th[3] = {-20, 0, 40};
+    int m[4];
+    for (int i = 0; i < 4; i++) {
+        int b = w->end_ids[order[i]];
+        m[i] = (int)((mask[b >> 6] >> (b & 63)) & 1u);
+    }
+    int T = 1000;
+    for (int i = 0; i < 3; i++)
+        if (m[i] != m[i + 1] && th[i] < T) T = th[i];
+    if (T == 1000) return 0;
+    double dmax = (101.0 - (double)T) / 9.0;
+    int rad = (int)((dmax + 1.0) / 2.0);
+    return rad > 12 ? 12 : rad;
 }

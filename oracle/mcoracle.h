@@ -103,6 +103,20 @@ int or_leaf_biome(const OrWorld *w, int leaf);
 typedef struct { int64_t octave_samples, tree_nodes, tree_queries, spline_nodes; } OrWork;
 void or_points_work(const OrWorld *w, int64_t seed, const int32_t *pts, int np, OrWork *work);
 
+/* Biome seed search (crack/src/gpu_biomes/gpu_biomes.h:44-56 gb_search): every candidate seed of the
+ * source is checked against the observations in order; reached[j] (nobs + 1 entries) counts the seeds
+ * that passed exactly j leading observations; seeds passing all are returned sorted as unsigned, at most
+ * max_found.  Sources: LIST (list[0..n)), STRUCTURE (base | i << 48, i < 65536), RANGE (base + i, i < n).
+ * An observation is a quart cell (or, with OR_OBS_BLOCK, a block resolved through BiomeManager's zoom)
+ * and a biome mask; flags' low byte is the End window half-width.  ties: also accept when any
+ * minimum-fitness leaf's biome is in the mask. */
+typedef struct { int32_t qx, qy, qz, flags; uint64_t mask[2]; } OrObs;
+#define OR_OBS_BLOCK 0x100
+enum { OR_SEEDS_LIST = 0, OR_SEEDS_STRUCTURE = 1, OR_SEEDS_RANGE = 2 };
+void or_search(const OrWorld *w, int kind, const int64_t *list, uint64_t base, uint64_t n, const OrObs *obs, int nobs,
+               int ties, uint64_t *reached, int64_t *found, uint32_t max_found, uint32_t *n_found, int threads);
+int or_obs_end_radius(const OrWorld *w, const uint64_t mask[2]);
+
 /* FNV-1a 64 over "minecraft:<name>\n" per cell (biome_grid_hashes.tsv digest). */
 uint64_t or_fnv1a64_names(const uint8_t *ids, size_t n);
 

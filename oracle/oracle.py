@@ -56,6 +56,10 @@ def lib():
         L.or_chunk_grid.argtypes = [vp, i64, i32, i32, i32, i32, i32, u8p, i32]
         L.or_fnv1a64_names.restype = C.c_uint64
         L.or_fnv1a64_names.argtypes = [u8p, C.c_size_t]
+        L.or_search.argtypes = [vp, i32, i64p, C.c_uint64, C.c_uint64, C.c_void_p, i32, i32, C.c_void_p, i64p,
+                                C.c_uint32, C.POINTER(C.c_uint32), i32]
+        L.or_obs_end_radius.restype = i32
+        L.or_obs_end_radius.argtypes = [vp, C.c_void_p]
         _lib = L
     return _lib
 
@@ -75,6 +79,23 @@ def biome_id(name: str) -> int:
 
 def hashed_seed(seed: int) -> int:
     return lib().or_hashed_seed(seed)
+
+
+SEEDS_LIST, SEEDS_STRUCTURE, SEEDS_RANGE = 0, 1, 2
+OBS_BLOCK = 0x100
+# one observation: qx, qy, qz, flags (OBS_BLOCK | End window half-width), mask[2]
+OBS_DTYPE = np.dtype([("qx", "<i4"), ("qy", "<i4"), ("qz", "<i4"), ("flags", "<i4"), ("mask", "<u8", (2,))])
+
+
+def make_obs(rows, block: bool = False, rad: int = 12) -> np.ndarray:
+    """Observations from (x, y, z, [biome ids]) rows."""
+    a = np.zeros(len(rows), OBS_DTYPE)
+    for i, (x, y, z, ids) in enumerate(rows):
+        a[i]["qx"], a[i]["qy"], a[i]["qz"] = x, y, z
+        a[i]["flags"] = (OBS_BLOCK if block else 0) | rad
+        for b in ids:
+            a[i]["mask"][b >> 6] |= np.uint64(1) << np.uint64(b & 63)
+    return a
 
 
 class World:
@@ -157,6 +178,26 @@ class World:
 
     def leaf_biome(self, leaf: int) -> int:
         return lib().or_leaf_biome(self._h, leaf)
+
+    def search(self, obs: np.ndarray, kind: int = SEEDS_STRUCTURE, base: int = 0, n: int = 0, seeds=None,
+               ties: bool = True, max_found: int = 1 << 16, threads: int = 0):
+        """Seed search: (found seeds sorted as unsigned, reached[nobs + 1])."""
+        obs = np.ascontiguousarray(obs, OBS_DTYPE)
+        lst = None
+        if kind == SEEDS_LIST:
+            lst = np.ascontiguousarray(seeds, np.int64)
+            n = lst.size
+        reached = np.zeros(len(obs) + 1, np.uint64)
+        found = np.zeros(max(1, max_found), np.int64)
+        nf = C.c_uint32()
+        lib().or_search(self._h, kind, _ptr(lst) if lst is not None else None, C.c_uint64(base & (2**64 - 1)),
+                        C.c_uint64(n), obs.ctypes.data, len(obs), int(ties), reached.ctypes.data, _ptr(found),
+                        max_found, C.byref(nf), threads)
+        return found[:nf.value].copy(), reached
+
+    def end_radius(self, mask) -> int:
+        m = np.ascontiguousarray(mask, np.uint64)
+        return lib().or_obs_end_radius(self._h, m.ctypes.data)
 
     def work(self, seed: int, pts):
         pts = np.ascontiguousarray(pts, dtype=np.int32).reshape(-1, 3)

@@ -10,6 +10,9 @@ Sources (read-only, present only where the reference tree is mounted):
   ``oracle/build.py`` -- random seeds x random quart points for every version, dimension and
   Overworld preset, stored as ``refpoints_<V>_<dim>_<preset>.npz`` (seeds, points, biome ids,
   quantised targets).  These extend the pinned cases to presets and 26.4 that the Java vectors lack.
+* the reference's seed-search known-answer observation files
+  (``crack/src/gpu_biomes/results/example_obs_26.3_overworld_seed*.txt``: quart cells and biomes from its
+  Java oracle for a known seed), copied to ``search/``.
 
 Usage:  python tests/golden/make_fixtures.py
 """
@@ -97,7 +100,17 @@ def reference_points() -> None:
                                     pts=pts, biome=biome, targets=tg)
 
 
+def copy_search_examples() -> None:
+    src = os.path.join(REF, "crack", "src", "gpu_biomes", "results")
+    dst = os.path.join(HERE, "search")
+    os.makedirs(dst, exist_ok=True)
+    for f in sorted(os.listdir(src)):
+        if f.startswith("example_obs_") and f.endswith(".txt"):
+            shutil.copyfile(os.path.join(src, f), os.path.join(dst, f))
+
+
 if __name__ == "__main__":
+    copy_search_examples()
     copy_vectors()
     reference_points()
     print("fixtures written under", HERE)

@@ -191,3 +191,10 @@ def test_fast_coordinate_split(mg):
     for seed in (1, 2):
         bf, bd = mg.check_split(1 << 26, seed)
         assert (bf, bd) == (0, 0)
+
+
+def test_fixed_point_octave(mg):
+    """The double branch's fixed-point octave (exact gradient sums, once-rounded first lerp differences)
+    equals the plain double octave on 2^24 random permutations x fractions."""
+    for seed in (3, 4):
+        assert mg.check_octave(1 << 24, seed) == 0
