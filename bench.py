@@ -175,12 +175,12 @@ def gpu_peaks(mg) -> dict:
 # Lattice (octave) samples per biome sample: 52 in the Overworld (six NormalNoises, two stacks each, with
 # the shift noise sampled twice), 8 in the Nether; the oracle's work counter pins both numbers.
 OCTAVES_PER_SAMPLE = {"minecraft:overworld": 52, "minecraft:the_nether": 8, "minecraft:the_end": 0}
-# FP64 operations of one octave sample as the kernels compute it: the double branch (26.1/26.2) does the
-# two rounded coordinate adds, fx - 1, eight gradient sums, two smoothsteps (7 each), the other fraction
-# minus one, seven lerps (3 each) and the amplitude product and sum (3): 50.  The float branch (26.3) does
-# only the two coordinate adds in FP64.  Smaller per-sample terms (shift coordinates, End simplex) are left
-# out, so the model is a lower bound.
-FP64_PER_OCTAVE = {"26.1": 50, "26.2": 50, "26.3": 2, "26.4-snapshot-2": 2}
+# FP64 operations of one octave sample as the kernels compute it.  Double branch (26.1/26.2): the two rounded
+# coordinate adds, two smoothsteps (7 each), the four first-level lerps' product and sum (the gradient sums
+# and lerp differences are exact in 2^-52 fixed point and run on the integer pipes), three more lerps (3
+# each) and the amplitude product and sum (3): 36.  Float branch (26.3): the two coordinate adds.  Smaller
+# per-sample terms (shift coordinates, End simplex) are left out, so the model is a lower bound.
+FP64_PER_OCTAVE = {"26.1": 36, "26.2": 36, "26.3": 2, "26.4-snapshot-2": 2}
 
 
 def batch_fp64_ops(reqs) -> float:
@@ -191,7 +191,7 @@ def batch_fp64_ops(reqs) -> float:
 # (work units per launch, unit name, pipe peak key).
 # DRAM bytes (read + write) per work unit of a launch, from one ncu capture each: k_batch per sample
 # (300-request prefix of the uneven batch), k_ow_seed_climate per seed (4,096 seeds x 8 points).
-DRAM_BYTES_PER_UNIT = {"k_batch": (4486912 + 955136) / 10987120, "k_ow_seed_climate": 98560 / 4096}
+DRAM_BYTES_PER_UNIT = {"k_batch": (4055296 + 963584) / 10987120, "k_ow_seed_climate": 98560 / 4096}
 
 
 def kernel_work(kernel: str, seeds8: bool, ns: int, np_: int, ntables: int) -> tuple[float, str, str] | None:
@@ -249,6 +249,8 @@ def run_gb300(args, rank, world, local_rank):
         return run_serve(args, rank, world, local_rank, mg, ge)
     elif args.workload == "dims4096":
         return run_dims(args, rank, world, local_rank, mg, ge)
+    elif args.workload == "search":
+        return run_search(args, rank, world, local_rank, mg, ge)
     else:
         w = gen.world("minecraft:overworld", "normal", 12345)
         nx = nz = 256
@@ -595,6 +597,105 @@ def serve_run(mg, worlds, stream, budget: int, max_inflight: int = 2):
             "batches": st["batches"], "mean_batch": round(st["requests_admitted"] / max(1, st["batches"]), 2)}
 
 
+SEARCH_SEED = 8675309
+
+
+def search_observations(mg, ge, version: str, dim: str):
+    """Observations of seed 8675309: the reference's 8-cell Overworld 26.3 known-answer file (committed as a
+    fixture) for the Overworld; for the Nether and the End, 8 cells at SplitMix64(5) positions in
+    [-5000, 5000) quarts with the biomes this library computes for that seed."""
+    if dim == "minecraft:overworld":
+        rows = []
+        path = os.path.join(REPO, "tests", "golden", "search", f"example_obs_26.3_overworld_seed{SEARCH_SEED}.txt")
+        names = {n: i for i, n in enumerate(mg.Generator.open(ge.data_root(), version).biome_names())}
+        for ln in open(path):
+            if ln.startswith("#") or not ln.strip():
+                continue
+            x, y, z, b = ln.split()
+            rows.append((int(x), int(y), int(z), [names[n] for n in b.split("|")]))
+        return mg.make_obs(rows)
+    r = splitmix64(5, 16)
+    pts = (-5000 + (r % np.uint64(10000)).astype(np.int64)).reshape(8, 2)
+    q = np.stack([pts[:, 0], np.full(8, 16), pts[:, 1]], 1).astype(np.int32)
+    w = mg.Generator.open(ge.data_root(), version).world(dim, "normal", 0)
+    ids = w.seed_points(np.array([SEARCH_SEED], np.int64), q)[0]
+    obs = mg.make_obs([(int(a), int(b), int(c), [int(i)]) for (a, b, c), i in zip(q, ids)])
+    if dim == "minecraft:the_end":
+        for o in obs:
+            o["flags"] = w.end_radius(o["mask"])
+    return obs
+
+
+def run_search(args, rank, world, local_rank, mg, ge):
+    """Biome seed search: the range [-2^25, 2^25) of candidate seeds (containing 8675309) against 8
+    observations, Overworld 26.3 (the headline value), 26.1, Nether 26.3 and End 26.3; ties mode on."""
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    n = args.search_candidates
+    base = -(n // 2)
+    cases = [("26.3", "minecraft:overworld"), ("26.1", "minecraft:overworld"), ("26.3", "minecraft:the_nether"),
+             ("26.3", "minecraft:the_end")]
+    res = {}
+    with ClockSampler(local_rank) as clk:
+        for v, d in cases:
+            obs = search_observations(mg, ge, v, d)
+            w = mg.Generator.open(ge.data_root(), v).world(d, "normal", 0)
+            for _ in range(args.warmup):
+                w.search(obs, kind=mg.SEEDS_RANGE, base=base, n=1 << 20)
+            mg.profile(True)
+            dev_ms, wall = 0.0, 0.0
+            for _ in range(args.steps):
+                t0 = time.perf_counter()
+                found, reached, ms = w.search(obs, kind=mg.SEEDS_RANGE, base=base, n=n)
+                wall += time.perf_counter() - t0
+                dev_ms += ms
+            mg.profile(False)
+            prof = mg.profile_read()
+            res[f"{v} {d.split(':')[1]}"] = {
+                "candidates_per_s": n * args.steps / (dev_ms * 1e-3), "e2e_candidates_per_s": n * args.steps / wall,
+                "ms_per_step": dev_ms / args.steps, "found": [int(x) for x in found[:8]], "n_found": int(len(found)),
+                "reached": [int(x) for x in reached],
+                "kernels": {k: {"ms_total": round(a, 3), "launches": b} for k, (a, b) in prof.items()}}
+    top = res["26.3 overworld"]
+    out = {"metric": "biome seed search candidates/sec", "value": top["candidates_per_s"], "unit": "candidates/s",
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": top["ms_per_step"],
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64+int64",
+           "data": "synthetic range of candidate seeds; observations of seed 8675309",
+           "config": {"workload": f"seed search: {n} candidates [-{n // 2}, {n // 2}) x 8 observations of seed "
+                                  "8675309 (Overworld: the reference's known-answer cells), ties mode",
+                      "candidates": n, "cases": res},
+           "e2e": {"value": top["e2e_candidates_per_s"], "unit": "candidates/s", "h2d_bytes_per_step": 8 * 32,
+                   "d2h_bytes_per_step": 8 * 9 + 8 * top["n_found"]},
+           "gpu_launches": sum(v["launches"] for v in top["kernels"].values())}
+    clocks = clk.summary()
+    if clocks:
+        out["clocks"] = clocks
+    if rank == 0:
+        if not args.skip_extras:
+            out["cpu_baseline"] = cpu_baseline_search(mg, ge, args.cpu_sample_s)
+        print(json.dumps(out), flush=True)
+
+
+def cpu_baseline_search(mg, ge, budget_s: float) -> dict:
+    """The search's reference algorithm (oracle restatement) on all host cores, Overworld 26.3."""
+    from oracle import oracle as O
+
+    cores = os.cpu_count() or 1
+    obs = search_observations(mg, ge, "26.3", "minecraft:overworld")
+    w = O.World(ge.data_root(), "26.3", "overworld")
+    n = 1 << 14
+    while True:
+        t0 = time.perf_counter()
+        w.search(obs, O.SEEDS_RANGE, base=SEARCH_SEED - n // 2, n=n, threads=cores)
+        dt = time.perf_counter() - t0
+        if dt > budget_s / 4 or n >= 1 << 24:
+            break
+        n *= 4
+    return {"value": n / dt, "unit": "candidates/s", "cores": cores, "kind": "port",
+            "sample": f"{n} candidates around 8675309 ({dt:.2f} s)"}
+
+
 def run_dims(args, rank, world, local_rank, mg, ge):
     """Other dimensions: 4,096 SplitMix64(2) seeds, a 64 x 64 quart grid at y=64 per seed, Nether 26.3 and
     End 26.3, each dimension one batched launch (plan + graph) of 4,096 requests."""
@@ -787,7 +888,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["seeds8", "grid256", "batch10k", "serve", "dims4096"], default="batch10k")
+    ap.add_argument("--workload", choices=["seeds8", "grid256", "batch10k", "serve", "dims4096", "search"],
+                    default="batch10k")
+    ap.add_argument("--search-candidates", type=int, default=1 << 26, help="search: candidates per step")
     ap.add_argument("--rates", default="500,1000,2000", help="serve: arrival rates (requests/s)")
     ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds per rate (60 = the configuration)")
     ap.add_argument("--requests", type=int, default=10000, help="batch10k: number of requests")

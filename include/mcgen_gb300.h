@@ -116,7 +116,7 @@ MCGEN_API int mcgen_gb300_server_stats(McGb300Server *s, McGb300ServerStats *out
  * seed; n ignored), MCGEN_SEEDS_RANGE base + i for i < n.  Each candidate is checked against obs[0..nobs)
  * in order and stops at the first observation it fails; reached[j] (nobs + 1 entries) counts candidates
  * that passed exactly j observations.  Candidates passing all are written to found, sorted as unsigned, at
- * most max_found (*n_found of them).  An observation (the reference's McgObs, engine/cuda/mc_gpu.cuh:47-54)
+ * most max_found (*n_found of them; when more pass, which ones is unspecified, as in the reference).  An observation (the reference's McgObs, engine/cuda/mc_gpu.cuh:47-54)
  * is a quart cell, or with MCGEN_OBS_BLOCK in flags a block that BiomeManager's zoom resolves with the
  * candidate's hashed seed, and the set of biome ids that satisfy it (mask bit id); flags' low byte is the
  * End window half-width (12 in the game; mcgen_gb300_obs_end_radius gives the narrowest exact one).

@@ -479,11 +479,14 @@ __device__ __forceinline__ double oct_d_z0(const MgLattice *__restrict__ L, doub
 }
 
 /* ------------------------------------------------------------------ NormalNoise (engine/mc_noise.h:285-324)
+ * Not inlined: a climate evaluation calls them six times per branch, and the grid kernels evaluate the
+ * climate at several sites (direct and along a tie chain); one out-of-line copy each keeps the kernels'
+ * hot code within the instruction cache, at the cost of a call per noise (2 x 2..9 octaves).
  * Every NormalNoise on the biome path has one input coordinate equal to zero: the five climate noises
  * and the Nether noises take (x, 0, z), ShiftA (x, 0, z), ShiftB (z, x, 0).  The second stack's input
  * x*(f*c) equals (x*c)*f exactly (f = 2^k), so xc = x*c is formed once per point. */
 /* float branch, non-legacy (interleaved first_k, second_k) */
-__device__ __forceinline__ float nn_f_y0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
+static __device__ __noinline__ float nn_f_y0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
                                          double xc, double zc) {
     float acc = 0.0f;
     const MgLattice *A = T + N.base, *B = A + N.nlev;
@@ -494,7 +497,7 @@ __device__ __forceinline__ float nn_f_y0(const MgNoise &N, const MgLattice *__re
     }
     return acc;
 }
-__device__ __forceinline__ float nn_f_z0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double y,
+static __device__ __noinline__ float nn_f_z0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double y,
                                          double xc, double yc) {
     float acc = 0.0f;
     const MgLattice *A = T + N.base, *B = A + N.nlev;
@@ -506,7 +509,7 @@ __device__ __forceinline__ float nn_f_z0(const MgNoise &N, const MgLattice *__re
     return acc;
 }
 /* float branch, legacy Nether form (whole first stack, then whole second stack) */
-__device__ __forceinline__ float nn_f_legacy_y0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
+static __device__ __noinline__ float nn_f_legacy_y0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
                                                 double xc, double zc) {
     float acc = 0.0f;
     const MgLattice *A = T + N.base, *B = A + N.nlev;
@@ -515,7 +518,7 @@ __device__ __forceinline__ float nn_f_legacy_y0(const MgNoise &N, const MgLattic
     return acc;
 }
 /* double branch: (first + second) * valueFactor */
-__device__ __forceinline__ double nn_d_y0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
+static __device__ __noinline__ double nn_d_y0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
                                           double xc, double zc) {
     double a = 0.0, b = 0.0;
     const MgLattice *A = T + N.base, *B = A + N.nlev;
@@ -529,7 +532,7 @@ __device__ __forceinline__ double nn_d_y0(const MgNoise &N, const MgLattice *__r
     }
     return (a + b) * N.vfac;
 }
-__device__ __forceinline__ double nn_d_z0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double y,
+static __device__ __noinline__ double nn_d_z0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double y,
                                           double xc, double yc) {
     double a = 0.0, b = 0.0;
     const MgLattice *A = T + N.base, *B = A + N.nlev;

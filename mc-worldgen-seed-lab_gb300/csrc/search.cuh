@@ -91,11 +91,14 @@ __device__ __forceinline__ void tree_ties(const MgTreeNode *__restrict__ T, cons
     }
 }
 
-/* observation met by a target: its ENGINE biome is in the mask, or (ties) any equal-fitness leaf's is */
+/* observation met by a target: its ENGINE biome is in the mask, or (ties) any equal-fitness leaf's is.  The
+ * ENGINE leaf is one of the equal-fitness leaves, so in ties mode the one traversal that collects their
+ * biomes decides alone. */
 __device__ __forceinline__ bool obs_accept(const MgObs &o, const MgTreeNode *__restrict__ T, const int32_t *tg, bool ties) {
-    uint64_t d;
-    if (obs_in(o, T[tree_search(T, tg, -1, d)].biome)) return true;
-    if (!ties) return false;
+    if (!ties) {
+        uint64_t d;
+        return obs_in(o, T[tree_search(T, tg, -1, d)].biome);
+    }
     uint64_t m[2];
     tree_ties(T, tg, m);
     return ((m[0] & o.mask[0]) | (m[1] & o.mask[1])) != 0;

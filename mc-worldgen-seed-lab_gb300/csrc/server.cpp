@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 #include <string.h>
 
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -80,7 +81,6 @@ struct McGb300Server {
     std::thread worker;
     bool stop = false;
     int max_batch = 4096;
-    int ctas = 0;
     Pool pool[3];
     std::vector<Batch> batches;
     std::deque<long long> pending;
@@ -91,6 +91,10 @@ struct McGb300Server {
 };
 
 namespace {
+
+/* tile shape of the served batches: 8 x 16 cells at 6 resident CTAs per SM, the shape the autotuner picks
+ * for the uneven mixed batch */
+const int kServeShape = 2;
 
 int crc(cudaError_t e) { return e == cudaSuccess ? 0 : e == cudaErrorMemoryAllocation ? MCGEN_E_NOMEM : MCGEN_E_INTERNAL; }
 
@@ -201,9 +205,8 @@ int launch_batch(McGb300Server *s, Batch &b) {
         r.state = lat;
         r.qx0 = T.req.qx0; r.qz0 = T.req.qz0; r.nx = T.req.nx; r.nz = T.req.nz; r.qy = T.req.qy;
         r.tie = MG_TIE_ENGINE;
-        r.tile0 = tiles;
+        r.tile0 = 0;
         r.out_off = out;
-        tiles += mg::batch_tiles(dim, r.qx0, r.qz0, r.nx, r.nz, 0);
         b.out_off.push_back(out);
         out += (long long)r.nx * r.nz;
         reqs.push_back(r);
@@ -211,6 +214,16 @@ int launch_batch(McGb300Server *s, Batch &b) {
         T.state = 1;
     }
     if (b.tickets.empty()) return 0;
+    /* processing order grouped by code path, heaviest first (as in a plan), then the tile numbering */
+    std::stable_sort(reqs.begin(), reqs.end(), [&](const MgBatchReq &x, const MgBatchReq &y) {
+        const MgWorldDesc &a = worlds[(size_t)x.world]->desc, &c = worlds[(size_t)y.world]->desc;
+        const int wa = a.dim * 2 + (a.fmode ? 1 : 0), wc = c.dim * 2 + (c.fmode ? 1 : 0);
+        return wa != wc ? wa < wc : x.world < y.world;
+    });
+    for (auto &r : reqs) {
+        r.tile0 = tiles;
+        tiles += mg::batch_tiles(worlds[(size_t)r.world]->desc.dim, r.qx0, r.qz0, r.nx, r.nz, kServeShape);
+    }
     cudaError_t e = cudaSuccess;
     std::vector<MgWorldDesc> wd;
     std::vector<const MgTreeNode *> tp;
@@ -261,7 +274,7 @@ int launch_batch(McGb300Server *s, Batch &b) {
     for (int k : wait_on)
         if ((e = cudaStreamWaitEvent(st, s->batches[(size_t)k].setup_done, 0))) return crc(e);
     int rc = mg::launch_batch(b.d_worlds, b.d_trees, b.d_reqs, (int)reqs.size(), tiles, s->pool[0].base, b.d_counter,
-                              b.d_out, s->ctas, 0, st);
+                              b.d_out, 0, kServeShape, st);
     if (rc) return MCGEN_E_INTERNAL;
     if ((e = cudaMemcpyAsync(b.h_out, b.d_out, (size_t)out, cudaMemcpyDeviceToHost, st))) return crc(e);
     if ((e = cudaEventRecord(b.done, st))) return crc(e);
@@ -372,11 +385,7 @@ MCGEN_API int mcgen_gb300_server_new(long long hbm_budget_bytes, int max_infligh
     s->stats.cache_slots[0] = s->pool[0].nslots;
     s->stats.cache_slots[1] = s->pool[1].nslots;
     s->stats.cache_slots[2] = s->pool[2].nslots;
-    int cps = 1, dev = 0, sms = 1;
-    mg::batch_prepare(&cps);
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    s->ctas = sms * cps;
+    mg::batch_prepare(nullptr); /* kernel attributes and resident grids, before any launch */
     s->batches.resize((size_t)max_inflight);
     for (auto &b : s->batches) {
         if ((e = cudaStreamCreateWithFlags(&b.st, cudaStreamNonBlocking)) ||

@@ -29,4 +29,4 @@ def test_fp64_model_covers_versions():
     assert set(bench.FP64_PER_OCTAVE) == set(VERSIONS)
     reqs = [("26.1", "minecraft:overworld", 1, 0, 0, 16, 16), ("26.3", "minecraft:the_nether", 2, 0, 0, 8, 16),
             ("26.2", "minecraft:the_end", 3, 0, 0, 16, 16)]
-    assert bench.batch_fp64_ops(reqs) == 256 * 52 * 50 + 64 * 8 * 2
+    assert bench.batch_fp64_ops(reqs) == 256 * 52 * 36 + 64 * 8 * 2
