@@ -166,8 +166,9 @@ MCGEN_API const char *mcgen_gb300_last_error(void);
  * branches (the double branch also checks the fraction in units of 2^-52).  Same seed, same inputs. */
 MCGEN_API int mcgen_gb300_check_split(long long n, unsigned long long seed, long long *bad_f, long long *bad_d);
 /* Device self-check of the double branch's fixed-point octave (gradient sums and first lerp differences in
- * units of 2^-52) against the plain double octave: n random (permutation, fractions) cases; *bad counts
- * results that differ as doubles. */
+ * units of 2^-52, smoothsteps in integer arithmetic) against the plain double octave: n random
+ * (permutation, fractions) cases; *bad counts octave results that differ as doubles and smoothsteps that
+ * differ in any bit. */
 MCGEN_API int mcgen_gb300_check_octave(long long n, unsigned long long seed, long long *bad);
 
 /* Pipe microbenchmarks on the current device, in giga-operations per second:
