@@ -14,7 +14,10 @@
  * Tie rules (about 0.04% of Overworld cells have two R-tree leaves at equal fitness):
  *   MCGEN_TIE_ENGINE     first minimum leaf in tree order (search without a candidate);
  *   MCGEN_TIE_GRID_CHAIN candidate = leaf of the previous cell, row-major (iz outer);
- *   MCGEN_TIE_CHUNK_CELL candidate chain along the chunk's fill order (what mcgen_biome_grid uses).
+ *   MCGEN_TIE_CHUNK_CELL candidate chain along the chunk's fill order (what mcgen_biome_grid uses);
+ *   MCGEN_TIE_CHUNK_ORDER candidate chain chunk by chunk (chunk rows, then each chunk's cells z-major) across
+ *                        the grid: 26.3's chunk-batched climate, the reference Java oracle's "chunk" mode
+ *                        (oracle/src/v263/oracle/compat/Compat.java:168-221) that its `chunk` golden digests pin.
  */
 #ifndef MCGEN_GB300_H
 #define MCGEN_GB300_H
@@ -23,15 +26,15 @@
 extern "C" {
 #endif
 
-enum { MCGEN_TIE_ENGINE = 0, MCGEN_TIE_GRID_CHAIN = 1, MCGEN_TIE_CHUNK_CELL = 2 };
+enum { MCGEN_TIE_ENGINE = 0, MCGEN_TIE_GRID_CHAIN = 1, MCGEN_TIE_CHUNK_CELL = 2, MCGEN_TIE_CHUNK_ORDER = 3 };
 
 /* Version / dimension / preset / seed of a world (McWorld is opaque in mcgen.h). */
 MCGEN_API int mcgen_gb300_world_info(const McWorld *w, int *version, int *dimension, int64_t *climate_seed,
                                      int *float_branch);
 
 /* Quart grid at quart y for the world's climate seed: out[iz*nx+ix] = biome of quart cell
- * (qx0+ix, qy, qz0+iz), no zoom.  tie_rule: MCGEN_TIE_ENGINE or MCGEN_TIE_GRID_CHAIN (the initial
- * candidate is none).  New in this library; the reference computes these grids in its Java oracle
+ * (qx0+ix, qy, qz0+iz), no zoom.  tie_rule: MCGEN_TIE_ENGINE, MCGEN_TIE_GRID_CHAIN or
+ * MCGEN_TIE_CHUNK_ORDER (the initial candidate is none).  New in this library; the reference computes these grids in its Java oracle
  * (ClimateApi.grid) and, per point, in engine/cuda/mcg_host.c:36-83. */
 MCGEN_API int mcgen_gb300_quart_grid(const McWorld *w, int qx0, int qz0, int nx, int nz, int qy, int tie_rule,
                                      uint8_t *out);
@@ -166,9 +169,8 @@ MCGEN_API const char *mcgen_gb300_last_error(void);
  * branches (the double branch also checks the fraction in units of 2^-52).  Same seed, same inputs. */
 MCGEN_API int mcgen_gb300_check_split(long long n, unsigned long long seed, long long *bad_f, long long *bad_d);
 /* Device self-check of the double branch's fixed-point octave (gradient sums and first lerp differences in
- * units of 2^-52, smoothsteps in integer arithmetic) against the plain double octave: n random
- * (permutation, fractions) cases; *bad counts octave results that differ as doubles and smoothsteps that
- * differ in any bit. */
+ * units of 2^-52) against the plain double octave: n random (permutation, fractions) cases; *bad counts
+ * results that differ as doubles. */
 MCGEN_API int mcgen_gb300_check_octave(long long n, unsigned long long seed, long long *bad);
 
 /* Pipe microbenchmarks on the current device, in giga-operations per second:

@@ -22,7 +22,7 @@ DATA_ROOT = HERE  # data/climate-<V>.txt and data/params/<V>/ live under this di
 MCGEN_OK, MCGEN_E_ARG, MCGEN_E_IO, MCGEN_E_DATA, MCGEN_E_VERSION = 0, 1, 2, 3, 4
 MCGEN_E_NOMEM, MCGEN_E_CANCEL, MCGEN_E_UNSUPPORTED, MCGEN_E_INTERNAL = 5, 6, 7, 8
 MCGEN_COMPUTE_CPU, MCGEN_COMPUTE_GPU, MCGEN_COMPUTE_AUTO = 0, 1, 2
-TIE_ENGINE, TIE_GRID_CHAIN, TIE_CHUNK_CELL = 0, 1, 2
+TIE_ENGINE, TIE_GRID_CHAIN, TIE_CHUNK_CELL, TIE_CHUNK_ORDER = 0, 1, 2, 3
 PIPES = {"fp32_fma": 0, "fp64_fma": 1, "fp64_add": 2, "int32_mad": 3, "cvt_f64_floor_s32": 4,
          "cvt_s32_f64": 5, "cvt_f64_f32": 6, "int64_mad": 7, "cvt_s64_f64": 8, "cvt_f32_f64": 9}
 ERR_BUF = 1024

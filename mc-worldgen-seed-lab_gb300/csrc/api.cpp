@@ -442,7 +442,7 @@ static int quart_grid_on(const McWorld *w, int qx0, int qz0, int nx, int nz, int
     DevBuf scratch(st);
     size_t sb = 0;
     if (w->dim == MG_END) sb = (size_t)(nx / 4 + 3) * (size_t)(nz / 4 + 3);
-    else if (rule == MCGEN_TIE_GRID_CHAIN) sb = mg::chain_scratch_bytes(n);
+    else if (rule == MCGEN_TIE_GRID_CHAIN || rule == MCGEN_TIE_CHUNK_ORDER) sb = mg::chain_scratch_bytes(n);
     cudaError_t e = scratch.alloc(sb);
     if (e) return cuda_code(e);
     int rc = mg::launch_quart_grid(w->desc, w->d_tree, w->d_state, qx0, qz0, nx, nz, qy, rule, d_out, scratch.p, st);
@@ -452,7 +452,7 @@ static int quart_grid_on(const McWorld *w, int qx0, int qz0, int nx, int nz, int
 MCGEN_API int mcgen_gb300_quart_grid(const McWorld *w, int qx0, int qz0, int nx, int nz, int qy, int tie_rule,
                                      uint8_t *out) {
     if (!w || !out || nx <= 0 || nz <= 0) return MCGEN_E_ARG;
-    if (tie_rule != MCGEN_TIE_ENGINE && tie_rule != MCGEN_TIE_GRID_CHAIN) return MCGEN_E_ARG;
+    if (tie_rule != MCGEN_TIE_ENGINE && tie_rule != MCGEN_TIE_GRID_CHAIN && tie_rule != MCGEN_TIE_CHUNK_ORDER) return MCGEN_E_ARG;
     if ((long long)nx * nz > (1LL << 31)) return MCGEN_E_ARG;
     std::lock_guard<std::mutex> lk(g_lock);
     if (!device_ready_locked()) return MCGEN_E_UNSUPPORTED;
@@ -470,7 +470,7 @@ MCGEN_API int mcgen_gb300_quart_grid(const McWorld *w, int qx0, int qz0, int nx,
 MCGEN_API int mcgen_gb300_quart_grid_dev(const McWorld *w, int qx0, int qz0, int nx, int nz, int qy, int tie_rule,
                                          uint8_t *d_out, void *stream) {
     if (!w || !d_out || nx <= 0 || nz <= 0) return MCGEN_E_ARG;
-    if (tie_rule != MCGEN_TIE_ENGINE && tie_rule != MCGEN_TIE_GRID_CHAIN) return MCGEN_E_ARG;
+    if (tie_rule != MCGEN_TIE_ENGINE && tie_rule != MCGEN_TIE_GRID_CHAIN && tie_rule != MCGEN_TIE_CHUNK_ORDER) return MCGEN_E_ARG;
     std::lock_guard<std::mutex> lk(g_lock);
     if (!device_ready_locked()) return MCGEN_E_UNSUPPORTED;
     int rc = world_device_locked(const_cast<McWorld *>(w));
@@ -550,7 +550,7 @@ MCGEN_API int mcgen_gb300_biome_grid_dev(const McWorld *w, int x0, int z0, int n
 MCGEN_API int mcgen_gb300_quart_grid_seed_dev(const McWorld *w, int64_t seed, int qx0, int qz0, int nx, int nz, int qy,
                                               int tie_rule, uint8_t *d_out, void *stream) {
     if (!w || !d_out || nx <= 0 || nz <= 0) return MCGEN_E_ARG;
-    if (tie_rule != MCGEN_TIE_ENGINE && tie_rule != MCGEN_TIE_GRID_CHAIN) return MCGEN_E_ARG;
+    if (tie_rule != MCGEN_TIE_ENGINE && tie_rule != MCGEN_TIE_GRID_CHAIN && tie_rule != MCGEN_TIE_CHUNK_ORDER) return MCGEN_E_ARG;
     std::lock_guard<std::mutex> lk(g_lock);
     if (!device_ready_locked()) return MCGEN_E_UNSUPPORTED;
     int rc = world_device_locked(const_cast<McWorld *>(w));
@@ -564,7 +564,7 @@ MCGEN_API int mcgen_gb300_quart_grid_seed_dev(const McWorld *w, int64_t seed, in
     if ((rc = mg::launch_setup(w->desc, (const int64_t *)d_seed.p, 1, (MgLattice *)state.p, st))) return cuda_code((cudaError_t)rc);
     size_t sb = 0;
     if (w->dim == MG_END) sb = (size_t)(nx / 4 + 3) * (size_t)(nz / 4 + 3);
-    else if (tie_rule == MCGEN_TIE_GRID_CHAIN) sb = mg::chain_scratch_bytes((long long)nx * nz);
+    else if (tie_rule == MCGEN_TIE_GRID_CHAIN || tie_rule == MCGEN_TIE_CHUNK_ORDER) sb = mg::chain_scratch_bytes((long long)nx * nz);
     if ((e = scratch.alloc(sb))) return cuda_code(e);
     rc = mg::launch_quart_grid(w->desc, w->d_tree, (const MgLattice *)state.p, qx0, qz0, nx, nz, qy, tie_rule, d_out,
                                scratch.p, st);

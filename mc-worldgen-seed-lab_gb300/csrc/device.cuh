@@ -243,60 +243,6 @@ __device__ __forceinline__ double fix_to_d(int64_t D) {
 __device__ __forceinline__ double fix_lerp(double u, int64_t A, int64_t B) {
     return fix_to_d(A) + u * fix_to_d(B - A);
 }
-/* Smoothstep t^3 (t (6t - 15) + 10) of t = F * 2^-52 (0 <= F < 2^52), bit-exact to the double arithmetic
- * of the reference -- each of its seven operations rounded to nearest-even in turn -- on the integer pipes.
- * A value is m * 2^e with m in [2^52, 2^53).  All intermediates are normal and, after t * (6t - 15) is
- * negated, the two differences are subtractions from small integer constants with results >= 1. */
-__device__ __forceinline__ void fx_mul(uint64_t m1, int e1, uint64_t m2, int e2, uint64_t &m, int &e) {
-    const uint64_t lo = m1 * m2, hi = __umul64hi(m1, m2); /* product in [2^104, 2^106) */
-    const int s = (hi >> 41) ? 53 : 52;
-    m = (hi << (64 - s)) | (lo >> s);
-    const uint64_t rem = lo & ((1ULL << s) - 1), half = 1ULL << (s - 1);
-    if (rem > half || (rem == half && (m & 1))) m++;
-    e = e1 + e2 + s;
-    if (m >> 53) { m >>= 1; e++; }
-}
-/* K - y for an integer constant K and 0 <= y = m * 2^e <= K - 1 (result >= 1), rounded to nearest-even */
-__device__ __forceinline__ void fx_ksub(uint64_t K, uint64_t m, int e, uint64_t &rm, int &re) {
-    /* y in units of 2^-55 (3 guard bits below the finest result ulp, 2^-52), the rest as a sticky bit */
-    const int k = e + 55;
-    uint64_t Y;
-    bool sticky;
-    if (k >= 0) {
-        Y = m << k;
-        sticky = false;
-    } else if (k > -64) {
-        Y = m >> -k;
-        sticky = (m & ((1ULL << -k) - 1)) != 0;
-    } else {
-        Y = 0;
-        sticky = m != 0;
-    }
-    const uint64_t R = (K << 55) - Y - (sticky ? 1 : 0); /* the exact difference is R + (sticky ? a fraction : 0) */
-    const int L = 64 - __clzll((long long)R);             /* >= 56: the result is >= 1 */
-    const int s = L - 53;
-    rm = R >> s;
-    const uint64_t rem = R & ((1ULL << s) - 1), half = 1ULL << (s - 1);
-    if (rem > half || (rem == half && (sticky || (rm & 1)))) rm++;
-    re = s - 55;
-    if (rm >> 53) { rm >>= 1; re++; }
-}
-__device__ __forceinline__ double fade_fix(int64_t F) {
-    if (F == 0) return 0.0;
-    const int L = 64 - __clzll(F);
-    const uint64_t mt = (uint64_t)F << (53 - L);
-    const int et = L - 105;
-    uint64_t ma, mb, mc, md, me, mf, mg;
-    int ea, eb, ec, ed, ee, ef, eg;
-    fx_mul(mt, et, mt, et, ma, ea);                   /* t * t */
-    fx_mul(ma, ea, mt, et, mb, eb);                   /* (t * t) * t */
-    fx_mul(mt, et, 3ULL << 51, -50, mc, ec);          /* t * 6 */
-    fx_ksub(15, mc, ec, md, ed);                      /* 15 - t * 6 = -(t * 6 - 15) */
-    fx_mul(mt, et, md, ed, me, ee);                   /* -(t * (t * 6 - 15)) */
-    fx_ksub(10, me, ee, mf, ef);                      /* t * (t * 6 - 15) + 10 */
-    fx_mul(mb, eb, mf, ef, mg, eg);                   /* t^3 * (...) */
-    return __longlong_as_double((long long)(((uint64_t)(eg + 52 + 1023) << 52) | (mg & ((1ULL << 52) - 1))));
-}
 template <typename P>
 __device__ __forceinline__ double octave_dfix(const P &p, int ix, double fx, int64_t FX, int iy, int64_t FY, double v,
                                               int iz, int64_t FZ, double w) {
@@ -305,7 +251,7 @@ __device__ __forceinline__ double octave_dfix(const P &p, int ix, double fx, int
     const int aa = p(a + iy), ab = p(a + iy + 1);
     const int ba = p(b + iy), bb = p(b + iy + 1);
     const int64_t GX = FX - ONE, GY = FY - ONE, GZ = FZ - ONE;
-    const double u = fade_fix(FX);
+    const double u = fade<double>(fx);
     const double x00 = fix_lerp(u, gdot_i(p(aa + iz), FX, FY, FZ), gdot_i(p(ba + iz), GX, FY, FZ));
     const double x10 = fix_lerp(u, gdot_i(p(ab + iz), FX, GY, FZ), gdot_i(p(bb + iz), GX, GY, FZ));
     const double x01 = fix_lerp(u, gdot_i(p(aa + iz + 1), FX, FY, GZ), gdot_i(p(ba + iz + 1), GX, FY, GZ));
@@ -316,13 +262,13 @@ __device__ __forceinline__ double octave_dfix(const P &p, int ix, double fx, int
 template <typename P, typename H>
 __device__ __forceinline__ double octave_d_y0(const P &p, const H &h, int ix, double fx, int64_t FX, int iz, double fz,
                                               int64_t FZ) {
-    if ((FX | FZ | h.Fy) >= 0) return octave_dfix(p, ix, fx, FX, h.iy, h.Fy, h.uyd, iz, FZ, fade_fix(FZ));
+    if ((FX | FZ | h.Fy) >= 0) return octave_dfix(p, ix, fx, FX, h.iy, h.Fy, h.uyd, iz, FZ, fade<double>(fz));
     return octave_y0<double>(p, h, ix, fx, iz, fz);
 }
 template <typename P, typename H>
 __device__ __forceinline__ double octave_d_z0(const P &p, const H &h, int ix, double fx, int64_t FX, int iy, double fy,
                                               int64_t FY) {
-    if ((FX | FY | h.Fz) >= 0) return octave_dfix(p, ix, fx, FX, iy, FY, fade_fix(FY), h.iz, h.Fz, h.uzd);
+    if ((FX | FY | h.Fz) >= 0) return octave_dfix(p, ix, fx, FX, iy, FY, fade<double>(fy), h.iz, h.Fz, h.uzd);
     return octave_z0<double>(p, h, ix, fx, iy, fy);
 }
 template <typename T>

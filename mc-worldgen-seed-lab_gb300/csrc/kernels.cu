@@ -237,6 +237,35 @@ __global__ void k_chain_resolve(const MgTreeNode *__restrict__ tree, const Chain
     out[g] = tree[leaf].biome;
 }
 
+/* CHUNK_ORDER: the chain runs chunk by chunk (chunk rows tz outer, tx inner) and, inside a chunk, over its
+ * cells in the grid (z outer, x inner), across chunks: the order of the 26.3 chunk-batched climate
+ * (oracle/src/v263/oracle/compat/Compat.java:168-221 in the reference).  order[pos] = cell index. */
+__global__ void k_chain_order(int qx0, int qz0, int nx, int nz, int32_t *__restrict__ order) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (long long)nx * nz) return;
+    const int qx = qx0 + (int)(g % nx), qz = qz0 + (int)(g / nx);
+    const int tx = qx >> 2, tz = qz >> 2;
+    const int za = max(tz * 4, qz0), zb = min(tz * 4 + 3, qz0 + nz - 1);
+    const int xa = max(tx * 4, qx0), xb = min(tx * 4 + 3, qx0 + nx - 1);
+    const long long pos = (long long)(za - qz0) * nx + (long long)(xa - qx0) * (zb - za + 1) +
+                          (long long)(qz - za) * (xb - xa + 1) + (qx - xa);
+    order[pos] = (int32_t)g;
+}
+/* the chain replay of k_chain_resolve along order[] */
+__global__ void k_chain_resolve_ordered(const MgTreeNode *__restrict__ tree, const ChainRec *__restrict__ rec, long long n,
+                                        const int32_t *__restrict__ order, uint8_t *__restrict__ out) {
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n || !rec[order[p]].tie) return;
+    long long j = p - 1;
+    while (j >= 0 && rec[order[j]].tie) j--;
+    int leaf = j >= 0 ? rec[order[j]].leaf : -1;
+    for (long long k = j + 1; k <= p; k++) {
+        const ChainRec &r = rec[order[k]];
+        if (leaf < 0 || node_dist(tree[leaf], r.tg) != r.d) leaf = r.leaf;
+    }
+    out[order[p]] = tree[leaf].biome;
+}
+
 /* mcgen_biome_grid: out[iz*nx+ix] = biome_at(x0 + ix*step, y, z0 + iz*step) (libmcgen/src/region.c:86-108) */
 template <bool FM, int DIM>
 __global__ void __launch_bounds__(128) k_blockgrid(const __grid_constant__ MgWorldDesc W, const MgTreeNode *__restrict__ tree,
@@ -340,7 +369,7 @@ int launch_end_lookup(const MgWorldDesc &W, const uint8_t *cls, int cx0, int cz0
     count_launch();
     return (int)cudaGetLastError();
 }
-size_t chain_scratch_bytes(long long ncells) { return (size_t)ncells * sizeof(ChainRec); }
+size_t chain_scratch_bytes(long long ncells) { return (size_t)ncells * (sizeof(ChainRec) + sizeof(int32_t)); }
 int launch_quart_grid(const MgWorldDesc &W, const MgTreeNode *tree, const MgLattice *state, int qx0, int qz0, int nx, int nz, int qy, int rule, uint8_t *out, void *scratch, cudaStream_t st) {
     long long n = (long long)nx * nz;
     if (n <= 0) return 0;
@@ -355,7 +384,7 @@ int launch_quart_grid(const MgWorldDesc &W, const MgTreeNode *tree, const MgLatt
         count_launch();
         return launch_end_lookup(W, cls, cx0, cz0, ncx, qx0, qz0, nx, nz, out, st);
     }
-    bool chain = rule == MG_TIE_GRID_CHAIN;
+    bool chain = rule == MG_TIE_GRID_CHAIN || rule == MG_TIE_CHUNK_ORDER;
     ChainRec *rec = (ChainRec *)scratch;
     if (W.fmode) {
         if (W.dim == MG_OVERWORLD) {
@@ -375,8 +404,14 @@ int launch_quart_grid(const MgWorldDesc &W, const MgTreeNode *tree, const MgLatt
         }
     }
     count_launch();
-    if (chain) {
+    if (rule == MG_TIE_GRID_CHAIN) {
         { ProfScope ps_(K_CHAIN_RESOLVE, st); k_chain_resolve<<<blocks_for(n, 256), 256, 0, st>>>(tree, rec, n, out); }
+        count_launch();
+    } else if (rule == MG_TIE_CHUNK_ORDER) {
+        int32_t *order = reinterpret_cast<int32_t *>(rec + n);
+        { ProfScope ps_(K_CHAIN_RESOLVE, st); k_chain_order<<<blocks_for(n, 256), 256, 0, st>>>(qx0, qz0, nx, nz, order); }
+        count_launch();
+        { ProfScope ps_(K_CHAIN_RESOLVE, st); k_chain_resolve_ordered<<<blocks_for(n, 256), 256, 0, st>>>(tree, rec, n, order, out); }
         count_launch();
     }
     return (int)cudaGetLastError();

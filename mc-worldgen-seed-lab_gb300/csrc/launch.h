@@ -33,7 +33,7 @@ int launch_ow_search_first(const MgWorldDesc &W, const MgTreeNode *tree, const i
                            const MgObs &o, int ties, void *scratch, int64_t *surv, unsigned *nsurv,
                            unsigned long long *fail, cudaStream_t st);
 
-/* one seed's quart grid.  Scratch: chain_scratch_bytes(nx*nz) for GRID_CHAIN; for the End,
+/* one seed's quart grid.  Scratch: chain_scratch_bytes(nx*nz) for GRID_CHAIN and CHUNK_ORDER; for the End,
  * (nx/4 + 2) * (nz/4 + 2) bytes of chunk classes. */
 size_t chain_scratch_bytes(long long ncells);
 int launch_quart_grid(const MgWorldDesc &W, const MgTreeNode *tree, const MgLattice *state, int qx0, int qz0, int nx,

@@ -18,7 +18,7 @@
 enum { MG_OVERWORLD = 0, MG_NETHER = 1, MG_END = 2 };
 enum { MG_V26_1 = 0, MG_V26_2 = 1, MG_V26_3 = 2, MG_V26_4 = 3 };
 /* how equal-fitness leaves resolve (see include/mcgen_gb300.h) */
-enum { MG_TIE_ENGINE = 0, MG_TIE_GRID_CHAIN = 1, MG_TIE_CHUNK_CELL = 2 };
+enum { MG_TIE_ENGINE = 0, MG_TIE_GRID_CHAIN = 1, MG_TIE_CHUNK_CELL = 2, MG_TIE_CHUNK_ORDER = 3 };
 
 /* One NormalNoise, seed-independent.  Level k of stack s uses lattice table base + s*nlev + k. */
 typedef struct {

@@ -3,9 +3,8 @@
  * on generated inputs that cover the ranges the biome path sees and the edges of the fast path:
  * integer quart coordinates, coordinates plus a float shift, their products with the second-stack factor,
  * tiny and huge values, values whose sum with the offset lands near an integer, in (-1, 0) or on 0, and
- * offsets at 0, near 256 and on integers.  Also: the double branch's fixed-point octave (octave_dfix, with
- * its integer smoothstep) against the plain double octave on random permutations and fractions, and the
- * integer smoothstep (fade_fix) bit for bit against the double one. */
+ * offsets at 0, near 256 and on integers.  Also: the double branch's fixed-point octave (octave_dfix)
+ * against the plain double octave on random permutations and fractions. */
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -103,9 +102,6 @@ __global__ void k_check_octave(long long n, uint64_t seed, unsigned long long *b
         const double a = octave_dfix(pp, ix, fx, F[0], iy, F[1], v, iz, F[2], w);
         const double c = octave_q<double>(pp, ix, fx, iy, fy, fy - 1.0, v, iz, fz, fz - 1.0, w);
         b += !(a == c);
-        /* the integer smoothstep, bit for bit */
-        b += __double_as_longlong(fade_fix(F[1])) != __double_as_longlong(v);
-        b += __double_as_longlong(fade_fix(F[2])) != __double_as_longlong(w);
     }
     if (b) atomicAdd(bad, b);
 }

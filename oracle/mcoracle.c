@@ -1608,3 +1608,33 @@ int or_obs_end_radius(const OrWorld *w, const uint64_t mask[2]) {
     int rad = (int)((dmax + 1.0) / 2.0);
     return rad > 12 ? 12 : rad;
 }
+
+/* ChunkGenerator's chunk-batched climate (26.3 "chunk" mode; oracle/src/v263/oracle/compat/Compat.java:168-221
+ * in the reference's Java oracle): the grid is walked chunk by chunk (4 x 4 quarts; chunk rows tz outer, tx
+ * inner) and, inside a chunk, over its cells in the grid (qz outer, qx inner); every R-tree search starts from
+ * the previous search's leaf (Climate.RTree's per-thread lastResult), across chunk boundaries.  The climate
+ * values are the point path's (sampleVolume on the quart-aligned chunk volume gives the same values). */
+void or_chunk_order_grid(const OrWorld *w, int64_t seed, int qx0, int qz0, int nx, int nz, int qy, uint8_t *out) {
+    SeedState *st = (SeedState *)malloc(sizeof(SeedState));
+    seed_init(w, seed, st);
+    const Tree *T = &w->tree;
+    const int tx0 = qx0 >> 2, tx1 = (qx0 + nx - 1) >> 2, tz0 = qz0 >> 2, tz1 = (qz0 + nz - 1) >> 2;
+    int last = -1;
+    for (int tz = tz0; tz <= tz1; tz++)
+        for (int tx = tx0; tx <= tx1; tx++) {
+            const int za = tz * 4 > qz0 ? tz * 4 : qz0, zb = tz * 4 + 3 < qz0 + nz - 1 ? tz * 4 + 3 : qz0 + nz - 1;
+            const int xa = tx * 4 > qx0 ? tx * 4 : qx0, xb = tx * 4 + 3 < qx0 + nx - 1 ? tx * 4 + 3 : qx0 + nx - 1;
+            for (int qz = za; qz <= zb; qz++)
+                for (int qx = xa; qx <= xb; qx++) {
+                    if (w->dim == OR_END) {
+                        out[(size_t)(qz - qz0) * nx + (qx - qx0)] = (u8)w->end_ids[end_class(&st->end, w->fmode, qx, qz)];
+                        continue;
+                    }
+                    i64 tg[TDIM];
+                    cell_target(w, st, qx, qy, qz, tg, NULL);
+                    last = tree_search(T, T->root, tg, last, NULL);
+                    out[(size_t)(qz - qz0) * nx + (qx - qx0)] = (u8)T->node[last].biome;
+                }
+        }
+    free(st);
+}

@@ -84,6 +84,10 @@ int or_biome_at(const OrWorld *w, int64_t seed, int x, int y, int z);
  * (libmcgen/src/region.c:86-122).  Parallel over rows. */
 void or_biome_grid(const OrWorld *w, int64_t seed, int x0, int z0, int nx, int nz, int step, int y,
                    uint8_t *out, int threads);
+/* 26.3 "chunk" mode grid (the Java oracle's chunk-batched climate): ties resolved by a candidate chain in
+ * chunk order (chunk rows, then the chunk's cells z-major), across chunks.  Single-threaded: the chain is
+ * sequential. */
+void or_chunk_order_grid(const OrWorld *w, int64_t seed, int qx0, int qz0, int nx, int nz, int qy, uint8_t *out);
 /* Quart grid with the chunk-cell tie chain per cell (no zoom). */
 void or_chunk_grid(const OrWorld *w, int64_t seed, int qx0, int qz0, int nx, int nz, int qy, uint8_t *out, int threads);
 /* mcgen_gpu_biome_points semantics: block points xyz[3n]. */

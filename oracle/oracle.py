@@ -56,6 +56,7 @@ def lib():
         L.or_chunk_grid.argtypes = [vp, i64, i32, i32, i32, i32, i32, u8p, i32]
         L.or_fnv1a64_names.restype = C.c_uint64
         L.or_fnv1a64_names.argtypes = [u8p, C.c_size_t]
+        L.or_chunk_order_grid.argtypes = [vp, i64, i32, i32, i32, i32, i32, u8p]
         L.or_search.argtypes = [vp, i32, i64p, C.c_uint64, C.c_uint64, C.c_void_p, i32, i32, C.c_void_p, i64p,
                                 C.c_uint32, C.POINTER(C.c_uint32), i32]
         L.or_obs_end_radius.restype = i32
@@ -178,6 +179,12 @@ class World:
 
     def leaf_biome(self, leaf: int) -> int:
         return lib().or_leaf_biome(self._h, leaf)
+
+    def chunk_order_grid(self, seed: int, qx0: int, qz0: int, nx: int, nz: int, qy: int) -> np.ndarray:
+        """26.3 "chunk" mode grid: ties chained in chunk order across the grid."""
+        out = np.empty((nz, nx), np.uint8)
+        lib().or_chunk_order_grid(self._h, seed, qx0, qz0, nx, nz, qy, _ptr(out))
+        return out
 
     def search(self, obs: np.ndarray, kind: int = SEEDS_STRUCTURE, base: int = 0, n: int = 0, seeds=None,
                ties: bool = True, max_found: int = 1 << 16, threads: int = 0):

@@ -198,3 +198,17 @@ def test_fixed_point_octave(mg):
     equals the plain double octave on 2^24 random permutations x fractions."""
     for seed in (3, 4):
         assert mg.check_octave(1 << 24, seed) == 0
+
+
+def test_chunk_mode_grid_hashes(gens, mg):
+    """The six golden 26.3 "chunk" digests through mcgen_gb300_quart_grid with MCGEN_TIE_CHUNK_ORDER, and an
+    unaligned grid (partial chunks on every side) against the oracle."""
+    rows = grid_hashes("26.3", "chunk")
+    assert len(rows) == 6
+    for dim, seed, qx0, qz0, n, qy, h in rows:
+        w = gens["26.3"].world("minecraft:" + dim, "normal", seed)
+        assert O.fnv1a64_names(w.quart_grid(qx0, qz0, n, n, qy, mg.TIE_CHUNK_ORDER)) == h, seed
+    w = gens["26.3"].world("minecraft:overworld", "normal", 777)
+    got = w.quart_grid(-301, 129, 203, 97, 16, mg.TIE_CHUNK_ORDER)
+    exp = O.World(ge.data_root(), "26.3", "overworld").chunk_order_grid(777, -301, 129, 203, 97, 16)
+    assert np.array_equal(got, exp)

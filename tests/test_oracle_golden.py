@@ -145,3 +145,13 @@ def test_world_errors(data_root):
         O.World(data_root, "26.3", "overworld", "no_such_preset")
     with pytest.raises(RuntimeError):
         O.World("/nonexistent", "26.3", "overworld")
+
+
+def test_chunk_mode_grid_hashes(data_root):
+    """26.3 "chunk" mode: all six golden FNV-1a64 digests of the 1024^2 Overworld grids whose ties are chained
+    in chunk order (the Java oracle's chunk-batched climate), pinned by the oracle's chunk-order grid."""
+    rows = grid_hashes("26.3", "chunk")
+    assert len(rows) == 6
+    w = O.World(data_root, "26.3", "overworld")
+    for dim, seed, qx0, qz0, n, qy, h in rows:
+        assert O.fnv1a64_names(w.chunk_order_grid(seed, qx0, qz0, n, n, qy)) == h, seed
