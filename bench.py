@@ -709,6 +709,7 @@ def run_dims(args, rank, world, local_rank, mg, ge):
     sh = stream.cuda_stream
     res = {}
     total_samples, total_ms, kern = 0, 0.0, {}
+    total_e2e_s, total_h2d = 0.0, 0
     with ClockSampler(local_rank) as clk:
         for dim in ("minecraft:the_nether", "minecraft:the_end"):
             w = gen.world(dim, "normal", 0)
@@ -731,9 +732,26 @@ def run_dims(args, rank, world, local_rank, mg, ge):
             mg.profile(False)
             for k, v in mg.profile_read().items():
                 kern[f"{dim.split(':')[1]}:{k}"] = {"ms_total": round(v[0], 4), "launches": v[1]}
-            res[dim.split(":")[1]] = {"ms_per_step": round(ms, 4), "samples_per_s": plan.output_bytes / (ms * 1e-3)}
+            # end to end: a plan from the host request list, run into pinned host memory, freed -- per step
+            h_out = torch.empty(plan.output_bytes, dtype=torch.uint8).pin_memory().numpy()
+            reqs = [(w, int(s), int(qx), int(qz), 64, 64, 16) for s, (qx, qz) in zip(seeds, origins)]
+            e2e_steps = 0 if args.skip_extras else min(args.steps, 5)
+            t0 = time.perf_counter()
+            h2d = 0
+            for _ in range(e2e_steps):
+                p = mg.Plan(reqs)
+                p.shape = plan.shape
+                p.run(h_out)
+                h2d = p.h2d_bytes
+                p.close()
+            e2e_s = time.perf_counter() - t0
+            res[dim.split(":")[1]] = {"ms_per_step": round(ms, 4), "samples_per_s": plan.output_bytes / (ms * 1e-3),
+                                      "e2e_samples_per_s": plan.output_bytes * e2e_steps / e2e_s if e2e_steps else None,
+                                      "h2d_bytes_per_step": int(h2d), "tile_shape": plan.shape}
             total_samples += plan.output_bytes
             total_ms += ms
+            total_e2e_s += e2e_s / e2e_steps if e2e_steps else 0.0
+            total_h2d += int(h2d)
     out = {"metric": METRIC, "value": total_samples * world / (total_ms * 1e-3), "unit": UNIT, "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (SplitMix64(2) seeds)",
@@ -741,11 +759,38 @@ def run_dims(args, rank, world, local_rank, mg, ge):
                                   "corners SplitMix64(102) uniform in [-30000,30000) blocks, Nether and End, one "
                                   "batched launch per dimension", "per_dimension": res},
            "kernels": kern, "gpu_launches": args.steps * 4}
+    if not args.skip_extras:
+        out["e2e"] = {"value": total_samples * world / total_e2e_s, "unit": UNIT, "h2d_bytes_per_step": total_h2d,
+                      "d2h_bytes_per_step": int(total_samples),
+                      "call": "Plan(requests) + plan_run(host buffer) + plan_free per dimension per step"}
     clocks = clk.summary()
     if clocks:
         out["clocks"] = clocks
     if rank == 0:
+        if not args.skip_extras:
+            out["cpu_baseline"] = cpu_baseline_dims(args.cpu_sample_s)
         print(json.dumps(out), flush=True)
+
+
+def cpu_baseline_dims(budget_s: float) -> dict:
+    """The reference algorithm (oracle port) on all host cores over the first seeds of the same workload."""
+    import __graft_entry__ as ge
+    from oracle import oracle as O
+
+    cores = os.cpu_count() or 1
+    seeds, origins = config3_inputs()
+    wn = O.World(ge.data_root(), "26.3", "the_nether")
+    we = O.World(ge.data_root(), "26.3", "the_end")
+    done, t0 = 0, time.perf_counter()
+    for sd, (qx, qz) in zip(seeds, origins):
+        wn.quart_grid(int(sd), int(qx), int(qz), 64, 64, 16, O.TIE_ENGINE, threads=cores)
+        we.quart_grid(int(sd), int(qx), int(qz), 64, 64, 16, O.TIE_ENGINE, threads=cores)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": done * 2 * 64 * 64 / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"first {done} of the 4096 seeds, Nether and End ({dt:.1f} s), rows over threads"}
 
 
 def run_serve(args, rank, world, local_rank, mg, ge):

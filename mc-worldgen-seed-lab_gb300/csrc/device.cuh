@@ -62,10 +62,33 @@ __device__ __forceinline__ int32_t lcg_bits(uint64_t &s, int bits) {
     s = (s * MG_LCG_MUL + 0xBULL) & MG_LCG_MASK;
     return (int32_t)(uint32_t)(s >> (48 - bits));
 }
+/* u % d for u < 2^31 and 2 <= d <= 256 by a multiply-high: with l = ceil(log2 d) and M = ceil(2^(31+l) / d)
+ * (< 2^32), floor(u / d) = umulhi(u, M) >> (l - 1) exactly, since M d - 2^(31+l) < d <= 2^l and u < 2^31
+ * (Granlund-Montgomery).  The table is indexed by d; in the shuffles every lane of a warp uses the same d. */
+struct DivMagic {
+    uint32_t m[257];
+    uint8_t sh[257];
+};
+constexpr DivMagic make_div_magic() {
+    DivMagic t{};
+    for (int d = 2; d <= 256; d++) {
+        int l = 0;
+        while ((1 << l) < d) l++;
+        t.m[d] = (uint32_t)(((1ULL << (31 + l)) + (uint64_t)d - 1) / (uint64_t)d);
+        t.sh[d] = (uint8_t)(l - 1);
+    }
+    return t;
+}
+static __constant__ DivMagic kDivMagic = make_div_magic();
+__device__ __forceinline__ int32_t mod_small(int32_t u, int32_t d) {
+    const uint32_t q = __umulhi((uint32_t)u, kDivMagic.m[d]) >> kDivMagic.sh[d];
+    return u - (int32_t)q * d;
+}
+/* java.util.Random.nextInt(bound) for 1 <= bound <= 256 (the permutation shuffles) */
 __device__ __forceinline__ int lcg_int(uint64_t &s, int32_t bound) {
     if ((bound & -bound) == bound) return (int)(((int64_t)bound * (int64_t)lcg_bits(s, 31)) >> 31);
     for (;;) {
-        int32_t b = lcg_bits(s, 31), v = b % bound;
+        int32_t b = lcg_bits(s, 31), v = mod_small(b, bound);
         if ((int32_t)((uint32_t)b - (uint32_t)v + (uint32_t)(bound - 1)) >= 0) return v;
     }
 }
@@ -522,13 +545,13 @@ static __device__ __noinline__ double nn_d_y0(const MgNoise &N, const MgLattice 
                                           double xc, double zc) {
     double a = 0.0, b = 0.0;
     const MgLattice *A = T + N.base, *B = A + N.nlev;
+    /* the two stacks' sums advance together (two independent octaves in flight); each keeps its order */
     for (int k = 0; k < N.nlev; k++) {
-        double f = N.freq[k];
-        a += N.amp_d[k] * oct_d_y0(A + k, x, z, f, N.fexp[k]) * N.vf_d[k];
-    }
-    for (int k = 0; k < N.nlev; k++) {
-        double f = N.freq[k];
-        b += N.amp_d[k] * oct_d_y0(B + k, xc, zc, f, N.fexp[k]) * N.vf_d[k];
+        const double f = N.freq[k];
+        const double oa = oct_d_y0(A + k, x, z, f, N.fexp[k]);
+        const double ob = oct_d_y0(B + k, xc, zc, f, N.fexp[k]);
+        a += N.amp_d[k] * oa * N.vf_d[k];
+        b += N.amp_d[k] * ob * N.vf_d[k];
     }
     return (a + b) * N.vfac;
 }
@@ -536,13 +559,13 @@ static __device__ __noinline__ double nn_d_z0(const MgNoise &N, const MgLattice 
                                           double xc, double yc) {
     double a = 0.0, b = 0.0;
     const MgLattice *A = T + N.base, *B = A + N.nlev;
+    /* the two stacks' sums advance together (two independent octaves in flight); each keeps its order */
     for (int k = 0; k < N.nlev; k++) {
-        double f = N.freq[k];
-        a += N.amp_d[k] * oct_d_z0(A + k, x, y, f, N.fexp[k]) * N.vf_d[k];
-    }
-    for (int k = 0; k < N.nlev; k++) {
-        double f = N.freq[k];
-        b += N.amp_d[k] * oct_d_z0(B + k, xc, yc, f, N.fexp[k]) * N.vf_d[k];
+        const double f = N.freq[k];
+        const double oa = oct_d_z0(A + k, x, y, f, N.fexp[k]);
+        const double ob = oct_d_z0(B + k, xc, yc, f, N.fexp[k]);
+        a += N.amp_d[k] * oa * N.vf_d[k];
+        b += N.amp_d[k] * ob * N.vf_d[k];
     }
     return (a + b) * N.vfac;
 }

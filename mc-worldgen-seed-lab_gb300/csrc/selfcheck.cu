@@ -64,6 +64,11 @@ __global__ void k_check_split(long long n, uint64_t seed, unsigned long long *ba
         split_dk(x, f, k, off, ia, da, F);
         split_d_plain(x * f, off, ib, db);
         bd += (ia != ib) || (__double_as_longlong(da) != __double_as_longlong(db)) || F != fixed52(db);
+        /* the multiply-high modulo of the legacy shuffles, against the division */
+        {
+            const int32_t d = 2 + (int32_t)(r3 % 255), u = (int32_t)(r2 >> 33);
+            bd += mod_small(u, d) != u % d;
+        }
     }
     if (bf) atomicAdd(&bad[0], bf);
     if (bd) atomicAdd(&bad[1], bd);
