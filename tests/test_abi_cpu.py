@@ -125,3 +125,36 @@ def test_no_device_fails_loudly(mg):
     assert w.biome_at(0, 64, 0) == -1
     ok, status = mg.gpu_status()
     assert not ok and "unavailable" in status
+
+
+def test_plan_and_search_argument_checks(mg):
+    """Argument checks of the batched and search entry points come before any device work."""
+    g = mg.Generator.open(ge.data_root(), "26.3")
+    w = g.world("minecraft:overworld", "normal", 1)
+    L = mg.load()
+    rq = (mg.McGb300Request * 2)(mg.McGb300Request(w.handle, 5, 0, 0, 4, 4, 16),
+                                  mg.McGb300Request(w.handle, 6, 0, 0, 0, 4, 16))
+    h = C.c_void_p()
+    assert L.mcgen_gb300_plan_new(rq, 2, 0, C.byref(h)) == mg.MCGEN_E_ARG        # an empty region
+    assert L.mcgen_gb300_plan_new(rq, 1, 1, C.byref(h)) == mg.MCGEN_E_ARG        # GRID_CHAIN is not a batch rule
+    assert L.mcgen_gb300_plan_new(None, 1, 0, C.byref(h)) == mg.MCGEN_E_ARG
+    obs = mg.make_obs([(0, 16, 0, [1])])
+    found = (C.c_int64 * 4)()
+    reached = (C.c_uint64 * 65)()
+    nf = C.c_uint32()
+
+    def search(o, n_obs, kind=1, lst=None, n=0):
+        return L.mcgen_gb300_search(w.handle, kind, lst, C.c_uint64(0), C.c_uint64(n),
+                                    o.ctypes.data if o is not None else None, n_obs, 1, found, 4, C.byref(nf), reached, None)
+
+    assert search(obs, 0) == mg.MCGEN_E_ARG                                       # no observation
+    assert search(obs, 65) == mg.MCGEN_E_ARG                                      # more than 64
+    assert search(None, 1) == mg.MCGEN_E_ARG
+    assert search(obs, 1, kind=3) == mg.MCGEN_E_ARG                               # unknown source
+    assert search(obs, 1, kind=0, lst=None, n=10) == mg.MCGEN_E_ARG               # list source without a list
+    bad = obs.copy()
+    bad["flags"][0] = 13                                                          # End window half-width > 12
+    assert search(bad, 1) == mg.MCGEN_E_ARG
+    bad["flags"][0] = 0x200                                                       # unknown flag
+    assert search(bad, 1) == mg.MCGEN_E_ARG
+    assert L.mcgen_gb300_obs_end_radius(None, None) == -1
