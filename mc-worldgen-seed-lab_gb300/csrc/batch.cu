@@ -22,14 +22,13 @@
 
 #include "batch.h"
 #include "climate.cuh"
+#include "endtile.cuh"
 #include "launch.h"
 #include "prof.h"
 
 namespace mg {
 
 #define BNT 128        /* threads per CTA: one quart cell per thread in Overworld / Nether tiles */
-#define END_TC 8       /* chunks per End tile side */
-#define END_WIN (END_TC + 24)
 
 /* ---------------------------------------------------------------- setup of a list of (world, seed) */
 #define LNT 128
@@ -134,11 +133,8 @@ __global__ void __launch_bounds__(LNT) k_setup_list_end(const MgSetupEntry *__re
  * they share storage: 24.6 KB per CTA, which leaves the register budget as the occupancy limit. */
 struct BatchEnd {
     uint8_t endp[256];
-    uint32_t rows[END_WIN];            /* bit i of rows[r]: window cell (i, r) is an island */
-    float isize[END_WIN * END_WIN];    /* its size */
-    uint8_t cls[END_TC * END_TC];
+    EndTile tile;
 };
-static_assert(END_WIN == 32 && BNT == 128 && END_TC * END_TC * 2 == BNT, "End tile layout: a warp fills one window row");
 struct BatchSmem {
     MgSpline spline;
     union {
@@ -173,78 +169,12 @@ template <bool FM>
 __device__ __forceinline__ void batch_end(const MgWorldDesc &W, BatchSmem &sm, const MgBatchReq &R, int tcx, int tcz,
                                           uint8_t *out) {
     const int cx0 = (R.qx0 >> 2) + tcx * END_TC, cz0 = (R.qz0 >> 2) + tcz * END_TC;
-    /* chunk c's height reads chunk cells c' + d, d in [-12, 12], with c' = (2c+1)/2 in Java int division
-     * (c for c >= 0, c + 1 for c < 0): a window of at most END_TC - 1 + 25 cells per axis */
-    const int wx0 = (cx0 * 2 + 1) / 2 - 12, wz0 = (cz0 * 2 + 1) / 2 - 12;
-    for (int i = threadIdx.x; i < END_WIN * END_WIN; i += blockDim.x) { /* 8 rounds, a window row per warp */
-        const long long tx = (long long)wx0 + i % END_WIN, tz = (long long)wz0 + i / END_WIN;
-        bool isl = false;
-        float size = 0.0f;
-        if (tx * tx + tz * tz > 4096LL) {
-            const double nv = simplex2(sm.end.endp, (double)tx, (double)tz, W.end_f2, W.end_g2);
-            isl = FM ? ((float)nv < -0.9f) : (nv < (double)-0.9f);
-            if (isl) size = fmodf(fabsf((float)tx) * 3439.0f + fabsf((float)tz) * 147.0f, 13.0f) + 9.0f;
-        }
-        sm.end.isize[i] = size;
-        const uint32_t m = __ballot_sync(0xFFFFFFFFu, isl);
-        if ((threadIdx.x & 31) == 0) sm.end.rows[i >> 5] = m;
-    }
-    __syncthreads();
-    /* two threads per chunk, each over half of the 25 window rows, visiting only the rows' island bits; the
-     * maximum does not depend on the order */
-    {
-        const int c = threadIdx.x >> 1, half = threadIdx.x & 1;
-        const int cx = cx0 + c % END_TC, cz = cz0 + c / END_TC;
-        const bool outer = (long long)cx * cx + (long long)cz * cz > 4096LL;
-        const int bx = (cx * 2 + 1) * 8, bz = (cz * 2 + 1) * 8;
-        float best = -100.0f;
-        if (outer) {
-            const int sx = bx / 8, sz = bz / 8;
-            const int ccx = sx / 2, ccz = sz / 2, ox = sx % 2, oz = sz % 2;
-            if (!FM) {
-                int32_t sq = (int32_t)((uint32_t)sx * (uint32_t)sx + (uint32_t)sz * (uint32_t)sz);
-                float len = (float)sqrt((double)(float)sq);
-                best = clampf(100.0f - len * 8.0f, -100.0f, 80.0f);
-            }
-            const int sh = ccx - 12 - wx0; /* 0 .. END_TC - 1 */
-            for (int dz = half ? 1 : -12; dz <= (half ? 12 : 0); dz++) {
-                const int row = ccz + dz - wz0;
-                uint32_t m = (sm.end.rows[row] >> sh) & 0x1FFFFFFu;
-                while (m) {
-                    const int b = __ffs((int)m) - 1;
-                    m &= m - 1;
-                    const int dx = b - 12;
-                    const float xd = (float)(ox - dx * 2), zd = (float)(oz - dz * 2);
-                    const float h = clampf(100.0f - (float)sqrt((double)(xd * xd + zd * zd)) * sm.end.isize[row * END_WIN + b + sh], -100.0f, 80.0f);
-                    best = best > h ? best : h;
-                }
-            }
-        }
-        const float other = __shfl_xor_sync(0xFFFFFFFFu, best, 1);
-        best = best > other ? best : other;
-        if (half == 0) {
-            int cls = 0;
-            if (outer) {
-                double e;
-                if (!FM) e = ((double)best - 8.0) / 128.0;
-                else {
-                    const float ddx = (float)(0 - bx), ddz = (float)(0 - bz);
-                    const float len = (float)sqrt((double)(ddx * ddx + 0.0f * 0.0f + ddz * ddz));
-                    const float cc = (clampf(100.0f - len, -100.0f, 80.0f) - 8.0f) * 0.0078125f;
-                    const float o = (best - 8.0f) / 128.0f;
-                    e = (double)(cc > o ? cc : o);
-                }
-                cls = e > 0.25 ? 1 : (e >= -0.0625 ? 2 : (e < -0.21875 ? 3 : 4));
-            }
-            sm.end.cls[c] = (uint8_t)cls;
-        }
-    }
-    __syncthreads();
+    end_tile_classes<FM>(sm.end.endp, W.end_f2, W.end_g2, cx0, cz0, sm.end.tile);
     for (int i = threadIdx.x; i < 16 * END_TC * END_TC; i += blockDim.x) {
         const int qx = 4 * cx0 + i % (4 * END_TC), qz = 4 * cz0 + i / (4 * END_TC);
         const int ix = qx - R.qx0, iz = qz - R.qz0;
         if (ix < 0 || iz < 0 || ix >= R.nx || iz >= R.nz) continue;
-        out[R.out_off + (size_t)iz * R.nx + ix] = (uint8_t)W.end_ids[sm.end.cls[(i / (16 * END_TC)) * END_TC + (i % (4 * END_TC)) / 4]];
+        out[R.out_off + (size_t)iz * R.nx + ix] = (uint8_t)W.end_ids[sm.end.tile.cls[(i / (16 * END_TC)) * END_TC + (i % (4 * END_TC)) / 4]];
     }
 }
 

@@ -9,13 +9,14 @@
  *                                   ENGINE biomes or GRID_CHAIN records (leaf, fitness, tie flag, target)
  *                   k_chain_resolve GRID_CHAIN replay for the (rare) tied cells
  *                   k_blockgrid     libmcgen mcgen_biome_grid: BiomeManager zoom + chunk-cell tie chain
- *                   k_end_chunks    End island class per chunk
+ *                   k_end_chunks    End island class per chunk, 8 x 8-chunk tiles (endtile.cuh)
  */
 #include <cuda_runtime.h>
 #include <stddef.h>
 #include <stdint.h>
 
 #include "climate.cuh"
+#include "endtile.cuh"
 #include "device.cuh"
 #include "launch.h"
 #include "prof.h"
@@ -300,16 +301,25 @@ __global__ void __launch_bounds__(128) k_blockgrid(const __grid_constant__ MgWor
 template <bool FM>
 __global__ void __launch_bounds__(128) k_end_chunks(const MgLattice *__restrict__ state, int cx0, int cz0, int ncx,
                                                     int ncz, uint8_t *__restrict__ cls, double F2, double G2) {
+    /* one 8 x 8-chunk tile per block (endtile.cuh) */
     __shared__ uint8_t p[256];
+    __shared__ EndTile tile;
     for (int i = threadIdx.x; i < 256; i += blockDim.x) p[i] = state->p[i];
     __syncthreads();
-    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= (long long)ncx * ncz) return;
-    cls[g] = (uint8_t)end_chunk_class(p, FM, cx0 + (int)(g % ncx), cz0 + (int)(g / ncx), F2, G2);
+    const int tw = (ncx + END_TC - 1) / END_TC;
+    const int tx0 = cx0 + (int)(blockIdx.x % tw) * END_TC, tz0 = cz0 + (int)(blockIdx.x / tw) * END_TC;
+    end_tile_classes<FM>(p, F2, G2, tx0, tz0, tile);
+    if (threadIdx.x < END_TC * END_TC) {
+        const int cx = tx0 + threadIdx.x % END_TC, cz = tz0 + threadIdx.x / END_TC;
+        if (cx < cx0 + ncx && cz < cz0 + ncz) cls[(size_t)(cz - cz0) * ncx + (cx - cx0)] = tile.cls[threadIdx.x];
+    }
 }
 
 /* ============================================================================ host launchers */
 static inline unsigned blocks_for(long long n, int nt) { return (unsigned)((n + nt - 1) / nt); }
+static unsigned end_tiles(int ncx, int ncz) {
+    return (unsigned)(((long long)(ncx + END_TC - 1) / END_TC) * ((ncz + END_TC - 1) / END_TC));
+}
 static size_t grid_smem(const MgWorldDesc &W) { return sizeof(MgSpline) + (size_t)W.ntables * sizeof(MgLattice); }
 
 int launch_setup(const MgWorldDesc &W, const int64_t *d_seeds, int ns, MgLattice *d_states, cudaStream_t st) {
@@ -379,8 +389,8 @@ int launch_quart_grid(const MgWorldDesc &W, const MgTreeNode *tree, const MgLatt
         int cx1 = ((qx0 + nx - 1) * 4) >> 4, cz1 = ((qz0 + nz - 1) * 4) >> 4;
         int ncx = cx1 - cx0 + 1, ncz = cz1 - cz0 + 1;
         uint8_t *cls = (uint8_t *)scratch;
-        if (W.fmode) { ProfScope ps_(K_END_CHUNKS, st); k_end_chunks<true><<<blocks_for((long long)ncx * ncz, 128), 128, 0, st>>>(state, cx0, cz0, ncx, ncz, cls, W.end_f2, W.end_g2); }
-        else { ProfScope ps_(K_END_CHUNKS, st); k_end_chunks<false><<<blocks_for((long long)ncx * ncz, 128), 128, 0, st>>>(state, cx0, cz0, ncx, ncz, cls, W.end_f2, W.end_g2); }
+        if (W.fmode) { ProfScope ps_(K_END_CHUNKS, st); k_end_chunks<true><<<end_tiles(ncx, ncz), 128, 0, st>>>(state, cx0, cz0, ncx, ncz, cls, W.end_f2, W.end_g2); }
+        else { ProfScope ps_(K_END_CHUNKS, st); k_end_chunks<false><<<end_tiles(ncx, ncz), 128, 0, st>>>(state, cx0, cz0, ncx, ncz, cls, W.end_f2, W.end_g2); }
         count_launch();
         return launch_end_lookup(W, cls, cx0, cz0, ncx, qx0, qz0, nx, nz, out, st);
     }
@@ -435,8 +445,8 @@ int launch_block_biomes(const MgWorldDesc &W, const MgTreeNode *tree, const MgLa
     if ((long long)nx * nz <= 0) return 0;
     uint8_t *cls = (uint8_t *)scratch; /* End chunk classes, or null: evaluate per sample */
     if (W.dim == MG_END && cls) {
-        if (W.fmode) { ProfScope ps_(K_END_CHUNKS, st); k_end_chunks<true><<<blocks_for((long long)encx * encz, 128), 128, 0, st>>>(state, ecx0, ecz0, encx, encz, cls, W.end_f2, W.end_g2); }
-        else { ProfScope ps_(K_END_CHUNKS, st); k_end_chunks<false><<<blocks_for((long long)encx * encz, 128), 128, 0, st>>>(state, ecx0, ecz0, encx, encz, cls, W.end_f2, W.end_g2); }
+        if (W.fmode) { ProfScope ps_(K_END_CHUNKS, st); k_end_chunks<true><<<end_tiles(encx, encz), 128, 0, st>>>(state, ecx0, ecz0, encx, encz, cls, W.end_f2, W.end_g2); }
+        else { ProfScope ps_(K_END_CHUNKS, st); k_end_chunks<false><<<end_tiles(encx, encz), 128, 0, st>>>(state, ecx0, ecz0, encx, encz, cls, W.end_f2, W.end_g2); }
         count_launch();
     }
     if (W.fmode) {
