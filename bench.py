@@ -103,6 +103,17 @@ def config4_requests(n: int = 10000, state: int = 3):
 
 
 # ------------------------------------------------------------------------------------------ helpers
+def max_over_ranks(x: float, world: int, device) -> float:
+    """The slowest rank's time: replicas run independently and the job takes as long as its slowest."""
+    if world <= 1:
+        return float(x)
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -314,10 +325,7 @@ def run_gb300(args, rank, world, local_rank):
     mg.profile(False)
     prof = mg.profile_read()
     launches = mg.launch_count() - launches0
-    t = torch.tensor([ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
+    ms_max = max_over_ranks(ms, world, dev)
     value = samples * args.steps * world / (ms_max * 1e-3)
 
     # end to end through the host-buffer C ABI (pinned host memory, copies inside the timed region)
@@ -331,10 +339,7 @@ def run_gb300(args, rank, world, local_rank):
         host_step()
     torch.cuda.synchronize(dev)
     e2e_s = max(time.perf_counter() - t0, 1e-9)
-    te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
-    e2e = samples * args.steps * world / float(te.item())
+    e2e = samples * args.steps * world / max_over_ranks(e2e_s, world, dev)
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -405,10 +410,7 @@ def run_batch(args, rank, world, local_rank, mg, ge):
         ms = ev0.elapsed_time(ev1)
     barrier()
     graph_launches = mg.launch_count() - launches0  # graph replays are not counted by the library
-    t = torch.tensor([ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
+    ms_max = max_over_ranks(ms, world, dev)
     value = samples * args.steps * world / (ms_max * 1e-3)
     # per-kernel times: one run without the graph, under the library's event profiler
     mg.profile(True)

@@ -30,10 +30,11 @@ def read_example(path):
     return m.group(1), m.group(2), int(m.group(3)), rows
 
 
-def oracle_obs(version: str, dim: str, seed: int, k: int, block: bool, rng_seed: int, spread: int = 5000):
+def oracle_obs(version: str, dim: str, seed: int, k: int, block: bool, rng_seed: int, spread: int = 5000,
+               preset: str = "normal"):
     """k observations of `seed` from the oracle: quart cells (or blocks through the zoom) with their biome."""
     rng = np.random.default_rng(rng_seed)
-    w = O.World(ge.data_root(), version, dim)
+    w = O.World(ge.data_root(), version, dim, preset)
     rows = []
     for _ in range(k):
         x, z = (int(v) for v in rng.integers(-spread, spread, 2))

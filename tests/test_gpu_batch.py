@@ -97,3 +97,28 @@ def test_batch_config4_sample(env):
         v, d, s, qx0, qz0, n, qy = reqs[i]
         exp = O.World(ge.data_root(), v, d.split(":")[1]).quart_grid(s, qx0, qz0, n, n, qy, O.TIE_ENGINE)
         assert np.array_equal(out[i], exp), reqs[i]
+
+
+def test_batch_presets_versions_extremes(env):
+    """Plans over worlds the uneven batch does not draw: 26.4-snapshot-2, amplified and large_biomes, at
+    coordinates near the +-30M-block world border, single cells, rows and a 700 x 3 strip; CHUNK_CELL too."""
+    mg, gens, worlds = env
+    wl = {("26.4-snapshot-2", "minecraft:overworld", "normal"): gens["26.4-snapshot-2"].world("minecraft:overworld", "normal", 0),
+          ("26.1", "minecraft:overworld", "amplified"): gens["26.1"].world("minecraft:overworld", "amplified", 0),
+          ("26.3", "minecraft:overworld", "large_biomes"): gens["26.3"].world("minecraft:overworld", "large_biomes", 0),
+          ("26.2", "minecraft:the_end", "normal"): gens["26.2"].world("minecraft:the_end", "normal", 0)}
+    cases = [(-7_499_990, 7_499_000, 24, 40), (7_499_000, -7_499_990, 1, 1), (-3, -2, 700, 3), (123, -456, 1, 65)]
+    reqs = []
+    for i, key in enumerate(wl):
+        for j, (qx0, qz0, nx, nz) in enumerate(cases):
+            reqs.append((key, (i * 7919 + j * 104729) * (-1) ** j, qx0, qz0, nx, nz, 16 if j % 2 else -10))
+    for rule in (0, 2):
+        plan = mg.Plan([(wl[k], s, qx0, qz0, nx, nz, qy) for k, s, qx0, qz0, nx, nz, qy in reqs], tie_rule=rule)
+        out = plan.split(plan.run())
+        for (k, s, qx0, qz0, nx, nz, qy), got in zip(reqs, out):
+            ow = O.World(ge.data_root(), k[0], k[1].split(":")[1], k[2])
+            if rule == 2 and not k[1].endswith("the_end"):
+                exp = ow.chunk_grid(s, qx0, qz0, nx, nz, qy)
+            else:
+                exp = ow.quart_grid(s, qx0, qz0, nx, nz, qy, O.TIE_ENGINE)
+            assert np.array_equal(got, exp), (k, s, qx0, qz0, nx, nz, rule)

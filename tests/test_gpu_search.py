@@ -103,3 +103,15 @@ def test_max_found_and_arguments(gens, mg):
         w.search(bad, kind=O.SEEDS_STRUCTURE, base=42)
     with pytest.raises(mg.McError):
         w.search(obs[:0], kind=O.SEEDS_STRUCTURE, base=42)
+
+
+@pytest.mark.parametrize("preset", ["amplified", "large_biomes"])
+def test_overworld_presets(gens, preset):
+    seed = 0x7777_1234_5678
+    obs = oracle_obs("26.3", "overworld", seed, 6, True, 21, spread=3000, preset=preset)
+    rng = np.random.default_rng(13)
+    lst = np.concatenate([rng.integers(-2**63, 2**63 - 1, 20000, dtype=np.int64), [seed]])
+    w = gens["26.3"].world("minecraft:overworld", preset, 0)
+    ow = O.World(ge.data_root(), "26.3", "overworld", preset)
+    f1, r1, f2, r2 = both(w, ow, obs, kind=O.SEEDS_LIST, seeds=lst)
+    assert np.array_equal(r1, r2) and np.array_equal(f1, f2) and seed in set(f1.tolist())
