@@ -176,10 +176,10 @@ __device__ __forceinline__ int64_t zoom_step(int64_t r, int64_t c) {
     v *= v * 6364136223846793005ULL + 1442695040888963407ULL;
     return (int64_t)(v + (uint64_t)c);
 }
+/* Math.floorMod(r >> 24, 1024) / 1024.0: the low ten bits, and the division by 2^10 is exact as a scaling */
 __device__ __forceinline__ double zoom_jitter(int64_t r) {
-    int64_t m = (r >> 24) % 1024;
-    if (m < 0) m += 1024;
-    return ((double)m / 1024.0 - 0.5) * 0.9;
+    const int m = (int)((r >> 24) & 1023);
+    return ((double)m * 0x1.0p-10 - 0.5) * 0.9;
 }
 __device__ __forceinline__ double zoom_dist(int64_t seed, int x, int y, int z, double dx, double dy, double dz) {
     int64_t r = seed;
@@ -224,8 +224,9 @@ __device__ int cell_chunk(const MgWorldDesc &W, const MgSpline &S, const MgLatti
     for (;;) {
         int sec = idx >> 6, r = idx & 63;
         cell_target<FM, DIM>(W, S, T, bx + (r >> 4), qmin + sec * 4 + ((r >> 2) & 3), bz + (r & 3), tg);
-        leaf = tree_search(tree, tg, -1, d);
-        if (idx == 0 || tree_count_at(tree, tg, d) < 2) break;
+        bool tied;
+        leaf = tree_search_tie(tree, tg, d, tied);
+        if (idx == 0 || !tied) break;
         idx--;
     }
     for (int k = idx + 1; k <= idx0; k++) { /* replay the chain forward */

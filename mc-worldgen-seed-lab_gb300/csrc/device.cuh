@@ -680,25 +680,34 @@ __device__ __forceinline__ int tree_search(const MgTreeNode *__restrict__ T, con
     }
     return res;
 }
-/* leaves at fitness d, capped at 2 (libmcgen/src/biome.c:76-85) */
-__device__ __forceinline__ int tree_count_at(const MgTreeNode *__restrict__ T, const int32_t *t, uint64_t d) {
-    int stk_node[10], stk_next[10], sp = 1, cnt = 0;
+/* tree_search (no candidate) and whether a second leaf has the same fitness, in one traversal: children
+ * are visited iff their box distance is <= the best so far, so every leaf at the final minimum is seen; the
+ * first leaf to reach the minimum in tree order is kept -- the leaf tree_search returns, since no leaf
+ * before it in tree order is as close -- and the leaves at the minimum are counted (capped at 2; the
+ * tie test of libmcgen/src/biome.c:76-85). */
+__device__ __forceinline__ int tree_search_tie(const MgTreeNode *__restrict__ T, const int32_t *t, uint64_t &best,
+                                               bool &tied) {
+    int stk_node[10], stk_next[10], sp = 1, res = -1, cnt = 0;
+    best = ~0ULL;
     stk_node[0] = 0;
     stk_next[0] = 0;
-    while (sp > 0 && cnt < 2) {
-        int nd = stk_node[sp - 1], c = stk_next[sp - 1];
+    while (sp > 0) {
+        const int nd = stk_node[sp - 1], c = stk_next[sp - 1];
         if (c >= T[nd].count) { sp--; continue; }
         stk_next[sp - 1] = c + 1;
-        int ci = T[nd].first + c;
-        uint64_t cd = node_dist(T[ci], t);
-        if (cd <= d) {
-            if (T[ci].count == 0) cnt += (cd == d);
-            else if (sp < 10) { stk_node[sp] = ci; stk_next[sp] = 0; sp++; }
+        const int ci = T[nd].first + c;
+        const uint64_t cd = node_dist(T[ci], t);
+        if (cd > best) continue;
+        if (T[ci].count == 0) {
+            if (cd < best) { best = cd; res = ci; cnt = 1; }
+            else if (cnt < 2) cnt++;
+        } else if (sp < 10) {
+            stk_node[sp] = ci; stk_next[sp] = 0; sp++;
         }
     }
-    return cnt;
+    tied = cnt >= 2;
+    return res;
 }
-
 /* (long)(v * 10000f) */
 __device__ __forceinline__ int32_t quantize(float v) { return (int32_t)(int64_t)(v * 10000.0f); }
 

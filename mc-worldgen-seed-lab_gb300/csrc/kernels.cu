@@ -211,15 +211,18 @@ __global__ void __launch_bounds__(128) k_grid(const __grid_constant__ MgWorldDes
     int32_t tg[6];
     cell_target<FM, DIM>(W, *S, T, qx0 + ix, qy, qz0 + iz, tg);
     uint64_t d;
-    int leaf = tree_search(tree, tg, -1, d);
-    out[g] = tree[leaf].biome;
     if (CHAIN) {
+        bool tied;
+        const int leaf = tree_search_tie(tree, tg, d, tied);
+        out[g] = tree[leaf].biome;
         ChainRec r;
         for (int k = 0; k < 6; k++) r.tg[k] = tg[k];
         r.d = d;
         r.leaf = leaf;
-        r.tie = tree_count_at(tree, tg, d) >= 2;
+        r.tie = tied;
         rec[g] = r;
+    } else {
+        out[g] = tree[tree_search(tree, tg, -1, d)].biome;
     }
 }
 /* GRID_CHAIN: a tied cell takes the previous cell's leaf when that leaf is also at minimum fitness.

@@ -429,7 +429,8 @@ MCGEN_API void mcgen_gb300_server_free(McGb300Server *s) {
 }
 
 MCGEN_API int mcgen_gb300_server_submit(McGb300Server *s, const McGb300Request *req, uint8_t *out, long long *ticket) {
-    if (!s || !req || !req->world || !ticket || req->nx <= 0 || req->nz <= 0 || (long long)req->nx * req->nz > (1LL << 28))
+    if (!s || !req || !req->world || !out || !ticket || req->nx <= 0 || req->nz <= 0 ||
+        (long long)req->nx * req->nz > (1LL << 28))
         return MCGEN_E_ARG;
     {
         /* the world's tree must be on the device before the worker references it */

@@ -3,6 +3,7 @@
 Each request's ids must be the same whether it is served alone or mixed with concurrent requests from
 several threads (different versions, dimensions, sizes, repeated seeds), and equal to the oracle; a small
 HBM budget must evict (LRU) without changing any result."""
+import ctypes as C
 import threading
 
 import numpy as np
@@ -90,3 +91,31 @@ def test_small_budget_evicts(env):
     st = srv.stats()
     srv.close()
     assert st["cache_evictions"] > 0
+
+
+def test_wait_timeout_and_ticket_rules(env):
+    """A wait that runs out returns MCGEN_E_CANCEL and the ticket stays valid; a ticket is waited for once;
+    unknown tickets and a missing output buffer are refused."""
+    mg, gens, worlds = env
+    srv = mg.Server(hbm_budget_bytes=64 << 20, max_inflight=1)
+    w = worlds[("26.1", "minecraft:overworld")]
+    big = srv.submit(w, 123, -256, -256, 512, 512, 16)   # long enough that a 0 ms wait usually runs out
+    small = srv.submit(w, 124, 0, 0, 8, 8, 16)
+    try:
+        srv.wait(small, 0)
+    except mg.McError as e:
+        assert e.code == mg.MCGEN_E_CANCEL
+    ids, lat = srv.wait(big)
+    exp = O.World(ge.data_root(), "26.1", "overworld").quart_grid(123, -256, -256, 512, 512, 16, O.TIE_ENGINE)
+    assert np.array_equal(ids, exp) and lat > 0
+    if small in srv._keep:
+        ids2, _ = srv.wait(small)
+        assert np.array_equal(ids2, O.World(ge.data_root(), "26.1", "overworld").quart_grid(124, 0, 0, 8, 8, 16, O.TIE_ENGINE))
+    with pytest.raises(mg.McError) as e:
+        srv.wait(big)                                      # already collected
+    assert e.value.code == mg.MCGEN_E_ARG
+    L = mg.load()
+    req = mg.McGb300Request(w.handle, 5, 0, 0, 4, 4, 16)
+    t = C.c_longlong()
+    assert L.mcgen_gb300_server_submit(srv._h, C.byref(req), None, C.byref(t)) == mg.MCGEN_E_ARG
+    srv.close()
