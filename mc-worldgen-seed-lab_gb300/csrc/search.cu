@@ -77,8 +77,7 @@ __global__ void __launch_bounds__(128) k_search_rest(const __grid_constant__ MgW
             obs_cell(o, seed, hs, have, qx, qy, qz);
             bool ok;
             if (DIM == MG_END) {
-                const int cls = end_chunk_class(T->p, FM, (qx * 4) >> 4, (qz * 4) >> 4, W.end_f2, W.end_g2, o.flags & 0xFF);
-                ok = obs_in(o, W.end_ids[cls]);
+                ok = end_accept<FM>(W, T->p, o, qx, qz);
             } else {
                 int32_t tg[6];
                 cell_target<FM, DIM>(W, S, T, qx, qy, qz, tg);

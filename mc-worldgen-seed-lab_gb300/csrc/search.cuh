@@ -104,6 +104,96 @@ __device__ __forceinline__ bool obs_accept(const MgObs &o, const MgTreeNode *__r
     return ((m[0] & o.mask[0]) | (m[1] & o.mask[1])) != 0;
 }
 
+/* The End check of an observation, deciding early (same answer as the full window).
+ * The class of a chunk is a step function of the highest island height h in its window, and h only grows
+ * as islands are visited, so the class only moves up the order small islands < barrens < midlands <
+ * highlands.  The window's cells are visited nearest first; the visit stops when (a) every class still
+ * reachable is in the mask (accept) or none is (reject), or (b) no remaining cell can raise h: a cell at
+ * offset (dx, dz) gives at most 100 - 9 sqrt(lb) with lb <= |offset|^2 (island size >= 9). */
+struct EndOrder {
+    int8_t dx[625], dz[625];
+    uint16_t lb[625]; /* ((2|dx| - 1)+)^2 + ((2|dz| - 1)+)^2, a lower bound of xd^2 + zd^2 */
+};
+constexpr EndOrder make_end_order() {
+    EndOrder t{};
+    int n = 0;
+    for (int dx = -12; dx <= 12; dx++)
+        for (int dz = -12; dz <= 12; dz++) {
+            const int ax = dx < 0 ? -dx : dx, az = dz < 0 ? -dz : dz;
+            const int bx = 2 * ax - 1 > 0 ? 2 * ax - 1 : 0, bz = 2 * az - 1 > 0 ? 2 * az - 1 : 0;
+            t.dx[n] = (int8_t)dx;
+            t.dz[n] = (int8_t)dz;
+            t.lb[n] = (uint16_t)(bx * bx + bz * bz);
+            n++;
+        }
+    for (int i = 1; i < 625; i++) /* insertion sort by lb (stable) */
+        for (int j = i; j > 0 && t.lb[j - 1] > t.lb[j]; j--) {
+            const int8_t a = t.dx[j], b = t.dz[j];
+            const uint16_t c = t.lb[j];
+            t.dx[j] = t.dx[j - 1]; t.dz[j] = t.dz[j - 1]; t.lb[j] = t.lb[j - 1];
+            t.dx[j - 1] = a; t.dz[j - 1] = b; t.lb[j - 1] = c;
+        }
+    return t;
+}
+static __constant__ EndOrder kEndOrder = make_end_order();
+
+/* class rank 0..3 (small islands, barrens, midlands, highlands) of a chunk outside the central disc */
+__device__ __forceinline__ int end_rank(double e) {
+    return e > 0.25 ? 3 : (e >= -0.0625 ? 2 : (e < -0.21875 ? 0 : 1));
+}
+template <bool FM>
+__device__ __forceinline__ bool end_accept(const MgWorldDesc &W, const uint8_t *__restrict__ p, const MgObs &o, int qx,
+                                           int qz) {
+    const int cx = (qx * 4) >> 4, cz = (qz * 4) >> 4;
+    if ((long long)cx * cx + (long long)cz * cz <= 4096LL) return obs_in(o, W.end_ids[0]);
+    const int rad = o.flags & 0xFF;
+    /* rank k -> class id: small islands, barrens, midlands, highlands */
+    const int cls_of_rank[4] = {W.end_ids[3], W.end_ids[4], W.end_ids[2], W.end_ids[1]};
+    bool in[4];
+    for (int k = 0; k < 4; k++) in[k] = obs_in(o, cls_of_rank[k]);
+    const int bx = (cx * 2 + 1) * 8, bz = (cz * 2 + 1) * 8;
+    const int sx = bx / 8, sz = bz / 8;
+    const int ccx = sx / 2, ccz = sz / 2, ox = sx % 2, oz = sz % 2;
+    float best;
+    float cdist = 0.0f;
+    if (!FM) {
+        int32_t sq = (int32_t)((uint32_t)sx * (uint32_t)sx + (uint32_t)sz * (uint32_t)sz);
+        float len = (float)sqrt((double)(float)sq);
+        best = clampf(100.0f - len * 8.0f, -100.0f, 80.0f);
+    } else {
+        best = -100.0f;
+        const float ddx = (float)(0 - bx), ddz = (float)(0 - bz);
+        const float len = (float)sqrt((double)(ddx * ddx + 0.0f * 0.0f + ddz * ddz));
+        cdist = (clampf(100.0f - len, -100.0f, 80.0f) - 8.0f) * 0.0078125f;
+    }
+    auto rank_now = [&]() {
+        if (!FM) return end_rank(((double)best - 8.0) / 128.0);
+        const float o2 = (best - 8.0f) / 128.0f;
+        return end_rank((double)(cdist > o2 ? cdist : o2));
+    };
+    for (int i = 0; i < 625; i++) {
+        int r = rank_now();
+        bool any = false, all = true;
+        for (int k = r; k < 4; k++) { any |= in[k]; all &= in[k]; }
+        if (all) return true;
+        if (!any) return false;
+        const int lb = kEndOrder.lb[i];
+        if (100.0f - 9.0f * sqrtf((float)lb) <= best) break; /* nothing left can raise h */
+        const int dx = kEndOrder.dx[i], dz = kEndOrder.dz[i];
+        if (dx < -rad || dx > rad || dz < -rad || dz > rad) continue;
+        const long long tx = (long long)ccx + dx, tz = (long long)ccz + dz;
+        if (tx * tx + tz * tz <= 4096LL) continue;
+        const double nv = simplex2(p, (double)tx, (double)tz, W.end_f2, W.end_g2);
+        const bool island = FM ? ((float)nv < -0.9f) : (nv < (double)-0.9f);
+        if (!island) continue;
+        const float size = fmodf(fabsf((float)tx) * 3439.0f + fabsf((float)tz) * 147.0f, 13.0f) + 9.0f;
+        const float xd = (float)(ox - dx * 2), zd = (float)(oz - dz * 2);
+        const float h = clampf(100.0f - (float)sqrt((double)(xd * xd + zd * zd)) * size, -100.0f, 80.0f);
+        best = best > h ? best : h;
+    }
+    return in[rank_now()];
+}
+
 /* candidate i of a source: 0 list, 1 structure seed base | i << 48, 2 base + i */
 __device__ __forceinline__ int64_t search_seed(int kind, const int64_t *__restrict__ list, uint64_t base, uint64_t i) {
     if (kind == 0) return list[i];
