@@ -627,20 +627,25 @@ def serve_run(mg, worlds, stream, budget: int, max_inflight: int = 2):
 SEARCH_SEED = 8675309
 
 
+def search_fixture_rows():
+    """(qx, qy, qz, [biome names]) of the reference's known-answer file for seed 8675309 (a test fixture)."""
+    rows = []
+    path = os.path.join(REPO, "tests", "golden", "search", f"example_obs_26.3_overworld_seed{SEARCH_SEED}.txt")
+    for ln in open(path):
+        if ln.startswith("#") or not ln.strip():
+            continue
+        x, y, z, b = ln.split()
+        rows.append((int(x), int(y), int(z), b.split("|")))
+    return rows
+
+
 def search_observations(mg, ge, version: str, dim: str):
     """Observations of seed 8675309: the reference's 8-cell Overworld 26.3 known-answer file (committed as a
     fixture) for the Overworld; for the Nether and the End, 8 cells at SplitMix64(5) positions in
     [-5000, 5000) quarts with the biomes this library computes for that seed."""
     if dim == "minecraft:overworld":
-        rows = []
-        path = os.path.join(REPO, "tests", "golden", "search", f"example_obs_26.3_overworld_seed{SEARCH_SEED}.txt")
         names = {n: i for i, n in enumerate(mg.Generator.open(ge.data_root(), version).biome_names())}
-        for ln in open(path):
-            if ln.startswith("#") or not ln.strip():
-                continue
-            x, y, z, b = ln.split()
-            rows.append((int(x), int(y), int(z), [names[n] for n in b.split("|")]))
-        return mg.make_obs(rows)
+        return mg.make_obs([(x, y, z, [names[n] for n in b]) for x, y, z, b in search_fixture_rows()])
     r = splitmix64(5, 16)
     pts = (-5000 + (r % np.uint64(10000)).astype(np.int64)).reshape(8, 2)
     q = np.stack([pts[:, 0], np.full(8, 16), pts[:, 1]], 1).astype(np.int32)
@@ -709,7 +714,7 @@ def cpu_baseline_search(mg, ge, budget_s: float) -> dict:
     from oracle import oracle as O
 
     cores = os.cpu_count() or 1
-    obs = search_observations(mg, ge, "26.3", "minecraft:overworld")
+    obs = O.make_obs([(x, y, z, [O.lib().or_biome_id(n.encode()) for n in b]) for x, y, z, b in search_fixture_rows()])
     w = O.World(ge.data_root(), "26.3", "overworld")
     n = 1 << 14
     while True:
@@ -931,6 +936,14 @@ def run_reference(args, rank, world):
         sample = f"first {nfirst} of the 4096 seeds, Nether and End 64x64 grids per step"
         config = {"workload": "other dimensions 26.3: 4096 SplitMix64(2) seeds x 64x64 quart grid at y=64, "
                               "Nether and End"}
+    elif args.workload == "search":
+        obs = O.make_obs([(x, y, z, [O.lib().or_biome_id(n.encode()) for n in b]) for x, y, z, b in search_fixture_rows()])
+        ncand = 1 << 18
+        per_step = lambda: w.search(obs, O.SEEDS_RANGE, base=SEARCH_SEED - ncand // 2, n=ncand, threads=cores)  # noqa: E731
+        samples = ncand
+        sample = f"{ncand} candidates around 8675309 per step, candidates over threads"
+        config = {"workload": "seed search: candidates x 8 observations of seed 8675309 (the reference's known-answer "
+                              "cells), Overworld 26.3, ties mode"}
     else:
         rows = 32
         per_step = lambda: w.biome_grid(12345, -512, -512, 256, rows, 4, 64, threads=cores)  # noqa: E731
@@ -938,6 +951,8 @@ def run_reference(args, rank, world):
         sample = f"{rows} of 256 grid rows per step"
         config = {"workload": "Overworld 26.3 normal, seed 12345, biome grid 256x256 step 4 y=64",
                   "version": "26.3", "dimension": "overworld"}
+    metric, unit = (("biome seed search candidates/sec", "candidates/s") if args.workload == "search"
+                    else (METRIC, UNIT))
     for _ in range(args.warmup):
         per_step()
     t0 = time.perf_counter()
@@ -945,12 +960,12 @@ def run_reference(args, rank, world):
         per_step()
     dt = time.perf_counter() - t0
     value = samples * args.steps / dt
-    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+    out = {"impl": "reference", "metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32+f64+int64", "data": "synthetic (SplitMix64 seeds and points)",
            "config": config,
-           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
-           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "cpu_baseline": {"value": value, "unit": unit, "cores": cores, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
 
