@@ -262,6 +262,8 @@ def run_gb300(args, rank, world, local_rank):
         return run_dims(args, rank, world, local_rank, mg, ge)
     elif args.workload == "search":
         return run_search(args, rank, world, local_rank, mg, ge)
+    elif args.workload == "map2048":
+        return run_map(args, rank, world, local_rank, mg, ge)
     else:
         w = gen.world("minecraft:overworld", "normal", 12345)
         nx = nz = 256
@@ -728,6 +730,84 @@ def cpu_baseline_search(mg, ge, budget_s: float) -> dict:
             "sample": f"{n} candidates around 8675309 ({dt:.2f} s)"}
 
 
+# The reference's published GPU biome-map times on an RTX 4080 SUPER, 2048 x 2048 cells at step 4 around the
+# origin, seed 12345, y = 64, result copied to the host included (docs/blender/gpu.md:116-121, measured with
+# libmcgen/tests/g9_bench.c:46-54): seconds per (version, dimension).
+MAP2048_PUBLISHED_S = {
+    ("26.1", "overworld"): 0.120, ("26.1", "the_nether"): 0.023, ("26.1", "the_end"): 0.079,
+    ("26.2", "overworld"): 0.119, ("26.2", "the_nether"): 0.023, ("26.2", "the_end"): 0.074,
+    ("26.3", "overworld"): 0.053, ("26.3", "the_nether"): 0.009, ("26.3", "the_end"): 0.074,
+    ("26.4-snapshot-2", "overworld"): 0.045, ("26.4-snapshot-2", "the_nether"): 0.009,
+    ("26.4-snapshot-2", "the_end"): 0.083}
+
+
+def run_map(args, rank, world, local_rank, mg, ge):
+    """The drop-in biome map: mcgen_gpu_biome_grid(w, -4096, -4096, 2048, 2048, 4, 64, host out) for seed
+    12345, every version and dimension (BiomeManager zoom + chunk-cell ties, ids copied to the host), the
+    reference's own GPU benchmark shape; best of --steps calls after --warmup."""
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    n, step, x0 = 2048, 4, -2048 * 4 // 2
+    L = mg.load()
+    h_out = torch.empty(n * n, dtype=torch.uint8).pin_memory()
+    ptr = h_out.data_ptr()
+    res = {}
+    launches0 = mg.launch_count()
+    with ClockSampler(local_rank) as clk:
+        for (v, d), pub in MAP2048_PUBLISHED_S.items():
+            w = mg.Generator.open(ge.data_root(), v).world("minecraft:" + d, "normal", 12345)
+            best = 1e30
+            for i in range(args.warmup + args.steps):
+                t0 = time.perf_counter()
+                rc = L.mcgen_gpu_biome_grid(w.handle, x0, x0, n, n, step, 64, ptr)
+                dt = time.perf_counter() - t0
+                if rc:
+                    raise mg.McError(rc, "mcgen_gpu_biome_grid failed")
+                if i >= args.warmup:
+                    best = min(best, dt)
+            res[f"{v} {d}"] = {"s": round(best, 5), "cells_per_s": n * n / best, "published_4080_s": pub,
+                               "speedup_vs_published": round(pub / best, 2)}
+    top = res["26.3 overworld"]
+    out = {"metric": "biome map cells/sec (mcgen_gpu_biome_grid, ids on the host)", "value": top["cells_per_s"],
+           "unit": "cells/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": top["s"] * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": round(top["cells_per_s"] / (n * n / MAP2048_PUBLISHED_S[("26.3", "overworld")]), 3),
+           "dtype": "f32+f64+int64", "data": "seed 12345, the reference benchmark's map",
+           "config": {"workload": "drop-in biome map 2048 x 2048 cells, x,z in [-4096, 4096) step 4, y=64, seed 12345, "
+                                  "zoom + chunk-cell ties, ids copied to pinned host memory; best of steps; "
+                                  "vs_baseline against the reference's RTX 4080 SUPER time for Overworld 26.3",
+                      "cases": res},
+           "e2e": {"value": top["cells_per_s"], "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": n * n},
+           "gpu_launches": int(mg.launch_count() - launches0)}
+    clocks = clk.summary()
+    if clocks:
+        out["clocks"] = clocks
+    if rank == 0:
+        if not args.skip_extras:
+            out["cpu_baseline"] = cpu_baseline_map(args.cpu_sample_s)
+        print(json.dumps(out), flush=True)
+
+
+def cpu_baseline_map(budget_s: float) -> dict:
+    """The oracle's biome map (Overworld 26.3) on all host cores over the first rows of the same map."""
+    import __graft_entry__ as ge
+    from oracle import oracle as O
+
+    cores = os.cpu_count() or 1
+    w = O.World(ge.data_root(), "26.3", "overworld")
+    rows = 8
+    while True:
+        t0 = time.perf_counter()
+        w.biome_grid(12345, -4096, -4096, 2048, rows, 4, 64, threads=cores)
+        dt = time.perf_counter() - t0
+        if dt > budget_s / 4 or rows >= 2048:
+            break
+        rows = min(2048, rows * 4)
+    return {"value": 2048 * rows / dt, "unit": "cells/s", "cores": cores, "kind": "port",
+            "sample": f"{rows} of the 2048 map rows ({dt:.2f} s), rows over threads"}
+
+
 def run_dims(args, rank, world, local_rank, mg, ge):
     """Other dimensions: 4,096 SplitMix64(2) seeds, a 64 x 64 quart grid at y=64 per seed, Nether 26.3 and
     End 26.3, each dimension one batched launch (plan + graph) of 4,096 requests."""
@@ -975,7 +1055,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["seeds8", "grid256", "batch10k", "serve", "dims4096", "search"],
+    ap.add_argument("--workload", choices=["seeds8", "grid256", "batch10k", "serve", "dims4096", "search", "map2048"],
                     default="batch10k")
     ap.add_argument("--search-candidates", type=int, default=1 << 26, help="search: candidates per step")
     ap.add_argument("--rates", default="500,1000,2000", help="serve: arrival rates (requests/s)")

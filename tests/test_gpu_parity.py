@@ -212,3 +212,15 @@ def test_chunk_mode_grid_hashes(gens, mg):
     got = w.quart_grid(-301, 129, 203, 97, 16, mg.TIE_CHUNK_ORDER)
     exp = O.World(ge.data_root(), "26.3", "overworld").chunk_order_grid(777, -301, 129, 203, 97, 16)
     assert np.array_equal(got, exp)
+
+
+@pytest.mark.parametrize("version,dim", [("26.3", "overworld"), ("26.1", "the_end"), ("26.4-snapshot-2", "the_nether")])
+def test_map2048_rows(gens, version, dim):
+    """The reference's GPU map benchmark shape (2048 x 2048 cells, x,z from -4096 step 4, y=64, seed 12345):
+    the whole map on the GPU, rows at the edges and the middle against the oracle."""
+    w = gens[version].world("minecraft:" + dim, "normal", 12345)
+    got = w.biome_grid(-4096, -4096, 2048, 2048, 4, 64)
+    ow = O.World(ge.data_root(), version, dim)
+    for r in (0, 1023, 2047):
+        exp = ow.biome_grid(12345, -4096, -4096 + 4 * r, 2048, 1, 4, 64)
+        assert np.array_equal(got[r:r + 1], exp), (r, int((got[r:r + 1] != exp).sum()))
