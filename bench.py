@@ -846,12 +846,12 @@ def run_dims(args, rank, world, local_rank, mg, ge):
                 kern[f"{dim.split(':')[1]}:{k}"] = {"ms_total": round(v[0], 4), "launches": v[1]}
             # end to end: a plan from the host request list, run into pinned host memory, freed -- per step
             h_out = torch.empty(plan.output_bytes, dtype=torch.uint8).pin_memory().numpy()
-            reqs = [(w, int(s), int(qx), int(qz), 64, 64, 16) for s, (qx, qz) in zip(seeds, origins)]
+            seeds_np, qx_np, qz_np = seeds, origins[:, 0], origins[:, 1]
             e2e_steps = 0 if args.skip_extras else min(args.steps, 5)
             t0 = time.perf_counter()
             h2d = 0
             for _ in range(e2e_steps):
-                p = mg.Plan(reqs)
+                p = mg.Plan(mg.RequestArray(w, seeds_np, qx_np, qz_np, 64, 64, 16))
                 p.shape = plan.shape
                 p.run(h_out)
                 h2d = p.h2d_bytes
@@ -874,7 +874,8 @@ def run_dims(args, rank, world, local_rank, mg, ge):
     if not args.skip_extras:
         out["e2e"] = {"value": total_samples * world / total_e2e_s, "unit": UNIT, "h2d_bytes_per_step": total_h2d,
                       "d2h_bytes_per_step": int(total_samples),
-                      "call": "Plan(requests) + plan_run(host buffer) + plan_free per dimension per step"}
+                      "call": "Plan(RequestArray(world, seeds, corners, 64, 64, 16)) + plan_run(host buffer) + "
+                              "plan_free per dimension per step"}
     clocks = clk.summary()
     if clocks:
         out["clocks"] = clocks

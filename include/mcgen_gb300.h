@@ -172,6 +172,11 @@ MCGEN_API int mcgen_gb300_check_split(long long n, unsigned long long seed, long
  * units of 2^-52) against the plain double octave: n random (permutation, fractions) cases; *bad counts
  * results that differ as doubles. */
 MCGEN_API int mcgen_gb300_check_octave(long long n, unsigned long long seed, long long *bad);
+/* Device self-check of BiomeManager's zoom choice (single-precision screen, double precision only for
+ * candidates within its error margin) against the double-precision first minimum of all 8 candidates:
+ * n random (zoom seed, block) cases; *bad counts different choices, *screened_out the cases that needed the
+ * double-precision comparison. */
+MCGEN_API int mcgen_gb300_check_zoom(long long n, unsigned long long seed, long long *bad, long long *screened_out);
 
 /* Pipe microbenchmarks on the current device, in giga-operations per second:
  * 0 FP32 FMA, 1 FP64 FMA, 2 FP64 add, 3 int32 multiply-add, 4 double->int floor conversion,

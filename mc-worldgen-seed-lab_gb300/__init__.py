@@ -91,6 +91,8 @@ _PROTOS = {
                                            C.POINTER(C.c_longlong)]),
     "mcgen_gb300_pipe_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
     "mcgen_gb300_check_octave": (C.c_int, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]),
+    "mcgen_gb300_check_zoom": (C.c_int, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong),
+                                         C.POINTER(C.c_longlong)]),
     "mcgen_gb300_search": (C.c_int, [_P, C.c_int, _P, C.c_uint64, C.c_uint64, _P, C.c_int, C.c_int, _P, C.c_uint32,
                                      C.POINTER(C.c_uint32), _P, C.POINTER(C.c_double)]),
     "mcgen_gb300_obs_end_radius": (C.c_int, [_P, _P]),
@@ -130,6 +132,12 @@ class McGb300ServerStats(C.Structure):
 class McGb300Request(C.Structure):
     _fields_ = [("world", _P), ("seed", C.c_int64), ("qx0", C.c_int32), ("qz0", C.c_int32), ("nx", C.c_int32),
                 ("nz", C.c_int32), ("qy", C.c_int32)]
+
+
+# McGb300Request as a numpy record, for building request lists without a per-request ctypes object
+REQUEST_DTYPE = np.dtype([("world", np.uint64), ("seed", np.int64), ("qx0", np.int32), ("qz0", np.int32),
+                          ("nx", np.int32), ("nz", np.int32), ("qy", np.int32)], align=True)
+assert REQUEST_DTYPE.itemsize == C.sizeof(McGb300Request)
 
 
 _lib = None
@@ -214,6 +222,13 @@ def check_octave(n: int, seed: int = 1) -> int:
     b = C.c_longlong()
     _check(load().mcgen_gb300_check_octave(n, seed, C.byref(b)), "mcgen_gb300_check_octave")
     return b.value
+
+
+def check_zoom(n: int, seed: int = 1) -> tuple[int, int]:
+    """(mismatches, cases decided in double precision) of the screened zoom choice against the plain one."""
+    b, c = C.c_longlong(), C.c_longlong()
+    _check(load().mcgen_gb300_check_zoom(n, seed, C.byref(b), C.byref(c)), "mcgen_gb300_check_zoom")
+    return b.value, c.value
 
 
 def pipe_rate(pipe: str) -> float:
@@ -429,21 +444,82 @@ class World:
                "mcgen_gb300_quart_grid_dev")
 
 
+class RequestArray:
+    """Requests as one McGb300Request record array: `worlds` (one World or a sequence, one per request),
+    seeds and corners as arrays.  The records hold the worlds' handles; the object keeps the worlds alive."""
+
+    def __init__(self, worlds, seeds, qx0, qz0, nx, nz, qy=16):
+        seeds = np.asarray(seeds)
+        n = len(seeds)
+        rec = np.zeros(n, REQUEST_DTYPE)
+        if isinstance(worlds, World):
+            self.worlds = [worlds]
+            rec["world"] = _handle_int(worlds)
+        else:
+            self.worlds = list(worlds)
+            if len(self.worlds) != n:
+                raise ValueError("one world per request")
+            rec["world"] = np.array([_handle_int(w) for w in self.worlds], np.uint64)
+        rec["seed"] = seeds.astype(np.uint64).view(np.int64) if seeds.dtype == np.uint64 else seeds.astype(np.int64)
+        for name, v in (("qx0", qx0), ("qz0", qz0), ("nx", nx), ("nz", nz), ("qy", qy)):
+            v = np.broadcast_to(np.asarray(v, np.int64), (n,))
+            if v.size and (v.min() < -2**31 or v.max() >= 2**31):
+                raise ValueError(f"{name} out of int32 range")
+            rec[name] = v
+        self.records = rec
+
+    def __len__(self):
+        return len(self.records)
+
+
+def _handle_int(w) -> int:
+    """A world's McWorld* as an integer (0 for a closed world, which the library rejects with E_ARG)."""
+    h = w.handle
+    return (h.value or 0) if h is not None else 0
+
+
+def _pack_requests(requests):
+    """[(world, seed, qx0, qz0, nx, nz, qy), ...] -> (record array, worlds)."""
+    n = len(requests)
+    rec = np.zeros(n, REQUEST_DTYPE)
+    if n == 0:
+        return rec, []
+    cols = list(zip(*requests))
+    if len(cols) != 7:
+        raise ValueError("a request is (world, seed, qx0, qz0, nx, nz, qy)")
+    worlds = list(cols[0])
+    handles = {}
+    for w in worlds:
+        if id(w) not in handles:
+            handles[id(w)] = _handle_int(w)
+    rec["world"] = np.fromiter((handles[id(w)] for w in worlds), np.uint64, n)
+    try:
+        rec["seed"] = np.array(cols[1], np.int64)
+    except OverflowError:  # seeds given as unsigned 64-bit values
+        rec["seed"] = np.fromiter((int(v) & 0xFFFFFFFFFFFFFFFF for v in cols[1]), np.uint64, n).view(np.int64)
+    for j, name in enumerate(("qx0", "qz0", "nx", "nz", "qy")):
+        v = np.array(cols[2 + j], np.int64)
+        if v.min() < -2**31 or v.max() >= 2**31:
+            raise ValueError(f"{name} out of int32 range")
+        rec[name] = v
+    return rec, worlds
+
+
 class Plan:
     """A frozen batch of quart-grid requests (mcgen_gb300_plan_*): [(world, seed, qx0, qz0, nx, nz, qy), ...]."""
 
     def __init__(self, requests, tie_rule: int = TIE_ENGINE):
         L = load()
-        arr = (McGb300Request * len(requests))()
-        self._worlds = []
-        for i, (w, seed, qx0, qz0, nx, nz, qy) in enumerate(requests):
-            arr[i] = McGb300Request(w.handle, int(seed), qx0, qz0, nx, nz, qy)
-            self._worlds.append(w)
+        if isinstance(requests, RequestArray):
+            arr, self._worlds = requests.records, list(requests.worlds)
+        else:
+            arr, self._worlds = _pack_requests(requests)
         h = _P()
-        _check(L.mcgen_gb300_plan_new(arr, len(requests), tie_rule, C.byref(h)), "mcgen_gb300_plan_new")
+        _check(L.mcgen_gb300_plan_new(arr.ctypes.data if len(arr) else None, len(arr), tie_rule, C.byref(h)),
+               "mcgen_gb300_plan_new")
         self._h = h
-        self.n = len(requests)
-        self.shapes = [(r[4], r[5]) for r in requests]
+        self.n = len(arr)
+        self.shapes = list(zip(arr["nx"].tolist(), arr["nz"].tolist()))
 
     def close(self):
         if self._h:

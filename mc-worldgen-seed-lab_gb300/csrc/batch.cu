@@ -291,13 +291,19 @@ static int prepare_t(int shape, int sms) {
 }
 /* kernel attributes (before any capture) and resident CTAs per SM of shape 0 */
 int batch_prepare(int *ctas_per_sm) {
+    static int prepared_dev = -1; /* the attributes are per device and set once (callers hold the ABI lock) */
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (prepared_dev == dev) {
+        if (ctas_per_sm) *ctas_per_sm = g_resident[0] / (sms > 0 ? sms : 1);
+        return 0;
+    }
     int rc = prepare_t<32, 8>(0, sms);
     if (!rc) rc = prepare_t<8, 4>(1, sms);
     if (!rc) rc = prepare_t<8, 6>(2, sms);
     if (!rc) rc = prepare_t<8, 8>(3, sms);
+    if (!rc) prepared_dev = dev;
     if (ctas_per_sm) *ctas_per_sm = g_resident[0] / (sms > 0 ? sms : 1);
     return rc;
 }

@@ -176,37 +176,81 @@ __device__ __forceinline__ int64_t zoom_step(int64_t r, int64_t c) {
     v *= v * 6364136223846793005ULL + 1442695040888963407ULL;
     return (int64_t)(v + (uint64_t)c);
 }
-/* Math.floorMod(r >> 24, 1024) / 1024.0: the low ten bits, and the division by 2^10 is exact as a scaling */
-__device__ __forceinline__ double zoom_jitter(int64_t r) {
-    const int m = (int)((r >> 24) & 1023);
-    return ((double)m * 0x1.0p-10 - 0.5) * 0.9;
-}
-__device__ __forceinline__ double zoom_dist(int64_t seed, int x, int y, int z, double dx, double dy, double dz) {
+/* Math.floorMod(r >> 24, 1024) / 1024.0: the ten bits above bit 23; the division by 2^10 is exact as a scaling */
+__device__ __forceinline__ int zoom_bits(int64_t r) { return (int)((r >> 24) & 1023); }
+__device__ __forceinline__ double zoom_jitter(int m) { return ((double)m * 0x1.0p-10 - 0.5) * 0.9; }
+/* the three jitter draws of candidate cell (x, y, z), ten bits each (x in bits 0-9, y 10-19, z 20-29) */
+__device__ __forceinline__ uint32_t zoom_draws(int64_t seed, int x, int y, int z) {
     int64_t r = seed;
     r = zoom_step(r, x); r = zoom_step(r, y); r = zoom_step(r, z);
     r = zoom_step(r, x); r = zoom_step(r, y); r = zoom_step(r, z);
-    double jx = zoom_jitter(r);
+    uint32_t m = (uint32_t)zoom_bits(r);
     r = zoom_step(r, seed);
-    double jy = zoom_jitter(r);
+    m |= (uint32_t)zoom_bits(r) << 10;
     r = zoom_step(r, seed);
-    double jz = zoom_jitter(r);
+    return m | (uint32_t)zoom_bits(r) << 20;
+}
+/* the fiddled distance in double, in the reference's order (z, y, x terms) */
+__device__ __forceinline__ double zoom_dist_d(uint32_t m, double dx, double dy, double dz) {
+    const double jx = zoom_jitter((int)(m & 1023)), jy = zoom_jitter((int)((m >> 10) & 1023)),
+                 jz = zoom_jitter((int)(m >> 20));
     return (dz + jz) * (dz + jz) + (dy + jy) * (dy + jy) + (dx + jx) * (dx + jx);
 }
-__device__ __forceinline__ void zoom_cell(int64_t zseed, int x, int y, int z, int &cx, int &cy, int &cz) {
-    int ax = x - 2, ay = y - 2, az = z - 2;
-    int px = ax >> 2, py = ay >> 2, pz = az >> 2;
-    double fx = (ax & 3) / 4.0, fy = (ay & 3) / 4.0, fz = (az & 3) / 4.0;
-    int best = 0;
-    double bd = __longlong_as_double(0x7FF0000000000000LL);
+/* The same in single precision, as a screen.  Against the double value it differs by at most 1.23e-6: each
+ * of the three squared terms by at most 2.48e-7 (the maximum over all 8 x 1024 (offset, draw) pairs, the
+ * draw's jitter taken as (m - 512) * fl32(0.9 / 1024)), and the two single-precision additions of terms below
+ * 6.31 by half an ulp (2^-22) each.  So a candidate whose screened distance exceeds the smallest screened one
+ * by more than ZOOM_MARGIN (four times twice that bound) cannot be the double-precision minimum. */
+#define ZOOM_MARGIN 1e-5f
+__device__ __forceinline__ float zoom_dist_f(uint32_t m, int qx, int qy, int qz) {
+    const float c = 0.9f / 1024.0f;
+    const float ux = (float)qx * 0.25f + (float)((int)(m & 1023) - 512) * c;
+    const float uy = (float)qy * 0.25f + (float)((int)((m >> 10) & 1023) - 512) * c;
+    const float uz = (float)qz * 0.25f + (float)((int)(m >> 20) - 512) * c;
+    return uz * uz + uy * uy + ux * ux;
+}
+/* BiomeManager.getBiome's choice among the 8 quart cells around block (x, y, z): the first candidate (in the
+ * order x, y, z bit = 0 first) with the smallest double-precision fiddled distance.  The distances are
+ * screened in single precision; only when a second candidate lies within ZOOM_MARGIN of the smallest are the
+ * close candidates' distances taken in double precision (in candidate order, strict comparison), which
+ * gives the same choice as the double-precision comparison of all 8. */
+__device__ __forceinline__ int zoom_pick(int64_t zseed, int px, int py, int pz, int fx, int fy, int fz, int &close) {
+    uint32_t mm[8];
+    float df[8];
+    float bf = __int_as_float(0x7F800000);
+#pragma unroll
     for (int i = 0; i < 8; i++) {
-        bool ex = (i & 4) == 0, ey = (i & 2) == 0, ez = (i & 1) == 0;
-        double d = zoom_dist(zseed, ex ? px : px + 1, ey ? py : py + 1, ez ? pz : pz + 1, ex ? fx : fx - 1.0,
-                             ey ? fy : fy - 1.0, ez ? fz : fz - 1.0);
-        if (bd > d) { best = i; bd = d; }
+        const int ox = (i >> 2) & 1, oy = (i >> 1) & 1, oz = i & 1;
+        mm[i] = zoom_draws(zseed, px + ox, py + oy, pz + oz);
+        df[i] = zoom_dist_f(mm[i], fx - 4 * ox, fy - 4 * oy, fz - 4 * oz);
+        bf = fminf(bf, df[i]);
     }
-    cx = (best & 4) == 0 ? px : px + 1;
-    cy = (best & 2) == 0 ? py : py + 1;
-    cz = (best & 1) == 0 ? pz : pz + 1;
+    const float lim = bf + ZOOM_MARGIN;
+    int best = -1;
+    close = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+        if (df[i] <= lim) { close++; if (best < 0) best = i; }
+    if (close > 1) {
+        double bd = __longlong_as_double(0x7FF0000000000000LL);
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            if (df[i] > lim) continue;
+            const int ox = (i >> 2) & 1, oy = (i >> 1) & 1, oz = i & 1;
+            const double d = zoom_dist_d(mm[i], fx * 0.25 - ox, fy * 0.25 - oy, fz * 0.25 - oz);
+            if (bd > d) { best = i; bd = d; }
+        }
+    }
+    return best;
+}
+__device__ __forceinline__ void zoom_cell(int64_t zseed, int x, int y, int z, int &cx, int &cy, int &cz) {
+    const int ax = x - 2, ay = y - 2, az = z - 2;
+    const int px = ax >> 2, py = ay >> 2, pz = az >> 2;
+    int close;
+    const int best = zoom_pick(zseed, px, py, pz, ax & 3, ay & 3, az & 3, close);
+    cx = px + ((best >> 2) & 1);
+    cy = py + ((best >> 1) & 1);
+    cz = pz + (best & 1);
 }
 /* world_biome_cell (libmcgen/src/biome.c:87-114): y clamped into the dimension; a tied cell walks back along
  * LevelChunkSection.fillBiomesFromNoise order (sections bottom-up, then x, y, z) to an untied cell or the

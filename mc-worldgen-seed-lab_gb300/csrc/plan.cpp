@@ -29,7 +29,8 @@ struct McGb300Plan {
     std::vector<long long> cells;
     int shape = 0;
     int ctas = 0;
-    /* device */
+    /* device: one allocation (d_arena) holds the lists, the lattice pool and the tile counter */
+    void *d_arena = nullptr;
     MgWorldDesc *d_worlds = nullptr;
     const MgTreeNode **d_trees = nullptr;
     MgBatchReq *d_reqs[BATCH_SHAPES] = {nullptr, nullptr, nullptr, nullptr};
@@ -63,13 +64,7 @@ int enqueue(McGb300Plan *p, uint8_t *d_out, int shape, cudaStream_t st) {
 void free_plan(McGb300Plan *p) {
     if (p->exec) cudaGraphExecDestroy(p->exec);
     if (p->cap) cudaStreamDestroy(p->cap);
-    cudaFree(p->d_worlds);
-    cudaFree((void *)p->d_trees);
-    for (auto *r : p->d_reqs) cudaFree(r);
-    for (auto *e : p->d_ent) cudaFree(e);
-    cudaFree(p->d_first);
-    cudaFree(p->d_pool);
-    cudaFree(p->d_counter);
+    cudaFree(p->d_arena);
     delete p;
 }
 
@@ -161,26 +156,42 @@ MCGEN_API int mcgen_gb300_plan_new(const McGb300Request *reqs, int n, int tie_ru
         }
         p->ntiles[s] = tiles;
     }
-    /* device copies */
-    cudaError_t e = cudaSuccess;
+    /* device copies: the lists are staged back to back (256-byte aligned) and uploaded in one copy; the
+     * lattice pool and the tile counter follow them in the same allocation */
     std::vector<MgWorldDesc> wd;
     std::vector<const MgTreeNode *> tp;
     for (auto *w : worlds) { wd.push_back(w->desc); tp.push_back(w->d_tree); }
-    auto up = [&](void **dst, const void *src, size_t bytes) {
-        if (e || !bytes) return;
-        if ((e = cudaMalloc(dst, bytes)) == cudaSuccess) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
-        p->h2d_bytes += (long long)bytes;
+    struct Part { void **dst; const void *src; size_t bytes, off; };
+    std::vector<Part> parts;
+    size_t at = 0;
+    auto place = [&](void **dst, const void *src, size_t bytes) {
+        if (!bytes) return;
+        at = (at + 255) & ~(size_t)255;
+        parts.push_back({dst, src, bytes, at});
+        at += bytes;
     };
-    up((void **)&p->d_worlds, wd.data(), sizeof(MgWorldDesc) * wd.size());
-    up((void **)&p->d_trees, tp.data(), sizeof(void *) * tp.size());
-    for (int s = 0; s < BATCH_SHAPES; s++) up((void **)&p->d_reqs[s], rq[s].data(), sizeof(MgBatchReq) * rq[s].size());
+    place((void **)&p->d_worlds, wd.data(), sizeof(MgWorldDesc) * wd.size());
+    place((void **)&p->d_trees, tp.data(), sizeof(void *) * tp.size());
+    for (int s = 0; s < BATCH_SHAPES; s++) place((void **)&p->d_reqs[s], rq[s].data(), sizeof(MgBatchReq) * rq[s].size());
     for (int d = 0; d < 3; d++) {
         p->nent[d] = (int)ent[d].size();
-        up((void **)&p->d_ent[d], ent[d].data(), sizeof(MgSetupEntry) * ent[d].size());
+        place((void **)&p->d_ent[d], ent[d].data(), sizeof(MgSetupEntry) * ent[d].size());
     }
-    up((void **)&p->d_first, first.data(), sizeof(int) * first.size());
-    if (!e && pool) e = cudaMalloc(&p->d_pool, sizeof(MgLattice) * (size_t)pool);
-    if (!e) e = cudaMalloc(&p->d_counter, sizeof(unsigned long long));
+    place((void **)&p->d_first, first.data(), sizeof(int) * first.size());
+    const size_t staged = at;
+    std::vector<uint8_t> host(staged);
+    for (const Part &q : parts) memcpy(host.data() + q.off, q.src, q.bytes);
+    const size_t pool_off = (at + 255) & ~(size_t)255;
+    const size_t counter_off = pool_off + sizeof(MgLattice) * (size_t)pool;
+    cudaError_t e = cudaMalloc(&p->d_arena, counter_off + sizeof(unsigned long long));
+    if (!e && staged) e = cudaMemcpy(p->d_arena, host.data(), staged, cudaMemcpyHostToDevice);
+    if (!e) {
+        uint8_t *base = (uint8_t *)p->d_arena;
+        for (const Part &q : parts) *q.dst = base + q.off;
+        if (pool) p->d_pool = (MgLattice *)(base + pool_off);
+        p->d_counter = (unsigned long long *)(base + counter_off);
+        p->h2d_bytes = (long long)staged;
+    }
     if (!e) e = (cudaError_t)mg::batch_prepare(nullptr);
     if (e) {
         free_plan(p);

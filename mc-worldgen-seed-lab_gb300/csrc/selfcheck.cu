@@ -4,12 +4,13 @@
  * integer quart coordinates, coordinates plus a float shift, their products with the second-stack factor,
  * tiny and huge values, values whose sum with the offset lands near an integer, in (-1, 0) or on 0, and
  * offsets at 0, near 256 and on integers.  Also: the double branch's fixed-point octave (octave_dfix)
- * against the plain double octave on random permutations and fractions. */
+ * against the plain double octave on random permutations and fractions, and the single-precision screen of
+ * BiomeManager's zoom (zoom_pick) against the double-precision choice among all 8 candidates. */
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "../../include/mcgen.h"
-#include "device.cuh"
+#include "climate.cuh"
 
 using namespace mgd;
 
@@ -111,7 +112,50 @@ __global__ void k_check_octave(long long n, uint64_t seed, unsigned long long *b
     if (b) atomicAdd(bad, b);
 }
 
+/* zoom: random zoom seeds and block positions (|x|, |z| < 2^25, y in [-64, 320)); every case compares the
+ * screened choice with the first strict minimum of the 8 double-precision distances (region.c:61-85) */
+__global__ void k_check_zoom(long long n, uint64_t seed, unsigned long long *out) {
+    unsigned long long bad = 0, close = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const uint64_t r = mix64(seed ^ mix64((uint64_t)i)), r2 = mix64(r);
+        const int64_t zseed = (int64_t)mix64(seed + (uint64_t)(i >> 10)); /* 1024 positions per zoom seed */
+        const int x = (int)(r & 0x3FFFFFF) - (1 << 25), z = (int)((r >> 26) & 0x3FFFFFF) - (1 << 25);
+        const int y = (int)(r2 % 384) - 64;
+        const int ax = x - 2, ay = y - 2, az = z - 2;
+        const int px = ax >> 2, py = ay >> 2, pz = az >> 2;
+        int c;
+        const int got = mg::zoom_pick(zseed, px, py, pz, ax & 3, ay & 3, az & 3, c);
+        close += c > 1;
+        double bd = __longlong_as_double(0x7FF0000000000000LL);
+        int want = 0;
+        for (int k = 0; k < 8; k++) {
+            const int ox = (k >> 2) & 1, oy = (k >> 1) & 1, oz = k & 1;
+            const double d = mg::zoom_dist_d(mg::zoom_draws(zseed, px + ox, py + oy, pz + oz),
+                                             (ax & 3) / 4.0 - ox, (ay & 3) / 4.0 - oy, (az & 3) / 4.0 - oz);
+            if (bd > d) { want = k; bd = d; }
+        }
+        bad += got != want;
+    }
+    atomicAdd(&out[0], bad);
+    atomicAdd(&out[1], close);
+}
+
 }  // namespace
+
+extern "C" MCGEN_API int mcgen_gb300_check_zoom(long long n, unsigned long long seed, long long *bad, long long *screened_out) {
+    if (n < 0 || !bad || !screened_out) return MCGEN_E_ARG;
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, 2 * sizeof(unsigned long long)) != cudaSuccess) return MCGEN_E_NOMEM;
+    cudaMemset(d, 0, 2 * sizeof(unsigned long long));
+    k_check_zoom<<<152 * 4, 256>>>(n, seed, d);
+    unsigned long long h[2] = {0, 0};
+    cudaError_t e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return MCGEN_E_INTERNAL;
+    *bad = (long long)h[0];
+    *screened_out = (long long)h[1];
+    return MCGEN_OK;
+}
 
 extern "C" MCGEN_API int mcgen_gb300_check_octave(long long n, unsigned long long seed, long long *bad) {
     if (n < 0 || !bad) return MCGEN_E_ARG;

@@ -7,6 +7,7 @@ import ctypes as C
 import os
 import re
 
+import numpy as np
 import pytest
 
 import __graft_entry__ as ge
@@ -158,3 +159,29 @@ def test_plan_and_search_argument_checks(mg):
     bad["flags"][0] = 0x200                                                       # unknown flag
     assert search(bad, 1) == mg.MCGEN_E_ARG
     assert L.mcgen_gb300_obs_end_radius(None, None) == -1
+
+
+def test_request_packing(mg):
+    """Request lists packed as numpy records are byte-identical to McGb300Request arrays (signed and unsigned
+    64-bit seeds, one world or one per request), and out-of-range fields are rejected on the host."""
+    g = mg.Generator.open(ge.data_root(), "26.3")
+    w1 = g.world("minecraft:overworld", "normal", 1)
+    w2 = g.world("minecraft:the_end", "normal", 1)
+    seeds = [-(2**63), 2**63 - 1, 2**63 + 7, 0, 12345]
+    reqs = [(w1 if i % 2 else w2, s, i - 3, 5 * i, 16 + i, 9, 16 - i) for i, s in enumerate(seeds)]
+    ref = (mg.McGb300Request * len(reqs))()
+    for i, (w, s, qx, qz, nx, nz, qy) in enumerate(reqs):
+        ref[i] = mg.McGb300Request(w.handle, s - 2**64 if s >= 2**63 else s, qx, qz, nx, nz, qy)
+    rec, worlds = mg._pack_requests(reqs)
+    assert rec.tobytes() == bytes(ref) and worlds == [r[0] for r in reqs]
+    ra = mg.RequestArray([r[0] for r in reqs], np.array([s % 2**64 for s in seeds], np.uint64),
+                         [r[2] for r in reqs], [r[3] for r in reqs], [r[4] for r in reqs], 9, [r[6] for r in reqs])
+    assert ra.records.tobytes() == bytes(ref) and len(ra) == len(reqs)
+    one = mg.RequestArray(w1, np.arange(4), 0, 0, 8, 8)
+    assert (one.records["world"] == w1.handle.value).all() and (one.records["qy"] == 16).all()
+    with pytest.raises(ValueError):
+        mg._pack_requests([(w1, 1, 2**31, 0, 4, 4, 16)])
+    with pytest.raises(ValueError):
+        mg.RequestArray(w1, [1, 2], 0, [0, -2**31 - 1], 4, 4)
+    with pytest.raises(ValueError):
+        mg.RequestArray([w1], [1, 2], 0, 0, 4, 4)

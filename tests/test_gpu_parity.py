@@ -200,6 +200,15 @@ def test_fixed_point_octave(mg):
         assert mg.check_octave(1 << 24, seed) == 0
 
 
+def test_zoom_screen(mg):
+    """BiomeManager's zoom choice, screened in single precision, equals the double-precision first minimum of
+    the 8 candidates on 2^27 random (zoom seed, block) cases, and the double-precision fallback ran."""
+    for seed in (5, 6):
+        bad, screened_out = mg.check_zoom(1 << 27, seed)
+        assert bad == 0
+        assert screened_out > 0
+
+
 def test_chunk_mode_grid_hashes(gens, mg):
     """The six golden 26.3 "chunk" digests through mcgen_gb300_quart_grid with MCGEN_TIE_CHUNK_ORDER, and an
     unaligned grid (partial chunks on every side) against the oracle."""
