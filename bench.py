@@ -186,16 +186,23 @@ def gpu_peaks(mg) -> dict:
 # Lattice (octave) samples per biome sample: 52 in the Overworld (six NormalNoises, two stacks each, with
 # the shift noise sampled twice), 8 in the Nether; the oracle's work counter pins both numbers.
 OCTAVES_PER_SAMPLE = {"minecraft:overworld": 52, "minecraft:the_nether": 8, "minecraft:the_end": 0}
-# FP64 operations of one octave sample as the kernels compute it.  Double branch (26.1/26.2): the two rounded
-# coordinate adds, two smoothsteps (7 each), the four first-level lerps' product and sum (the gradient sums
-# and lerp differences are exact in 2^-52 fixed point and run on the integer pipes), three more lerps (3
-# each) and the amplitude product and sum (3): 36.  Float branch (26.3): the two coordinate adds.  Smaller
-# per-sample terms (shift coordinates, End simplex) are left out, so the model is a lower bound.
-FP64_PER_OCTAVE = {"26.1": 36, "26.2": 36, "26.3": 2, "26.4-snapshot-2": 2}
+# FP64 operations per sample as the kernels compute them.  Float branch (26.3+): the two rounded coordinate
+# adds of every octave sample (Overworld 52 x 2, Nether 8 x 2).  Double branch (26.1/26.2), Overworld: the
+# shift noise's 12 octave samples exactly in double (36 each: 2 coordinate adds, 2 smoothsteps of 7, the four
+# first-level lerps' product and sum, 3 more lerps of 3, the amplitude products and sum), the 40 climate
+# octave samples in 59-bit fixed point with only their 2 coordinate adds on the FP64 pipe, and per climate
+# noise the conversion of the fixed-point sum (2) and the screen's two adds and two conversions (4), plus
+# ridges_folded (3 + 4): 432 + 80 + 37 = 549.  Nether: 8 x 2 + 2 x 6 = 28.  The rare values the screen leaves
+# to the exact double path and the End's simplex are left out, so the model is a lower bound.
+FP64_PER_SAMPLE = {("double", "minecraft:overworld"): 549, ("double", "minecraft:the_nether"): 28,
+                   ("float", "minecraft:overworld"): 104, ("float", "minecraft:the_nether"): 16,
+                   ("double", "minecraft:the_end"): 0, ("float", "minecraft:the_end"): 0}
+DOUBLE_BRANCH = ("26.1", "26.2")
 
 
 def batch_fp64_ops(reqs) -> float:
-    return float(sum(n * n * OCTAVES_PER_SAMPLE[d] * FP64_PER_OCTAVE[v] for v, d, s, qx0, qz0, n, qy in reqs))
+    return float(sum(n * n * FP64_PER_SAMPLE[("double" if v in DOUBLE_BRANCH else "float", d)]
+                     for v, d, s, qx0, qz0, n, qy in reqs))
 
 
 # Algorithmic work per launch of each kernel, counted from the reference algorithm:
@@ -521,7 +528,7 @@ def run_batch(args, rank, world, local_rank, mg, ge):
                                "traffic_note": "DRAM bytes per sample from the ncu capture of a 300-request launch "
                                                "(profiles/k_batch_uneven_batch.md) x samples; a lower bound at full "
                                                "size, where the output no longer fits L2",
-                               "work": f"{ops:.4g} FP64 ops per launch (lattice model)",
+                               "work": f"{ops:.4g} FP64 ops per launch (per-sample model of the screened evaluation)",
                                "peak_source": "measured in-run (FP64 add pipe microbenchmark)"}
         if not args.skip_extras:
             out["cpu_baseline"] = cpu_baseline_batch(reqs, args.cpu_sample_s)

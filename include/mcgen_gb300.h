@@ -177,6 +177,14 @@ MCGEN_API int mcgen_gb300_check_octave(long long n, unsigned long long seed, lon
  * n random (zoom seed, block) cases; *bad counts different choices, *screened_out the cases that needed the
  * double-precision comparison. */
 MCGEN_API int mcgen_gb300_check_zoom(long long n, unsigned long long seed, long long *bad, long long *screened_out);
+/* Device self-check of the double branch's screened climate noises (fixed-point value, exact double only
+ * where the float rounding is not settled by the error bound) on the world's own seed lattices: n random
+ * coordinates (integer part of magnitude up to 2^25 plus a shift in (-4, 4)), every screened noise of the
+ * world (Overworld 26.1/26.2: temperature .. ridge and ridges_folded; Nether: both).  *bad counts floats
+ * that differ from the exact path's, *screened_out the values left to the exact path, *worst_ratio the
+ * largest |fixed-point - exact| over the bound.  MCGEN_E_ARG for float-branch and End worlds. */
+MCGEN_API int mcgen_gb300_check_noise(const McWorld *w, long long n, unsigned long long seed, long long *bad,
+                                      long long *screened_out, double *worst_ratio);
 
 /* Pipe microbenchmarks on the current device, in giga-operations per second:
  * 0 FP32 FMA, 1 FP64 FMA, 2 FP64 add, 3 int32 multiply-add, 4 double->int floor conversion,

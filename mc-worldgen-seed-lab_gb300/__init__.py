@@ -93,6 +93,8 @@ _PROTOS = {
     "mcgen_gb300_check_octave": (C.c_int, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]),
     "mcgen_gb300_check_zoom": (C.c_int, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong),
                                          C.POINTER(C.c_longlong)]),
+    "mcgen_gb300_check_noise": (C.c_int, [_P, C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong),
+                                          C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
     "mcgen_gb300_search": (C.c_int, [_P, C.c_int, _P, C.c_uint64, C.c_uint64, _P, C.c_int, C.c_int, _P, C.c_uint32,
                                      C.POINTER(C.c_uint32), _P, C.POINTER(C.c_double)]),
     "mcgen_gb300_obs_end_radius": (C.c_int, [_P, _P]),
@@ -229,6 +231,15 @@ def check_zoom(n: int, seed: int = 1) -> tuple[int, int]:
     b, c = C.c_longlong(), C.c_longlong()
     _check(load().mcgen_gb300_check_zoom(n, seed, C.byref(b), C.byref(c)), "mcgen_gb300_check_zoom")
     return b.value, c.value
+
+
+def check_noise(world: "World", n: int, seed: int = 1) -> tuple[int, int, float]:
+    """(mismatches, values left to the exact path, worst error / bound) of the double branch's screened
+    climate noises against the exact double evaluation, on the world's own seed lattices."""
+    b, c, r = C.c_longlong(), C.c_longlong(), C.c_double()
+    _check(load().mcgen_gb300_check_noise(world.handle, n, seed, C.byref(b), C.byref(c), C.byref(r)),
+           "mcgen_gb300_check_noise")
+    return b.value, c.value, r.value
 
 
 def pipe_rate(pipe: str) -> float:

@@ -39,6 +39,61 @@ __device__ __forceinline__ void climate_finish_d(const MgWorldDesc &W, const MgS
     tg[3] = quantize((float)ev); tg[4] = quantize((float)depth); tg[5] = quantize((float)rv);
 }
 
+/* the same from the float values the reference takes of the five noises and of ridges_folded */
+__device__ __forceinline__ void climate_finish_df(const MgWorldDesc &W, const MgSpline &S, float tf, float hf, float cf,
+                                                  float ef, float rvf, float rff, int by, int32_t tg[6]) {
+    float co[4] = {cf, ef, rvf, rff};
+    double off = 0.0 + (W.off_d + (double)spline_eval(S, co)) * 1.0;
+    double fac = ((double)by - (double)W.grad_from_y) / ((double)W.grad_to_y - (double)W.grad_from_y);
+    double g = fac < 0.0 ? W.grad_from_d
+                         : (fac > 1.0 ? W.grad_to_d : W.grad_from_d + fac * (W.grad_to_d - W.grad_from_d));
+    double depth = g + off;
+    tg[0] = quantize(tf); tg[1] = quantize(hf); tg[2] = quantize(cf);
+    tg[3] = quantize(ef); tg[4] = quantize((float)depth); tg[5] = quantize(rvf);
+}
+/* (float) of a double-branch NormalNoise at (x, 0, z): the screened fixed-point value when it settles the
+ * rounding, else the exact double evaluation */
+__device__ __forceinline__ float nn_d_y0_float(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
+                                               double xc, double zc) {
+    double a;
+    float f;
+    if (N.fix_err >= 0.0 && nn_q_y0(N, T, x, z, xc, zc, a) && cast_settled(a, N.fix_err, f)) return f;
+    return (float)nn_d_y0(N, T, x, z, xc, zc);
+}
+/* ridge noise and ridges_folded (|(|r| + c0)| + c1) * c2 as floats.  ridges_folded of two doubles within d
+ * of each other, each step rounded, differ by at most |c2| (d + 1e-14) (values below 17 before the product),
+ * so the screen's bound for it is |c2| (fix_err + 1e-14) + 1e-13. */
+__device__ __forceinline__ void ridge_float(const MgWorldDesc &W, const MgLattice *__restrict__ T, double x, double z,
+                                            double xc, double zc, float &rvf, float &rff) {
+    const MgNoise &N = W.noise[5];
+    double a;
+    if (N.fix_err >= 0.0 && nn_q_y0(N, T, x, z, xc, zc, a)) {
+        const double rf = (fabs(fabs(a) + W.rf_d[0]) + W.rf_d[1]) * W.rf_d[2];
+        if (cast_settled(a, N.fix_err, rvf) && cast_settled(rf, fabs(W.rf_d[2]) * (N.fix_err + 1e-14) + 1e-13, rff))
+            return;
+    }
+    const double rv = nn_d_y0(N, T, x, z, xc, zc);
+    rvf = (float)rv;
+    rff = (float)((fabs(fabs(rv) + W.rf_d[0]) + W.rf_d[1]) * W.rf_d[2]);
+}
+
+/* double branch of the Overworld climate, out of line (the kernels reach the climate from two sites each:
+ * the cell itself and the tie chain) */
+static __device__ __noinline__ void climate_ow_d(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
+                                                 double X, double Z, double Xc, double Zc, int by, int32_t *tg) {
+    double sx = nn_d_y0(W.noise[0], T, X, Z, Xc, Zc) * 4.0;
+    double sz = nn_d_z0(W.noise[0], T, Z, X, Zc, Xc) * 4.0;
+    double x = X + sx, z = Z + sz;
+    double xc = x * MG_SECOND_STACK, zc = z * MG_SECOND_STACK;
+    const float tf = nn_d_y0_float(W.noise[1], T, x, z, xc, zc);
+    const float hf = nn_d_y0_float(W.noise[2], T, x, z, xc, zc);
+    const float cf = nn_d_y0_float(W.noise[3], T, x, z, xc, zc);
+    const float ef = nn_d_y0_float(W.noise[4], T, x, z, xc, zc);
+    float rvf, rff;
+    ridge_float(W, T, x, z, xc, zc, rvf, rff);
+    climate_finish_df(W, S, tf, hf, cf, ef, rvf, rff, by, tg);
+}
+
 /* Overworld climate of quart cell (qx, qy, qz) -> 6 quantised targets (engine/mc_climate.h:113-170). */
 template <bool FM>
 __device__ __forceinline__ void climate_ow(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
@@ -58,16 +113,7 @@ __device__ __forceinline__ void climate_ow(const MgWorldDesc &W, const MgSpline 
         float rv = nn_f_y0(W.noise[5], T, x, z, xc, zc);
         climate_finish_f(W, S, tv, hv, cv, ev, rv, by, tg);
     } else {
-        double sx = nn_d_y0(W.noise[0], T, X, Z, Xc, Zc) * 4.0;
-        double sz = nn_d_z0(W.noise[0], T, Z, X, Zc, Xc) * 4.0;
-        double x = X + sx, z = Z + sz;
-        double xc = x * MG_SECOND_STACK, zc = z * MG_SECOND_STACK;
-        double tv = nn_d_y0(W.noise[1], T, x, z, xc, zc);
-        double hv = nn_d_y0(W.noise[2], T, x, z, xc, zc);
-        double cv = nn_d_y0(W.noise[3], T, x, z, xc, zc);
-        double ev = nn_d_y0(W.noise[4], T, x, z, xc, zc);
-        double rv = nn_d_y0(W.noise[5], T, x, z, xc, zc);
-        climate_finish_d(W, S, tv, hv, cv, ev, rv, by, tg);
+        climate_ow_d(W, S, T, X, Z, Xc, Zc, by, tg);
     }
 }
 /* Nether: temperature and vegetation at (x/4, 0, z/4) (engine/cuda/mcg_host.c:63-74) */
@@ -81,8 +127,8 @@ __device__ __forceinline__ void climate_nether(const MgWorldDesc &W, const MgLat
         t = nn_f_legacy_y0(W.nether[0], T, X, Z, Xc, Zc);
         h = nn_f_legacy_y0(W.nether[1], T, X, Z, Xc, Zc);
     } else {
-        t = (float)nn_d_y0(W.nether[0], T, X, Z, Xc, Zc);
-        h = (float)nn_d_y0(W.nether[1], T, X, Z, Xc, Zc);
+        t = nn_d_y0_float(W.nether[0], T, X, Z, Xc, Zc);
+        h = nn_d_y0_float(W.nether[1], T, X, Z, Xc, Zc);
     }
     tg[0] = quantize(t);
     tg[1] = quantize(h);

@@ -299,6 +299,39 @@ __device__ __forceinline__ T octave(const uint8_t *__restrict__ p, int ix, T fx,
     return octave_p<T>(PlainPerm{p}, ix, fx, iy, fy, iz, fz);
 }
 
+/* Double branch, screened: the octave in 59-bit fixed point (values times 2^59 in int64, |value| < 16),
+ * an approximation of the exact real value of the reference's formula.  Products truncate (error below
+ * 2^-59 each); sums and the exact-integer gradient sums are exact.  The reference's own double rounding
+ * differs from the exact value by far more (the bound used by the screen, MgNoise::fix_err), so the
+ * approximation decides the reference's float result except near a float rounding boundary. */
+#define MG_Q 59
+__device__ __forceinline__ int64_t mulq(int64_t a, int64_t b) {
+    const uint64_t hi = (uint64_t)__mul64hi(a, b), lo = (uint64_t)a * (uint64_t)b;
+    return (int64_t)((hi << (64 - MG_Q)) | (lo >> MG_Q));
+}
+/* smoothstep t^3 (t (6 t - 15) + 10) of 0 <= t < 1 */
+__device__ __forceinline__ int64_t fadeq(int64_t t) {
+    const int64_t p = mulq(6 * t - (15LL << MG_Q), t) + (10LL << MG_Q);
+    return mulq(mulq(mulq(t, t), t), p);
+}
+__device__ __forceinline__ int64_t lerpq(int64_t t, int64_t a, int64_t b) { return a + mulq(t, b - a); }
+/* fractions X, Y, Z and smoothsteps V, W (of Y, Z) in the fixed point */
+template <typename P>
+__device__ __forceinline__ int64_t octave_qfix(const P &p, int ix, int64_t X, int iy, int64_t Y, int64_t V, int iz,
+                                               int64_t Z, int64_t W) {
+    const int64_t ONE = 1LL << MG_Q;
+    const int a = p(ix), b = p(ix + 1);
+    const int aa = p(a + iy), ab = p(a + iy + 1);
+    const int ba = p(b + iy), bb = p(b + iy + 1);
+    const int64_t GX = X - ONE, GY = Y - ONE, GZ = Z - ONE;
+    const int64_t U = fadeq(X);
+    const int64_t x00 = lerpq(U, gdot_i(p(aa + iz), X, Y, Z), gdot_i(p(ba + iz), GX, Y, Z));
+    const int64_t x10 = lerpq(U, gdot_i(p(ab + iz), X, GY, Z), gdot_i(p(bb + iz), GX, GY, Z));
+    const int64_t x01 = lerpq(U, gdot_i(p(aa + iz + 1), X, Y, GZ), gdot_i(p(ba + iz + 1), GX, Y, GZ));
+    const int64_t x11 = lerpq(U, gdot_i(p(ab + iz + 1), X, GY, GZ), gdot_i(p(bb + iz + 1), GX, GY, GZ));
+    return lerpq(W, lerpq(V, x00, x10), lerpq(V, x01, x11));
+}
+
 /* 26.3 PerlinNoise.wrap: identity inside (-2^24, 2^24) (engine/mc_noise.h:86-89) */
 __device__ __forceinline__ double wrap_new(double x) {
     const double lim = 16777215.999999998;
@@ -568,6 +601,40 @@ static __device__ __noinline__ double nn_d_z0(const MgNoise &N, const MgLattice 
         b += N.amp_d[k] * ob * N.vf_d[k];
     }
     return (a + b) * N.vfac;
+}
+
+/* double branch, screened (input y zero): the NormalNoise value in fixed point (every level's amplitude,
+ * level value factor and the noise's value factor folded into N.cq) as a double; false when a fraction of
+ * the input split is not a multiple of 2^-52 (the exact path handles those) */
+static __device__ __noinline__ bool nn_q_y0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
+                                        double xc, double zc, double &v) {
+    int64_t acc = 0;
+    const MgLattice *A = T + N.base;
+    /* one loop over both stacks' levels (the sum is exact, so its order is free): one copy of the octave
+     * code keeps the kernels' hot code small */
+    for (int j = 0; j < 2 * N.nlev; j++) {
+        const int k = j >> 1, second = j & 1;
+        const MgLattice *L = A + second * N.nlev + k;
+        const double f = N.freq[k];
+        int ix, iz;
+        double fx, fz;
+        int64_t FX, FZ;
+        split_dk(second ? xc : x, f, N.fexp[k], L->ox, ix, fx, FX);
+        split_dk(second ? zc : z, f, N.fexp[k], L->oz, iz, fz, FZ);
+        if ((FX | FZ | L->Fy) < 0) return false;
+        const int64_t Y = L->Fy << (MG_Q - 52), X = FX << (MG_Q - 52), Z = FZ << (MG_Q - 52);
+        acc += mulq(N.cq[k], octave_qfix(PlainPerm{L->p}, ix, X, L->iy, Y, fadeq(Y), iz, Z, fadeq(Z)));
+    }
+    v = (double)acc * 0x1.0p-59;
+    return true;
+}
+/* the float the reference's double value rounds to, from an approximation a within err of that value: true
+ * when every double in [a - err, a + err] rounds to the same float (rounding is monotone; err includes the
+ * rounding of a +- err) */
+__device__ __forceinline__ bool cast_settled(double a, double err, float &f) {
+    const float lo = __double2float_rn(a - err), hi = __double2float_rn(a + err);
+    f = lo;
+    return lo == hi;
 }
 
 /* ------------------------------------------------------------------ offset spline (engine/mc_climate.h:38-66)

@@ -272,7 +272,7 @@ __global__ void k_chain_resolve_ordered(const MgTreeNode *__restrict__ tree, con
 
 /* mcgen_biome_grid: out[iz*nx+ix] = biome_at(x0 + ix*step, y, z0 + iz*step) (libmcgen/src/region.c:86-108) */
 template <bool FM, int DIM>
-__global__ void __launch_bounds__(128) k_blockgrid(const __grid_constant__ MgWorldDesc W, const MgTreeNode *__restrict__ tree,
+__global__ void __launch_bounds__(128, 6) k_blockgrid(const __grid_constant__ MgWorldDesc W, const MgTreeNode *__restrict__ tree,
                                                    const MgLattice *__restrict__ state, int64_t zseed, int x0, int z0,
                                                    int nx, int nz, int step, int y, const int32_t *__restrict__ xyz,
                                                    uint8_t *__restrict__ out, const uint8_t *__restrict__ end_cls,

@@ -35,6 +35,10 @@ typedef struct {
     double vf_d[MG_MAX_OCT];       /* double branch: value factor of the level */
     double vfac;                   /* double branch: NormalNoise value factor */
     float amp_f[MG_MAX_OCT];       /* float branch: layer amplitude */
+    /* double branch, screened evaluation: amp_d[k] * vf_d[k] * vfac times 2^59, and the bound on the
+     * difference between the fixed-point value and the reference's double value (< 0: not screened) */
+    int64_t cq[MG_MAX_OCT];
+    double fix_err;
 } MgNoise;
 
 /* Offset spline (CubicSpline over continents, erosion, ridges, ridges_folded), float.

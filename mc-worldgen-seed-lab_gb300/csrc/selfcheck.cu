@@ -4,12 +4,16 @@
  * integer quart coordinates, coordinates plus a float shift, their products with the second-stack factor,
  * tiny and huge values, values whose sum with the offset lands near an integer, in (-1, 0) or on 0, and
  * offsets at 0, near 256 and on integers.  Also: the double branch's fixed-point octave (octave_dfix)
- * against the plain double octave on random permutations and fractions, and the single-precision screen of
- * BiomeManager's zoom (zoom_pick) against the double-precision choice among all 8 candidates. */
+ * against the plain double octave on random permutations and fractions, the single-precision screen of
+ * BiomeManager's zoom (zoom_pick) against the double-precision choice among all 8 candidates, and the
+ * fixed-point screen of the double branch's climate noises (nn_q_y0 + cast_settled) against the exact double
+ * evaluation on a world's own seed lattices. */
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "../../include/mcgen.h"
+#include "abi_internal.h"
 #include "climate.cuh"
 
 using namespace mgd;
@@ -140,7 +144,71 @@ __global__ void k_check_zoom(long long n, uint64_t seed, unsigned long long *out
     atomicAdd(&out[1], close);
 }
 
+/* noise screen: coordinates x = X + s with X an integer of magnitude class 2^10, 2^16, 2^21 or 2^25 and s a
+ * random double in (-4, 4) (the climate noises take quart coordinates plus a shift of up to 4); every
+ * screened noise of the world (Overworld: temperature .. ridge and ridges_folded; Nether: temperature,
+ * vegetation) is compared with the float of the exact double value.  out: mismatches, cases the screen left
+ * to the exact path, and the largest |fixed - exact| / fix_err as a double's bits. */
+__global__ void k_check_noise(const __grid_constant__ MgWorldDesc W, const MgLattice *__restrict__ T, long long n,
+                              uint64_t seed, unsigned long long *out) {
+    unsigned long long bad = 0, left = 0;
+    double worst = 0.0;
+    const int nn = W.dim == MG_OVERWORLD ? 5 : 2;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const uint64_t r = mix64(seed ^ mix64((uint64_t)i)), r2 = mix64(r), r3 = mix64(r2), r4 = mix64(r3);
+        const int lim = 1 << ((r & 3) == 0 ? 10 : ((r & 3) == 1 ? 16 : ((r & 3) == 2 ? 21 : 25)));
+        const int X = (int)((r >> 8) % (uint64_t)(2 * lim)) - lim, Z = (int)((r2 >> 8) % (uint64_t)(2 * lim)) - lim;
+        const double sx = ((double)(r3 >> 11) * 0x1.0p-53 * 2.0 - 1.0) * 4.0;
+        const double sz = ((double)(r4 >> 11) * 0x1.0p-53 * 2.0 - 1.0) * 4.0;
+        const double x = (double)X + sx, z = (double)Z + sz;
+        const double xc = x * MG_SECOND_STACK, zc = z * MG_SECOND_STACK;
+        for (int j = 0; j < nn; j++) {
+            const MgNoise &N = W.dim == MG_OVERWORLD ? W.noise[1 + j] : W.nether[j];
+            if (N.fix_err < 0.0) continue;
+            const double e = mgd::nn_d_y0(N, T, x, z, xc, zc);
+            double a;
+            float f;
+            if (!mgd::nn_q_y0(N, T, x, z, xc, zc, a)) { left++; continue; }
+            const double ratio = fabs(a - e) / N.fix_err;
+            worst = ratio > worst ? ratio : worst;
+            if (!mgd::cast_settled(a, N.fix_err, f)) { left++; continue; }
+            bad += f != (float)e;
+            if (W.dim == MG_OVERWORLD && j == 4) {
+                const double rfa = (fabs(fabs(a) + W.rf_d[0]) + W.rf_d[1]) * W.rf_d[2];
+                const double rfe = (fabs(fabs(e) + W.rf_d[0]) + W.rf_d[1]) * W.rf_d[2];
+                if (!mgd::cast_settled(rfa, fabs(W.rf_d[2]) * (N.fix_err + 1e-14) + 1e-13, f)) { left++; continue; }
+                bad += f != (float)rfe;
+            }
+        }
+    }
+    atomicAdd(&out[0], bad);
+    atomicAdd(&out[1], left);
+    atomicMax(&out[2], (unsigned long long)__double_as_longlong(worst)); /* non-negative: bits order as values */
+}
+
 }  // namespace
+
+extern "C" MCGEN_API int mcgen_gb300_check_noise(const McWorld *w, long long n, unsigned long long seed, long long *bad,
+                                                 long long *screened_out, double *worst_ratio) {
+    if (!w || n < 0 || !bad || !screened_out || !worst_ratio) return MCGEN_E_ARG;
+    if (w->desc.dim == MG_END || w->desc.fmode) return MCGEN_E_ARG; /* the double branch's noises only */
+    std::lock_guard<std::mutex> lk(mg::abi_lock());
+    if (!mg::abi_device_ready()) return MCGEN_E_UNSUPPORTED;
+    int rc = mg::abi_world_device(const_cast<McWorld *>(w));
+    if (rc) return rc;
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, 3 * sizeof(unsigned long long)) != cudaSuccess) return MCGEN_E_NOMEM;
+    cudaMemset(d, 0, 3 * sizeof(unsigned long long));
+    k_check_noise<<<152 * 4, 128>>>(w->desc, w->d_state, n, seed, d);
+    unsigned long long h[3] = {0, 0, 0};
+    cudaError_t e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return MCGEN_E_INTERNAL;
+    *bad = (long long)h[0];
+    *screened_out = (long long)h[1];
+    memcpy(worst_ratio, &h[2], sizeof(double));
+    return MCGEN_OK;
+}
 
 extern "C" MCGEN_API int mcgen_gb300_check_zoom(long long n, unsigned long long seed, long long *bad, long long *screened_out) {
     if (n < 0 || !bad || !screened_out) return MCGEN_E_ARG;

@@ -171,6 +171,39 @@ static void octave_seeds(MgNoise *s) {
     }
 }
 
+/* a * b * c * 2^59, truncated toward zero (|a b c| < 16; relative error below 2^-62 before the truncation) */
+static int64_t q59_product(double a, double b, double c) {
+    if (a == 0.0 || b == 0.0 || c == 0.0) return 0;
+    int ea, eb, ec;
+    const double fa = frexp(a, &ea), fb = frexp(b, &eb), fc = frexp(c, &ec); /* |f| in [0.5, 1) */
+    const __int128 ma = (int64_t)ldexp(fa, 53), mb = (int64_t)ldexp(fb, 53), mc = (int64_t)ldexp(fc, 53);
+    const __int128 p = (ma * mb) / ((__int128)1 << 43); /* |p| < 2^63: a b 2^(63 - ea - eb) */
+    const __int128 q = p * mc;                           /* a b c 2^(116 - ea - eb - ec) */
+    const int sh = 116 - 59 - (ea + eb + ec);
+    if (sh <= 0) return 0; /* not reached for |a b c| < 16 */
+    return (int64_t)(q / ((__int128)1 << (sh < 127 ? sh : 127)));
+}
+
+/* Bound on |fixed-point value - the reference's double value| of one double-branch NormalNoise, for the
+ * screened evaluation (nn_q_y0).  With u = 2^-53, the reference's octave (octave_dfix's operations: the
+ * smoothstep's 7 rounded operations, within 50u of the exact smoothstep; first-level lerps with exact
+ * gradient sums below 2 and once-rounded differences below 4, within 212u; second and third levels within
+ * 846u and 2748u) is within 3000u of the exact octave value, whose magnitude is below 2.1.  Each level's
+ * term (amp * o) * vf adds 2 roundings, each running sum of a stack one per level, the stack sum, the value
+ * factor product and the conversion of the fixed-point sum one each, on magnitudes below 2.1 * sum|c|.  The
+ * fixed-point evaluation itself is within 1e-16 per level.  The bound is taken 25 % larger, and
+ * cast_settled's two roundings of a +- err are added.  Negative: not screened (sum too large for the fixed
+ * point's range). */
+static double screen_bound(const MgNoise *s) {
+    const double u = 0x1.0p-53;
+    double c = 0.0;
+    for (int k = 0; k < s->nlev; k++) c += fabs(s->amp_d[k] * s->vf_d[k] * s->vfac);
+    const double vmax = 2.1 * 2.0 * c;
+    if (vmax * 1.01 >= 15.0) return -1.0;
+    const double e = 2.0 * c * (3000.0 * u + 4.2 * u) + (2.0 * s->nlev + 6.0) * u * vmax + 2.0 * s->nlev * 1e-16;
+    return 1.25 * e + 4.0 * u * vmax;
+}
+
 /* PerlinNoise/NormalNoise constants of 26.1/26.2 (engine/mc_noise.h:178-196) */
 static void noise_double(MgNoise *s, const NoiseParams &P, int legacy) {
     memset(s, 0, sizeof *s);
@@ -194,6 +227,8 @@ static void noise_double(MgNoise *s, const NoiseParams &P, int legacy) {
         in_f *= 2.0;
         val_f /= 2.0;
     }
+    for (int k = 0; k < s->nlev; k++) s->cq[k] = q59_product(s->amp_d[k], s->vf_d[k], s->vfac);
+    s->fix_err = screen_bound(s);
     octave_seeds(s);
 }
 

@@ -209,6 +209,21 @@ def test_zoom_screen(mg):
         assert screened_out > 0
 
 
+@pytest.mark.parametrize("version", ["26.1", "26.2"])
+@pytest.mark.parametrize("dim", ["minecraft:overworld", "minecraft:the_nether"])
+def test_noise_screen(gens, mg, version, dim):
+    """The double branch's climate noises evaluated in fixed point and screened by their error bound give the
+    exact double path's floats on 2^22 random coordinates per seed; the bound holds with room (the largest
+    observed error is a small fraction of it) and the exact path is left only a small share of the values."""
+    for seed in (12345, -(2**62) + 17):
+        w = gens[version].world(dim, "normal", seed)
+        bad, left, worst = mg.check_noise(w, 1 << 22, seed & 0xFFFF)
+        n_values = (1 << 22) * (6 if dim.endswith("overworld") else 2)
+        assert bad == 0
+        assert worst < 0.25
+        assert left < n_values // 50
+
+
 def test_chunk_mode_grid_hashes(gens, mg):
     """The six golden 26.3 "chunk" digests through mcgen_gb300_quart_grid with MCGEN_TIE_CHUNK_ORDER, and an
     unaligned grid (partial chunks on every side) against the oracle."""
