@@ -185,6 +185,13 @@ MCGEN_API int mcgen_gb300_check_zoom(long long n, unsigned long long seed, long 
  * largest |fixed-point - exact| over the bound.  MCGEN_E_ARG for float-branch and End worlds. */
 MCGEN_API int mcgen_gb300_check_noise(const McWorld *w, long long n, unsigned long long seed, long long *bad,
                                       long long *screened_out, double *worst_ratio);
+/* Device self-check of the double branch's whole Overworld climate as the kernels compute it (exact shift
+ * noises, climate noises screened in fixed point) against the plain double evaluation of every noise: n
+ * random quart cells (|qx|, |qz| up to 2^21).  *bad counts cells whose six quantised targets differ,
+ * *fallback the cells with at least one value the screen left to the exact double path.  MCGEN_E_ARG for
+ * float-branch, Nether and End worlds. */
+MCGEN_API int mcgen_gb300_check_climate(const McWorld *w, long long n, unsigned long long seed, long long *bad,
+                                        long long *fallback);
 
 /* Pipe microbenchmarks on the current device, in giga-operations per second:
  * 0 FP32 FMA, 1 FP64 FMA, 2 FP64 add, 3 int32 multiply-add, 4 double->int floor conversion,

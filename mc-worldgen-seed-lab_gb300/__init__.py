@@ -95,6 +95,8 @@ _PROTOS = {
                                          C.POINTER(C.c_longlong)]),
     "mcgen_gb300_check_noise": (C.c_int, [_P, C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong),
                                           C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
+    "mcgen_gb300_check_climate": (C.c_int, [_P, C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong),
+                                            C.POINTER(C.c_longlong)]),
     "mcgen_gb300_search": (C.c_int, [_P, C.c_int, _P, C.c_uint64, C.c_uint64, _P, C.c_int, C.c_int, _P, C.c_uint32,
                                      C.POINTER(C.c_uint32), _P, C.POINTER(C.c_double)]),
     "mcgen_gb300_obs_end_radius": (C.c_int, [_P, _P]),
@@ -240,6 +242,16 @@ def check_noise(world: "World", n: int, seed: int = 1) -> tuple[int, int, float]
     _check(load().mcgen_gb300_check_noise(world.handle, n, seed, C.byref(b), C.byref(c), C.byref(r)),
            "mcgen_gb300_check_noise")
     return b.value, c.value, r.value
+
+
+def check_climate(world: "World", n: int, seed: int = 1) -> tuple[int, int]:
+    """(cells whose targets differ, cells with a value the screen left to the exact path) of the double
+    branch's Overworld climate as the kernels compute it against the plain double evaluation, on n random
+    quart cells."""
+    b, c = C.c_longlong(), C.c_longlong()
+    _check(load().mcgen_gb300_check_climate(world.handle, n, seed, C.byref(b), C.byref(c)),
+           "mcgen_gb300_check_climate")
+    return b.value, c.value
 
 
 def pipe_rate(pipe: str) -> float:

@@ -39,8 +39,8 @@ __device__ __forceinline__ void lst_swap(uint8_t *mine, int i, int j) {
     *a = y;
     *b = x;
 }
-__device__ __forceinline__ void lst_store(uint32_t (*perm)[LNT], int t, MgLattice &h, MgLattice *L) {
-    lattice_header(h);
+__device__ __forceinline__ void lst_store(uint32_t (*perm)[LNT], int t, MgLattice &h, MgLattice *L, bool dbl) {
+    lattice_header(h, dbl);
     const uint4 *src = reinterpret_cast<const uint4 *>(&h);
     uint4 *dst = reinterpret_cast<uint4 *>(L);
     for (int q = 0; q < MG_LAT_HDR_WORDS; q++) dst[q] = src[q];
@@ -80,10 +80,10 @@ __global__ void __launch_bounds__(LNT) k_setup_list_xo(const MgWorldDesc *__rest
     for (int w = 0; w < 64; w++) perm[w][t] = 0x03020100u + 0x04040404u * (uint32_t)w;
     uint8_t *mine = reinterpret_cast<uint8_t *>(&perm[0][t]);
     for (int q = 0; q < 256; q++) lst_swap(mine, q, q + xo_int(x, 256u - (uint32_t)q));
-    lst_store(perm, t, h, pool + E.slot + j);
+    lst_store(perm, t, h, pool + E.slot + j, !W.fmode);
 }
 /* Nether entries: one thread per (entry, noise); End entries: one thread per entry. */
-__device__ __forceinline__ void lst_legacy(uint64_t &s, uint32_t (*perm)[LNT], int t, MgLattice *L) {
+__device__ __forceinline__ void lst_legacy(uint64_t &s, uint32_t (*perm)[LNT], int t, MgLattice *L, bool dbl) {
     MgLattice h;
     h.ox = lcg_double(s) * 256.0;
     h.oy = lcg_double(s) * 256.0;
@@ -91,7 +91,7 @@ __device__ __forceinline__ void lst_legacy(uint64_t &s, uint32_t (*perm)[LNT], i
     for (int w = 0; w < 64; w++) perm[w][t] = 0x03020100u + 0x04040404u * (uint32_t)w;
     uint8_t *mine = reinterpret_cast<uint8_t *>(&perm[0][t]);
     for (int q = 0; q < 256; q++) lst_swap(mine, q, q + lcg_int(s, 256 - q));
-    if (L) lst_store(perm, t, h, L);
+    if (L) lst_store(perm, t, h, L, dbl);
 }
 __global__ void __launch_bounds__(LNT) k_setup_list_legacy(const MgWorldDesc *__restrict__ worlds,
                                                            const MgSetupEntry *__restrict__ ent, int n,
@@ -113,9 +113,9 @@ __global__ void __launch_bounds__(LNT) k_setup_list_legacy(const MgWorldDesc *__
     for (int stack = 0; stack < 2; stack++) {
         MgLattice *S = T + stack * N.nlev;
         const bool keep_zero = zero >= 0 && zero < N.octs && slot[zero] >= 0;
-        lst_legacy(st, perm, t, keep_zero ? S + slot[zero] : nullptr);
+        lst_legacy(st, perm, t, keep_zero ? S + slot[zero] : nullptr, !W.fmode);
         for (int q = zero - 1; q >= 0; q--) {
-            if (q < N.octs && slot[q] >= 0) lst_legacy(st, perm, t, S + slot[q]);
+            if (q < N.octs && slot[q] >= 0) lst_legacy(st, perm, t, S + slot[q], !W.fmode);
             else st = lcg_jump(st, 262);
         }
     }
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(LNT) k_setup_list_end(const MgSetupEntry *__re
     const long long g = (long long)blockIdx.x * LNT + threadIdx.x;
     if (g >= n) return;
     uint64_t st = lcg_jump(lcg_init(ent[g].seed), 17292);
-    lst_legacy(st, perm, threadIdx.x, pool + ent[g].slot);
+    lst_legacy(st, perm, threadIdx.x, pool + ent[g].slot, false); /* the End reads the permutation only */
 }
 
 /* ---------------------------------------------------------------- the persistent batch kernel */

@@ -55,30 +55,43 @@ __device__ __forceinline__ void climate_finish_df(const MgWorldDesc &W, const Mg
  * rounding, else the exact double evaluation */
 __device__ __forceinline__ float nn_d_y0_float(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
                                                double xc, double zc) {
-    double a;
     float f;
-    if (N.fix_err >= 0.0 && nn_q_y0(N, T, x, z, xc, zc, a) && cast_settled(a, N.fix_err, f)) return f;
+    if (N.fix_err >= 0.0) {
+        const int64_t q = nn_q<false>(N, T, x, z, xc, zc);
+        if (q != MG_QFAIL && cast_settled((double)q * 0x1.0p-59, N.fix_err, f)) return f;
+    }
     return (float)nn_d_y0(N, T, x, z, xc, zc);
 }
-/* ridge noise and ridges_folded (|(|r| + c0)| + c1) * c2 as floats.  ridges_folded of two doubles within d
- * of each other, each step rounded, differ by at most |c2| (d + 1e-14) (values below 17 before the product),
- * so the screen's bound for it is |c2| (fix_err + 1e-14) + 1e-13. */
+/* ridges_folded (|(|r| + c0)| + c1) * c2 of a ridge value.  ridges_folded of two doubles within d of each
+ * other, each step rounded, differ by at most |c2| (d + 1e-14) (values below 17 before the product), so the
+ * screen's bound for it, from a ridge value within err of the reference's, is |c2| (err + 1e-14) + 1e-13. */
+__device__ __forceinline__ double ridges_folded_d(const MgWorldDesc &W, double r) {
+    return (fabs(fabs(r) + W.rf_d[0]) + W.rf_d[1]) * W.rf_d[2];
+}
+__device__ __forceinline__ double ridges_folded_err(const MgWorldDesc &W, double err) {
+    return fabs(W.rf_d[2]) * (err + 1e-14) + 1e-13;
+}
+/* ridge noise and ridges_folded as floats */
 __device__ __forceinline__ void ridge_float(const MgWorldDesc &W, const MgLattice *__restrict__ T, double x, double z,
                                             double xc, double zc, float &rvf, float &rff) {
     const MgNoise &N = W.noise[5];
-    double a;
-    if (N.fix_err >= 0.0 && nn_q_y0(N, T, x, z, xc, zc, a)) {
-        const double rf = (fabs(fabs(a) + W.rf_d[0]) + W.rf_d[1]) * W.rf_d[2];
-        if (cast_settled(a, N.fix_err, rvf) && cast_settled(rf, fabs(W.rf_d[2]) * (N.fix_err + 1e-14) + 1e-13, rff))
-            return;
+    if (N.fix_err >= 0.0) {
+        const int64_t q = nn_q<false>(N, T, x, z, xc, zc);
+        if (q != MG_QFAIL) {
+            const double a = (double)q * 0x1.0p-59;
+            if (cast_settled(a, N.fix_err, rvf) && cast_settled(ridges_folded_d(W, a), ridges_folded_err(W, N.fix_err), rff))
+                return;
+        }
     }
     const double rv = nn_d_y0(N, T, x, z, xc, zc);
     rvf = (float)rv;
-    rff = (float)((fabs(fabs(rv) + W.rf_d[0]) + W.rf_d[1]) * W.rf_d[2]);
+    rff = (float)ridges_folded_d(W, rv);
 }
 
 /* double branch of the Overworld climate, out of line (the kernels reach the climate from two sites each:
- * the cell itself and the tie chain) */
+ * the cell itself and the tie chain).  The shift noises stay exact in double: their value moves the climate
+ * noises' input coordinates, and the kernels' integer pipes (which carry the screened climate noises) are
+ * busier than the FP64 pipe, so a fixed-point shift measured slower. */
 static __device__ __noinline__ void climate_ow_d(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
                                                  double X, double Z, double Xc, double Zc, int by, int32_t *tg) {
     double sx = nn_d_y0(W.noise[0], T, X, Z, Xc, Zc) * 4.0;

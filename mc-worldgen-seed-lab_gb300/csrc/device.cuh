@@ -113,6 +113,22 @@ __device__ __forceinline__ uint64_t lcg_jump(uint64_t s, uint32_t n) {
 __device__ __forceinline__ int ifloor(double v) { return __double2int_rd(v); }
 __device__ __forceinline__ int64_t lfloor(double v) { return __double2ll_rd(v); }
 
+/* Double branch, screened: the octave in 59-bit fixed point (values times 2^59 in int64, |value| < 16),
+ * an approximation of the exact real value of the reference's formula.  Products truncate (error below
+ * 2^-59 each); sums and the exact-integer gradient sums are exact.  The reference's own double rounding
+ * differs from the exact value by far more (the bound used by the screen, MgNoise::fix_err), so the
+ * approximation decides the reference's float result except near a float rounding boundary. */
+#define MG_Q 59
+__device__ __forceinline__ int64_t mulq(int64_t a, int64_t b) {
+    const uint64_t hi = (uint64_t)__mul64hi(a, b), lo = (uint64_t)a * (uint64_t)b;
+    return (int64_t)((hi << (64 - MG_Q)) | (lo >> MG_Q));
+}
+/* smoothstep t^3 (t (6 t - 15) + 10) of 0 <= t < 1 */
+__device__ __forceinline__ int64_t fadeq(int64_t t) {
+    const int64_t p = mulq(6 * t - (15LL << MG_Q), t) + (10LL << MG_Q);
+    return mulq(mulq(mulq(t, t), t), p);
+}
+
 /* ------------------------------------------------------------------ lattice header */
 template <typename T>
 __device__ __forceinline__ T fade_h(T t) { return t * t * t * (t * (t * (T)6 - (T)15) + (T)10); }
@@ -127,9 +143,10 @@ __device__ __forceinline__ int64_t fixed52(double d) {
     return (int64_t)(m >> -e);
 }
 /* fill the y/z splits a zero input coordinate uses (the reference computes the same values per sample);
- * H is MgLattice or any header with the same field names */
+ * H is MgLattice or any header with the same field names; dbl: a double-branch world's lattice (the
+ * fixed-point smoothsteps), else the float branch's */
 template <typename H>
-__device__ __forceinline__ void lattice_header(H &L) {
+__device__ __forceinline__ void lattice_header(H &L, bool dbl) {
     L.iy = ifloor(L.oy);
     L.iz = ifloor(L.oz);
     L.fyd = L.oy - (double)L.iy;
@@ -138,10 +155,15 @@ __device__ __forceinline__ void lattice_header(H &L) {
     L.uzd = fade_h<double>(L.fzd);
     L.Fy = fixed52(L.fyd);
     L.Fz = fixed52(L.fzd);
-    L.fy = (float)L.fyd;
-    L.fz = (float)L.fzd;
-    L.uy = fade_h<float>(L.fy);
-    L.uz = fade_h<float>(L.fz);
+    if (dbl) {
+        L.z0.q.uy = L.Fy < 0 ? 0 : fadeq(L.Fy << (MG_Q - 52));
+        L.z0.q.uz = L.Fz < 0 ? 0 : fadeq(L.Fz << (MG_Q - 52));
+    } else {
+        L.z0.f.fy = (float)L.fyd;
+        L.z0.f.fz = (float)L.fzd;
+        L.z0.f.uy = fade_h<float>(L.z0.f.fy);
+        L.z0.f.uz = fade_h<float>(L.z0.f.fz);
+    }
 }
 /* the header's 16-byte words (the permutation follows them) */
 #define MG_LAT_HDR_WORDS ((int)(offsetof(MgLattice, p) / 16))
@@ -208,12 +230,12 @@ __device__ __forceinline__ T octave_p(const P &p, int ix, T fx, int iy, T fy, in
 /* input coordinate y (resp. z) zero: its split comes from the lattice header */
 template <typename T> struct Hdr;
 template <> struct Hdr<float> {
-    template <typename H> __device__ static float fy(const H &h) { return h.fy; }
-    template <typename H> __device__ static float fz(const H &h) { return h.fz; }
-    template <typename H> __device__ static float gy(const H &h) { return h.fy - 1.0f; }
-    template <typename H> __device__ static float gz(const H &h) { return h.fz - 1.0f; }
-    template <typename H> __device__ static float uy(const H &h) { return h.uy; }
-    template <typename H> __device__ static float uz(const H &h) { return h.uz; }
+    template <typename H> __device__ static float fy(const H &h) { return h.z0.f.fy; }
+    template <typename H> __device__ static float fz(const H &h) { return h.z0.f.fz; }
+    template <typename H> __device__ static float gy(const H &h) { return h.z0.f.fy - 1.0f; }
+    template <typename H> __device__ static float gz(const H &h) { return h.z0.f.fz - 1.0f; }
+    template <typename H> __device__ static float uy(const H &h) { return h.z0.f.uy; }
+    template <typename H> __device__ static float uz(const H &h) { return h.z0.f.uz; }
 };
 template <> struct Hdr<double> {
     template <typename H> __device__ static double fy(const H &h) { return h.fyd; }
@@ -299,21 +321,7 @@ __device__ __forceinline__ T octave(const uint8_t *__restrict__ p, int ix, T fx,
     return octave_p<T>(PlainPerm{p}, ix, fx, iy, fy, iz, fz);
 }
 
-/* Double branch, screened: the octave in 59-bit fixed point (values times 2^59 in int64, |value| < 16),
- * an approximation of the exact real value of the reference's formula.  Products truncate (error below
- * 2^-59 each); sums and the exact-integer gradient sums are exact.  The reference's own double rounding
- * differs from the exact value by far more (the bound used by the screen, MgNoise::fix_err), so the
- * approximation decides the reference's float result except near a float rounding boundary. */
-#define MG_Q 59
-__device__ __forceinline__ int64_t mulq(int64_t a, int64_t b) {
-    const uint64_t hi = (uint64_t)__mul64hi(a, b), lo = (uint64_t)a * (uint64_t)b;
-    return (int64_t)((hi << (64 - MG_Q)) | (lo >> MG_Q));
-}
-/* smoothstep t^3 (t (6 t - 15) + 10) of 0 <= t < 1 */
-__device__ __forceinline__ int64_t fadeq(int64_t t) {
-    const int64_t p = mulq(6 * t - (15LL << MG_Q), t) + (10LL << MG_Q);
-    return mulq(mulq(mulq(t, t), t), p);
-}
+/* the octave in the 59-bit fixed point of mulq / fadeq */
 __device__ __forceinline__ int64_t lerpq(int64_t t, int64_t a, int64_t b) { return a + mulq(t, b - a); }
 /* fractions X, Y, Z and smoothsteps V, W (of Y, Z) in the fixed point */
 template <typename P>
@@ -603,30 +611,39 @@ static __device__ __noinline__ double nn_d_z0(const MgNoise &N, const MgLattice 
     return (a + b) * N.vfac;
 }
 
-/* double branch, screened (input y zero): the NormalNoise value in fixed point (every level's amplitude,
- * level value factor and the noise's value factor folded into N.cq) as a double; false when a fraction of
- * the input split is not a multiple of 2^-52 (the exact path handles those) */
-static __device__ __noinline__ bool nn_q_y0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
-                                        double xc, double zc, double &v) {
+/* double branch, screened: the NormalNoise value in fixed point (every level's amplitude, level value
+ * factor and the noise's value factor folded into N.cq), in units of 2^-59; input (a, 0, b) (Z0 false:
+ * the climate noises and ShiftA) or (a, b, 0) (Z0 true: ShiftB), with ac, bc the second stack's inputs.
+ * The zero coordinate's split and smoothstep come from the lattice header.  MG_QFAIL when a fraction of the
+ * input split is not a multiple of 2^-52 (the exact path handles those); |value| < 15 * 2^59 otherwise. */
+#define MG_QFAIL INT64_MIN
+template <bool Z0>
+static __device__ __noinline__ int64_t nn_q(const MgNoise &N, const MgLattice *__restrict__ T, double a, double b,
+                                            double ac, double bc) {
     int64_t acc = 0;
     const MgLattice *A = T + N.base;
-    /* one loop over both stacks' levels (the sum is exact, so its order is free): one copy of the octave
-     * code keeps the kernels' hot code small */
-    for (int j = 0; j < 2 * N.nlev; j++) {
-        const int k = j >> 1, second = j & 1;
-        const MgLattice *L = A + second * N.nlev + k;
+    /* per level, the two stacks' octaves (independent: two dependency chains in flight), then one product
+     * with the level's constant (the sum is exact, so its order is free) */
+    for (int k = 0; k < N.nlev; k++) {
         const double f = N.freq[k];
-        int ix, iz;
-        double fx, fz;
-        int64_t FX, FZ;
-        split_dk(second ? xc : x, f, N.fexp[k], L->ox, ix, fx, FX);
-        split_dk(second ? zc : z, f, N.fexp[k], L->oz, iz, fz, FZ);
-        if ((FX | FZ | L->Fy) < 0) return false;
-        const int64_t Y = L->Fy << (MG_Q - 52), X = FX << (MG_Q - 52), Z = FZ << (MG_Q - 52);
-        acc += mulq(N.cq[k], octave_qfix(PlainPerm{L->p}, ix, X, L->iy, Y, fadeq(Y), iz, Z, fadeq(Z)));
+        int64_t o[2];
+#pragma unroll
+        for (int st = 0; st < 2; st++) {
+            const MgLattice *L = A + st * N.nlev + k;
+            int ia, ib;
+            double fa, fb;
+            int64_t FA, FB;
+            split_dk(st ? ac : a, f, N.fexp[k], L->ox, ia, fa, FA);
+            split_dk(st ? bc : b, f, N.fexp[k], Z0 ? L->oy : L->oz, ib, fb, FB);
+            const int64_t F0 = Z0 ? L->Fz : L->Fy;
+            if ((FA | FB | F0) < 0) return MG_QFAIL;
+            const int64_t XA = FA << (MG_Q - 52), XB = FB << (MG_Q - 52), X0 = F0 << (MG_Q - 52);
+            o[st] = Z0 ? octave_qfix(PlainPerm{L->p}, ia, XA, ib, XB, fadeq(XB), L->iz, X0, L->z0.q.uz)
+                       : octave_qfix(PlainPerm{L->p}, ia, XA, L->iy, X0, L->z0.q.uy, ib, XB, fadeq(XB));
+        }
+        acc += mulq(N.cq[k], o[0] + o[1]);
     }
-    v = (double)acc * 0x1.0p-59;
-    return true;
+    return acc;
 }
 /* the float the reference's double value rounds to, from an approximation a within err of that value: true
  * when every double in [a - err, a + err] rounds to the same float (rounding is monotone; err includes the

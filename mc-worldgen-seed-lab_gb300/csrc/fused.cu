@@ -39,7 +39,7 @@ struct OffHdr {
     double ox, oy, oz, fyd, fzd, uyd, uzd;
     int64_t Fy, Fz;
     int iy, iz;
-    float fy, fz, uy, uz;
+    MgLatZero z0;
 };
 
 template <typename V>
@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(FNT) k_ow_seed_climate(const __grid_constant__
     /* split of the offsets used by a zero input coordinate */
     OffHdr h;
     h.ox = ox; h.oy = oy; h.oz = oz;
-    lattice_header(h);
+    lattice_header(h, !FM);
     if (t < nown) sm.hdr[t] = h;
     const uint8_t *pbase = reinterpret_cast<const uint8_t *>(&sm.perm[0][0]);
     const MgNoise &N = W.noise[noise];

@@ -55,8 +55,8 @@ __device__ __forceinline__ void perm_store(uint32_t (*perm)[SETUP_NT], int t, Mg
 #pragma unroll 4
     for (int q = 0; q < 16; q++) dst[q] = make_uint4(perm[4 * q][t], perm[4 * q + 1][t], perm[4 * q + 2][t], perm[4 * q + 3][t]);
 }
-__device__ __forceinline__ void header_store(MgLattice &h, MgLattice *L) {
-    lattice_header(h);
+__device__ __forceinline__ void header_store(MgLattice &h, MgLattice *L, bool dbl) {
+    lattice_header(h, dbl);
     const uint4 *src = reinterpret_cast<const uint4 *>(&h);
     uint4 *dst = reinterpret_cast<uint4 *>(L);
 #pragma unroll
@@ -91,12 +91,12 @@ __global__ void __launch_bounds__(SETUP_NT) k_setup_xo(const __grid_constant__ M
     uint8_t *base = reinterpret_cast<uint8_t *>(&perm[0][0]);
     for (int q = 0; q < 256; q++) perm_swap(base, t, q, q + xo_int(x, 256u - (uint32_t)q));
     MgLattice *L = out + g;
-    header_store(h, L);
+    header_store(h, L, !W.fmode);
     perm_store(perm, t, L);
 }
 
 /* one legacy lattice from the LCG into the thread's shuffle slot, then to `L` (if non-null) */
-__device__ __forceinline__ void legacy_lattice(uint64_t &s, uint32_t (*perm)[SETUP_NT], int t, MgLattice *L) {
+__device__ __forceinline__ void legacy_lattice(uint64_t &s, uint32_t (*perm)[SETUP_NT], int t, MgLattice *L, bool dbl) {
     MgLattice h;
     h.ox = lcg_double(s) * 256.0;
     h.oy = lcg_double(s) * 256.0;
@@ -105,7 +105,7 @@ __device__ __forceinline__ void legacy_lattice(uint64_t &s, uint32_t (*perm)[SET
     uint8_t *base = reinterpret_cast<uint8_t *>(&perm[0][0]);
     for (int q = 0; q < 256; q++) perm_swap(base, t, q, q + lcg_int(s, 256 - q));
     if (L) {
-        header_store(h, L);
+        header_store(h, L, dbl);
         perm_store(perm, t, L);
     }
 }
@@ -129,9 +129,9 @@ __global__ void __launch_bounds__(SETUP_NT) k_setup_legacy(const __grid_constant
     for (int stack = 0; stack < 2; stack++) {
         MgLattice *S = T + stack * N.nlev;
         bool keep_zero = zero >= 0 && zero < N.octs && slot[zero] >= 0;
-        legacy_lattice(st, perm, t, keep_zero ? S + slot[zero] : nullptr);
+        legacy_lattice(st, perm, t, keep_zero ? S + slot[zero] : nullptr, !W.fmode);
         for (int q = zero - 1; q >= 0; q--) {
-            if (q < N.octs && slot[q] >= 0) legacy_lattice(st, perm, t, S + slot[q]);
+            if (q < N.octs && slot[q] >= 0) legacy_lattice(st, perm, t, S + slot[q], !W.fmode);
             else st = lcg_jump(st, 262);
         }
     }
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(SETUP_NT) k_setup_end(const int64_t *__restric
     const long long g = (long long)blockIdx.x * SETUP_NT + t;
     if (g >= ns) return;
     uint64_t st = lcg_jump(lcg_init(seeds[g]), 17292);
-    legacy_lattice(st, perm, t, out + g);
+    legacy_lattice(st, perm, t, out + g, false); /* the End reads the permutation only */
 }
 
 /* ============================================================================ sampling kernels */

@@ -86,6 +86,17 @@ typedef struct {
     MgSpline spline;
 } MgWorldDesc;
 
+/* Split of the y and z offsets for a zero input coordinate, by branch. */
+typedef union {
+    struct {
+        float fy, fz;  /* (float)fyd, (float)fzd */
+        float uy, uz;  /* smoothstep(fy), smoothstep(fz) in float */
+    } f;               /* float branch */
+    struct {
+        int64_t uy, uz; /* smoothstep of Fy, Fz in 2^-59 fixed point (0 where Fy, Fz < 0) */
+    } q;                /* double branch (the screened fixed-point evaluation) */
+} MgLatZero;
+
 /* One Perlin octave of one seed: offsets, the lattice split of the y and z offsets (what a zero input
  * coordinate uses: fraction and smoothstep of the fraction, and the fraction as a multiple of 2^-52 for
  * the double branch's exact fixed-point gradient sums), and the permutation.
@@ -96,8 +107,7 @@ typedef struct __attribute__((aligned(16))) {
     double uyd, uzd;   /* smoothstep(fyd), smoothstep(fzd) */
     int64_t Fy, Fz;    /* fyd, fzd in units of 2^-52, or -1 when not a multiple of 2^-52 */
     int32_t iy, iz;    /* floor(oy), floor(oz) */
-    float fy, fz;      /* (float)fyd, (float)fzd (float branch) */
-    float uy, uz;      /* smoothstep(fy), smoothstep(fz) in float */
+    MgLatZero z0;
     uint8_t p[256];
 } MgLattice;
 

@@ -5,9 +5,10 @@
  * tiny and huge values, values whose sum with the offset lands near an integer, in (-1, 0) or on 0, and
  * offsets at 0, near 256 and on integers.  Also: the double branch's fixed-point octave (octave_dfix)
  * against the plain double octave on random permutations and fractions, the single-precision screen of
- * BiomeManager's zoom (zoom_pick) against the double-precision choice among all 8 candidates, and the
- * fixed-point screen of the double branch's climate noises (nn_q_y0 + cast_settled) against the exact double
- * evaluation on a world's own seed lattices. */
+ * BiomeManager's zoom (zoom_pick) against the double-precision choice among all 8 candidates, the
+ * fixed-point screen of the double branch's climate noises (nn_q + cast_settled) against the exact double
+ * evaluation on a world's own seed lattices, and the double branch's whole Overworld climate as the kernels
+ * compute it (climate_ow_d) against the plain double evaluation. */
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -166,9 +167,10 @@ __global__ void k_check_noise(const __grid_constant__ MgWorldDesc W, const MgLat
             const MgNoise &N = W.dim == MG_OVERWORLD ? W.noise[1 + j] : W.nether[j];
             if (N.fix_err < 0.0) continue;
             const double e = mgd::nn_d_y0(N, T, x, z, xc, zc);
-            double a;
             float f;
-            if (!mgd::nn_q_y0(N, T, x, z, xc, zc, a)) { left++; continue; }
+            const int64_t q = mgd::nn_q<false>(N, T, x, z, xc, zc);
+            if (q == MG_QFAIL) { left++; continue; }
+            const double a = (double)q * 0x1.0p-59;
             const double ratio = fabs(a - e) / N.fix_err;
             worst = ratio > worst ? ratio : worst;
             if (!mgd::cast_settled(a, N.fix_err, f)) { left++; continue; }
@@ -186,7 +188,68 @@ __global__ void k_check_noise(const __grid_constant__ MgWorldDesc W, const MgLat
     atomicMax(&out[2], (unsigned long long)__double_as_longlong(worst)); /* non-negative: bits order as values */
 }
 
+/* Overworld climate of the double branch as the kernels compute it (climate_ow_d: exact shift noises, the
+ * five climate noises screened in fixed point) against the plain double evaluation of every noise: random
+ * quart cells (|qx|, |qz| below 2^8, 2^11, 2^13, 2^15, 2^18 or 2^21, qy in [-16, 80)).  out: cells whose
+ * six targets differ, cells with at least one value the screen left to the exact path. */
+__global__ void k_check_climate(const __grid_constant__ MgWorldDesc W, const MgLattice *__restrict__ T, long long n,
+                                uint64_t seed, unsigned long long *out) {
+    unsigned long long bad = 0, left = 0;
+    const int lims[6] = {8, 11, 13, 15, 18, 21};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const uint64_t r = mix64(seed ^ mix64((uint64_t)i)), r2 = mix64(r), r3 = mix64(r2);
+        const int lim = 1 << lims[(r & 0xFF) % 6];
+        const int qx = (int)((r >> 8) % (uint64_t)(2 * lim)) - lim, qz = (int)((r2 >> 8) % (uint64_t)(2 * lim)) - lim;
+        const int by = 4 * ((int)(r3 % 96) - 16);
+        const double X = (double)qx, Z = (double)qz, Xc = X * MG_SECOND_STACK, Zc = Z * MG_SECOND_STACK;
+        int32_t got[6], want[6];
+        mg::climate_ow_d(W, W.spline, T, X, Z, Xc, Zc, by, got);
+        const double x = X + mgd::nn_d_y0(W.noise[0], T, X, Z, Xc, Zc) * 4.0;
+        const double z = Z + mgd::nn_d_z0(W.noise[0], T, Z, X, Zc, Xc) * 4.0;
+        const double xc = x * MG_SECOND_STACK, zc = z * MG_SECOND_STACK;
+        double v[5];
+        bool exact = false;
+        for (int j = 0; j < 5; j++) {
+            const MgNoise &N = W.noise[1 + j];
+            v[j] = mgd::nn_d_y0(N, T, x, z, xc, zc);
+            const int64_t q = N.fix_err < 0.0 ? MG_QFAIL : mgd::nn_q<false>(N, T, x, z, xc, zc);
+            float f;
+            exact |= q == MG_QFAIL || !mgd::cast_settled((double)q * 0x1.0p-59, N.fix_err, f);
+            if (j == 4 && !exact)
+                exact |= !mgd::cast_settled(mg::ridges_folded_d(W, (double)q * 0x1.0p-59), mg::ridges_folded_err(W, N.fix_err), f);
+        }
+        mg::climate_finish_d(W, W.spline, v[0], v[1], v[2], v[3], v[4], by, want);
+        bool diff = false;
+        for (int j = 0; j < 6; j++) diff |= got[j] != want[j];
+        bad += diff;
+        left += exact;
+    }
+    atomicAdd(&out[0], bad);
+    atomicAdd(&out[1], left);
+}
+
 }  // namespace
+
+extern "C" MCGEN_API int mcgen_gb300_check_climate(const McWorld *w, long long n, unsigned long long seed, long long *bad,
+                                                   long long *fallback) {
+    if (!w || n < 0 || !bad || !fallback) return MCGEN_E_ARG;
+    if (w->desc.dim != MG_OVERWORLD || w->desc.fmode) return MCGEN_E_ARG; /* the double branch's Overworld only */
+    std::lock_guard<std::mutex> lk(mg::abi_lock());
+    if (!mg::abi_device_ready()) return MCGEN_E_UNSUPPORTED;
+    int rc = mg::abi_world_device(const_cast<McWorld *>(w));
+    if (rc) return rc;
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, 2 * sizeof(unsigned long long)) != cudaSuccess) return MCGEN_E_NOMEM;
+    cudaMemset(d, 0, 2 * sizeof(unsigned long long));
+    k_check_climate<<<152 * 4, 128>>>(w->desc, w->d_state, n, seed, d);
+    unsigned long long h[2] = {0, 0};
+    cudaError_t e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return MCGEN_E_INTERNAL;
+    *bad = (long long)h[0];
+    *fallback = (long long)h[1];
+    return MCGEN_OK;
+}
 
 extern "C" MCGEN_API int mcgen_gb300_check_noise(const McWorld *w, long long n, unsigned long long seed, long long *bad,
                                                  long long *screened_out, double *worst_ratio) {

@@ -185,25 +185,32 @@ static int64_t q59_product(double a, double b, double c) {
 }
 
 /* Bound on |fixed-point value - the reference's double value| of one double-branch NormalNoise, for the
- * screened evaluation (nn_q_y0).  With u = 2^-53, the reference's octave (octave_dfix's operations: the
- * smoothstep's 7 rounded operations, within 50u of the exact smoothstep; first-level lerps with exact
- * gradient sums below 2 and once-rounded differences below 4, within 212u; second and third levels within
- * 846u and 2748u) is within 3000u of the exact octave value, whose magnitude is below 2.1.  Each level's
- * term (amp * o) * vf adds 2 roundings, each running sum of a stack one per level, the stack sum, the value
- * factor product and the conversion of the fixed-point sum one each, on magnitudes below 2.1 * sum|c|.  The
- * fixed-point evaluation itself is within 1e-16 per level.  The bound is taken 25 % larger, and
- * cast_settled's two roundings of a +- err are added.  Negative: not screened (sum too large for the fixed
- * point's range). */
+ * screened evaluation (nn_q).  With u = 2^-53, the reference's octave (improved_noise_d's operations, all
+ * rounded to nearest) against the exact real value at the same double inputs:
+ *  - the fractions, their differences with 1 and the eight gradient sums are exact (multiples of 2^-52
+ *    below 2 in magnitude);
+ *  - the smoothstep t^3 (t (6t - 15) + 10) is within 44u of the exact one: the inner factor's four
+ *    roundings (6t, -15, *t, +10) add at most (6 + 15 + 9 + 10)u = 40u, scaled by t^3 <= 1, the cube's two
+ *    roundings 2u t^3 times an inner factor <= 10 that is 1 where t^3 is 1 (<= 2u t^3 (6t^2 - 15t + 10)
+ *    <= 2u), and the product's rounding u; 50u is used;
+ *  - one lerp a + s (b - a) with s within 50u of the exact smoothstep S in [0, 1], |a|, |b| <= 2 exact-valued
+ *    within E: the propagated input error is (1 - S) e_a + S e_b <= E, the smoothstep error times
+ *    |b - a| <= 4 adds 200u, the rounding of b - a (times S) 4u, of the product 4u and of the sum 2u:
+ *    E + 210u.  The three lerp levels (E = 0, then 210u, 420u) give 630u; 640u is used.
+ * Each level's term (amp * o) * vf adds 2 roundings, each running sum of a stack one per level, the stack sum,
+ * the value factor product and the conversion of the fixed-point sum one each, on magnitudes below
+ * 2.1 * sum|c|.  The fixed-point evaluation itself is within 1e-16 per level.  The bound is taken 25 %
+ * larger, and cast_settled's two roundings of a +- err are added.  Negative: not screened (sum too large for
+ * the fixed point's range). */
 static double screen_bound(const MgNoise *s) {
     const double u = 0x1.0p-53;
     double c = 0.0;
     for (int k = 0; k < s->nlev; k++) c += fabs(s->amp_d[k] * s->vf_d[k] * s->vfac);
     const double vmax = 2.1 * 2.0 * c;
     if (vmax * 1.01 >= 15.0) return -1.0;
-    const double e = 2.0 * c * (3000.0 * u + 4.2 * u) + (2.0 * s->nlev + 6.0) * u * vmax + 2.0 * s->nlev * 1e-16;
+    const double e = 2.0 * c * (640.0 * u + 4.2 * u) + (2.0 * s->nlev + 6.0) * u * vmax + 2.0 * s->nlev * 1e-16;
     return 1.25 * e + 4.0 * u * vmax;
 }
-
 /* PerlinNoise/NormalNoise constants of 26.1/26.2 (engine/mc_noise.h:178-196) */
 static void noise_double(MgNoise *s, const NoiseParams &P, int legacy) {
     memset(s, 0, sizeof *s);

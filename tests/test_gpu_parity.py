@@ -219,9 +219,24 @@ def test_noise_screen(gens, mg, version, dim):
         w = gens[version].world(dim, "normal", seed)
         bad, left, worst = mg.check_noise(w, 1 << 22, seed & 0xFFFF)
         n_values = (1 << 22) * (6 if dim.endswith("overworld") else 2)
+        print(f"{version} {dim} seed {seed}: worst error / bound {worst:.4f}, left to the exact path {left / n_values:.2e}")
         assert bad == 0
-        assert worst < 0.25
+        assert worst < 0.5
         assert left < n_values // 50
+
+
+@pytest.mark.parametrize("version", ["26.1", "26.2"])
+@pytest.mark.parametrize("preset", ["normal", "large_biomes", "amplified"])
+def test_climate_screen(gens, mg, version, preset):
+    """The double branch's Overworld climate as the kernels compute it (exact shift noises, climate noises
+    screened in fixed point) gives the plain double evaluation's six targets on 2^21 random quart cells per
+    seed out to |q| = 2^21, and the screen leaves only a small share of the cells to the exact path."""
+    for seed in (12345, -(2**62) + 17):
+        w = gens[version].world("minecraft:overworld", preset, seed)
+        bad, fallback = mg.check_climate(w, 1 << 21, seed & 0xFFFF)
+        print(f"{version} {preset} seed {seed}: cells with a value left to the exact path {fallback / (1 << 21):.2e}")
+        assert bad == 0
+        assert fallback < (1 << 21) // 10
 
 
 def test_chunk_mode_grid_hashes(gens, mg):
