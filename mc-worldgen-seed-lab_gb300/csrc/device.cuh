@@ -303,18 +303,35 @@ __device__ __forceinline__ double octave_dfix(const P &p, int ix, double fx, int
     const double x11 = fix_lerp(u, gdot_i(p(ab + iz + 1), FX, GY, GZ), gdot_i(p(bb + iz + 1), GX, GY, GZ));
     return lerp<double>(w, lerp<double>(v, x00, x10), lerp<double>(v, x01, x11));
 }
+/* the plain double octave, for a fraction that is not a multiple of 2^-52 (rare): out of line for a plain
+ * table, inline for the interleaved shared layout */
+static __device__ __noinline__ double octave_d_plain(const uint8_t *p, int ix, double fx, int iy, double fy, double v,
+                                                     int iz, double fz, double w) {
+    return octave_q<double>(PlainPerm{p}, ix, fx, iy, fy, fy - 1.0, v, iz, fz, fz - 1.0, w);
+}
+template <typename P>
+__device__ __forceinline__ double octave_d_rare(const P &p, int ix, double fx, int iy, double fy, double v, int iz,
+                                                double fz, double w) {
+    return octave_q<double>(p, ix, fx, iy, fy, fy - 1.0, v, iz, fz, fz - 1.0, w);
+}
+__device__ __forceinline__ double octave_d_rare(const PlainPerm &p, int ix, double fx, int iy, double fy, double v, int iz,
+                                                double fz, double w) {
+    return octave_d_plain(p.p, ix, fx, iy, fy, v, iz, fz, w);
+}
 /* double octave with input y (resp. z) zero: fixed point when every fraction allows it */
 template <typename P, typename H>
 __device__ __forceinline__ double octave_d_y0(const P &p, const H &h, int ix, double fx, int64_t FX, int iz, double fz,
                                               int64_t FZ) {
-    if ((FX | FZ | h.Fy) >= 0) return octave_dfix(p, ix, fx, FX, h.iy, h.Fy, h.uyd, iz, FZ, fade<double>(fz));
-    return octave_y0<double>(p, h, ix, fx, iz, fz);
+    const double w = fade<double>(fz);
+    if ((FX | FZ | h.Fy) >= 0) return octave_dfix(p, ix, fx, FX, h.iy, h.Fy, h.uyd, iz, FZ, w);
+    return octave_d_rare(p, ix, fx, h.iy, h.fyd, h.uyd, iz, fz, w);
 }
 template <typename P, typename H>
 __device__ __forceinline__ double octave_d_z0(const P &p, const H &h, int ix, double fx, int64_t FX, int iy, double fy,
                                               int64_t FY) {
-    if ((FX | FY | h.Fz) >= 0) return octave_dfix(p, ix, fx, FX, iy, FY, fade<double>(fy), h.iz, h.Fz, h.uzd);
-    return octave_z0<double>(p, h, ix, fx, iy, fy);
+    const double v = fade<double>(fy);
+    if ((FX | FY | h.Fz) >= 0) return octave_dfix(p, ix, fx, FX, iy, FY, v, h.iz, h.Fz, h.uzd);
+    return octave_d_rare(p, ix, fx, iy, fy, v, h.iz, h.fzd, h.uzd);
 }
 template <typename T>
 __device__ __forceinline__ T octave(const uint8_t *__restrict__ p, int ix, T fx, int iy, T fy, int iz, T fz) {
@@ -453,10 +470,34 @@ __device__ __forceinline__ bool scale_small(double x, int k, double &v) {
     v = __longlong_as_double((long long)(b + ((uint64_t)(int64_t)k << 52)));
     return true;
 }
+/* The plain splits (|v| >= 2^23, s in (-1, 0), tiny s: rare) carry the wrap's double division; one
+ * out-of-line copy keeps them out of the octave loops' hot code. */
+struct SplitF {
+    int i;
+    float f;
+};
+struct SplitD {
+    int i;
+    double f;
+    int64_t F;
+};
+static __device__ __noinline__ SplitF split_f_slow(double v, double off) {
+    SplitF r;
+    split_f_plain(v, off, r.i, r.f);
+    return r;
+}
+static __device__ __noinline__ SplitD split_d_slow(double v, double off) {
+    SplitD r;
+    split_d_plain(v, off, r.i, r.f);
+    r.F = fixed52(r.f);
+    return r;
+}
 __device__ __forceinline__ void split_fk(double x, double f, int k, double off, int &i, float &fr) {
     double v, fd;
     if (scale_small(x, k, v) && split_bits<true>(v + off, i, fr, fd)) return;
-    split_f_plain(x * f, off, i, fr);
+    const SplitF r = split_f_slow(x * f, off);
+    i = r.i;
+    fr = r.f;
 }
 /* Double-branch split of s = v + off that also gives the fraction in units of 2^-52 (F, or -1 when the
  * fraction is not a multiple of 2^-52); false where the plain arithmetic must be used. */
@@ -506,40 +547,39 @@ __device__ __forceinline__ bool split_bits_d(double s, int &i, double &fd, int64
 __device__ __forceinline__ void split_dk(double x, double f, int k, double off, int &i, double &fr, int64_t &F) {
     double v;
     if (scale_small(x, k, v) && split_bits_d(v + off, i, fr, F)) return;
-    split_d_plain(x * f, off, i, fr);
-    F = fixed52(fr);
+    const SplitD r = split_d_slow(x * f, off);
+    i = r.i;
+    fr = r.f;
+    F = r.F;
 }
 
-/* Octave with input (x*f, 0, z*f) and with input (x*f, y*f, 0); the zero coordinate uses the table's split. */
-__device__ __forceinline__ float oct_f_y0(const MgLattice *__restrict__ L, double x, double z, double f, int k) {
-    int ix, iz;
-    float fx, fz;
-    split_fk(x, f, k, L->ox, ix, fx);
-    split_fk(z, f, k, L->oz, iz, fz);
-    return octave_y0<float>(PlainPerm{L->p}, *L, ix, fx, iz, fz);
+/* Octave of lattice L with input (a*f, 0, b*f) (z0 false) or (a*f, b*f, 0) (z0 true); the zero coordinate
+ * uses the table's split.  One copy serves both forms (the zero coordinate's values are selected), which
+ * keeps the noise loops' code small. */
+__device__ __forceinline__ float oct_f(const MgLattice *__restrict__ L, double a, double b, double f, int k, bool z0) {
+    int ia, ib;
+    float fa, fb;
+    split_fk(a, f, k, L->ox, ia, fa);
+    split_fk(b, f, k, z0 ? L->oy : L->oz, ib, fb);
+    const int i0 = z0 ? L->iz : L->iy;
+    const float f0 = z0 ? L->z0.f.fz : L->z0.f.fy, u0 = z0 ? L->z0.f.uz : L->z0.f.uy, ub = fade<float>(fb);
+    const int iy = z0 ? ib : i0, iz = z0 ? i0 : ib;
+    const float fy = z0 ? fb : f0, fz = z0 ? f0 : fb, v = z0 ? ub : u0, w = z0 ? u0 : ub;
+    return octave_q<float>(PlainPerm{L->p}, ia, fa, iy, fy, fy - 1.0f, v, iz, fz, fz - 1.0f, w);
 }
-__device__ __forceinline__ float oct_f_z0(const MgLattice *__restrict__ L, double x, double y, double f, int k) {
-    int ix, iy;
-    float fx, fy;
-    split_fk(x, f, k, L->ox, ix, fx);
-    split_fk(y, f, k, L->oy, iy, fy);
-    return octave_z0<float>(PlainPerm{L->p}, *L, ix, fx, iy, fy);
-}
-__device__ __forceinline__ double oct_d_y0(const MgLattice *__restrict__ L, double x, double z, double f, int k) {
-    int ix, iz;
-    double fx, fz;
-    int64_t FX, FZ;
-    split_dk(x, f, k, L->ox, ix, fx, FX);
-    split_dk(z, f, k, L->oz, iz, fz, FZ);
-    return octave_d_y0(PlainPerm{L->p}, *L, ix, fx, FX, iz, fz, FZ);
-}
-__device__ __forceinline__ double oct_d_z0(const MgLattice *__restrict__ L, double x, double y, double f, int k) {
-    int ix, iy;
-    double fx, fy;
-    int64_t FX, FY;
-    split_dk(x, f, k, L->ox, ix, fx, FX);
-    split_dk(y, f, k, L->oy, iy, fy, FY);
-    return octave_d_z0(PlainPerm{L->p}, *L, ix, fx, FX, iy, fy, FY);
+__device__ __forceinline__ double oct_d(const MgLattice *__restrict__ L, double a, double b, double f, int k, bool z0) {
+    int ia, ib;
+    double fa, fb;
+    int64_t FA, FB;
+    split_dk(a, f, k, L->ox, ia, fa, FA);
+    split_dk(b, f, k, z0 ? L->oy : L->oz, ib, fb, FB);
+    const int i0 = z0 ? L->iz : L->iy;
+    const int64_t F0 = z0 ? L->Fz : L->Fy;
+    const double f0 = z0 ? L->fzd : L->fyd, u0 = z0 ? L->uzd : L->uyd, ub = fade<double>(fb);
+    const int iy = z0 ? ib : i0, iz = z0 ? i0 : ib;
+    const double v = z0 ? ub : u0, w = z0 ? u0 : ub;
+    if ((FA | FB | F0) >= 0) return octave_dfix(PlainPerm{L->p}, ia, fa, FA, iy, z0 ? FB : F0, v, iz, z0 ? F0 : FB, w);
+    return octave_d_plain(L->p, ia, fa, iy, z0 ? fb : f0, v, iz, z0 ? f0 : fb, w);
 }
 
 /* ------------------------------------------------------------------ NormalNoise (engine/mc_noise.h:285-324)
@@ -549,66 +589,57 @@ __device__ __forceinline__ double oct_d_z0(const MgLattice *__restrict__ L, doub
  * Every NormalNoise on the biome path has one input coordinate equal to zero: the five climate noises
  * and the Nether noises take (x, 0, z), ShiftA (x, 0, z), ShiftB (z, x, 0).  The second stack's input
  * x*(f*c) equals (x*c)*f exactly (f = 2^k), so xc = x*c is formed once per point. */
-/* float branch, non-legacy (interleaved first_k, second_k) */
-static __device__ __noinline__ float nn_f_y0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
-                                         double xc, double zc) {
+/* float branch, non-legacy (interleaved first_k, second_k); input (a, 0, b), or (a, b, 0) when z0 */
+static __device__ __noinline__ float nn_f(const MgNoise &N, const MgLattice *__restrict__ T, double a, double b,
+                                          double ac, double bc, bool z0) {
     float acc = 0.0f;
     const MgLattice *A = T + N.base, *B = A + N.nlev;
     for (int k = 0; k < N.nlev; k++) {
         double f = N.freq[k];
-        acc += N.amp_f[k] * oct_f_y0(A + k, x, z, f, N.fexp[k]);
-        acc += N.amp_f[k] * oct_f_y0(B + k, xc, zc, f, N.fexp[k]);
+        acc += N.amp_f[k] * oct_f(A + k, a, b, f, N.fexp[k], z0);
+        acc += N.amp_f[k] * oct_f(B + k, ac, bc, f, N.fexp[k], z0);
     }
     return acc;
 }
-static __device__ __noinline__ float nn_f_z0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double y,
+__device__ __forceinline__ float nn_f_y0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
+                                         double xc, double zc) {
+    return nn_f(N, T, x, z, xc, zc, false);
+}
+__device__ __forceinline__ float nn_f_z0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double y,
                                          double xc, double yc) {
-    float acc = 0.0f;
-    const MgLattice *A = T + N.base, *B = A + N.nlev;
-    for (int k = 0; k < N.nlev; k++) {
-        double f = N.freq[k];
-        acc += N.amp_f[k] * oct_f_z0(A + k, x, y, f, N.fexp[k]);
-        acc += N.amp_f[k] * oct_f_z0(B + k, xc, yc, f, N.fexp[k]);
-    }
-    return acc;
+    return nn_f(N, T, x, y, xc, yc, true);
 }
 /* float branch, legacy Nether form (whole first stack, then whole second stack) */
 static __device__ __noinline__ float nn_f_legacy_y0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
                                                 double xc, double zc) {
     float acc = 0.0f;
     const MgLattice *A = T + N.base, *B = A + N.nlev;
-    for (int k = 0; k < N.nlev; k++) acc += N.amp_f[k] * oct_f_y0(A + k, x, z, N.freq[k], N.fexp[k]);
-    for (int k = 0; k < N.nlev; k++) acc += N.amp_f[k] * oct_f_y0(B + k, xc, zc, N.freq[k], N.fexp[k]);
+    for (int k = 0; k < N.nlev; k++) acc += N.amp_f[k] * oct_f(A + k, x, z, N.freq[k], N.fexp[k], false);
+    for (int k = 0; k < N.nlev; k++) acc += N.amp_f[k] * oct_f(B + k, xc, zc, N.freq[k], N.fexp[k], false);
     return acc;
 }
-/* double branch: (first + second) * valueFactor */
-static __device__ __noinline__ double nn_d_y0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
-                                          double xc, double zc) {
-    double a = 0.0, b = 0.0;
+/* double branch: (first + second) * valueFactor; input (a, 0, b), or (a, b, 0) when z0 */
+static __device__ __noinline__ double nn_d(const MgNoise &N, const MgLattice *__restrict__ T, double a, double b,
+                                           double ac, double bc, bool z0) {
+    double s1 = 0.0, s2 = 0.0;
     const MgLattice *A = T + N.base, *B = A + N.nlev;
     /* the two stacks' sums advance together (two independent octaves in flight); each keeps its order */
     for (int k = 0; k < N.nlev; k++) {
         const double f = N.freq[k];
-        const double oa = oct_d_y0(A + k, x, z, f, N.fexp[k]);
-        const double ob = oct_d_y0(B + k, xc, zc, f, N.fexp[k]);
-        a += N.amp_d[k] * oa * N.vf_d[k];
-        b += N.amp_d[k] * ob * N.vf_d[k];
+        const double oa = oct_d(A + k, a, b, f, N.fexp[k], z0);
+        const double ob = oct_d(B + k, ac, bc, f, N.fexp[k], z0);
+        s1 += N.amp_d[k] * oa * N.vf_d[k];
+        s2 += N.amp_d[k] * ob * N.vf_d[k];
     }
-    return (a + b) * N.vfac;
+    return (s1 + s2) * N.vfac;
 }
-static __device__ __noinline__ double nn_d_z0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double y,
+__device__ __forceinline__ double nn_d_y0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
+                                          double xc, double zc) {
+    return nn_d(N, T, x, z, xc, zc, false);
+}
+__device__ __forceinline__ double nn_d_z0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double y,
                                           double xc, double yc) {
-    double a = 0.0, b = 0.0;
-    const MgLattice *A = T + N.base, *B = A + N.nlev;
-    /* the two stacks' sums advance together (two independent octaves in flight); each keeps its order */
-    for (int k = 0; k < N.nlev; k++) {
-        const double f = N.freq[k];
-        const double oa = oct_d_z0(A + k, x, y, f, N.fexp[k]);
-        const double ob = oct_d_z0(B + k, xc, yc, f, N.fexp[k]);
-        a += N.amp_d[k] * oa * N.vf_d[k];
-        b += N.amp_d[k] * ob * N.vf_d[k];
-    }
-    return (a + b) * N.vfac;
+    return nn_d(N, T, x, y, xc, yc, true);
 }
 
 /* double branch, screened: the NormalNoise value in fixed point (every level's amplitude, level value

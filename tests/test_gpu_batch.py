@@ -79,6 +79,11 @@ def test_batch_equals_plain_and_replays(env):
         worlds[k].quart_grid_seed_dev(s, qx0, qz0, nx, nz, qy, 0, plain.data_ptr() + plan.offset(i), stream)
     assert np.array_equal(plain.cpu().numpy(), first)
     # every tile shape the autotuner tries gives the same ids
+    for shape in range(4):
+        plan.shape = shape
+        d_out.fill_(0xEE)
+        plan.run_dev(d_out.data_ptr(), stream)
+        assert np.array_equal(d_out.cpu().numpy(), first), shape
     ms = plan.autotune(d_out.data_ptr(), reps=1)
     assert ms > 0 and 0 <= plan.shape < 4
     plan.run_dev(d_out.data_ptr(), stream)
