@@ -594,6 +594,8 @@ static __device__ __noinline__ float nn_f(const MgNoise &N, const MgLattice *__r
                                           double ac, double bc, bool z0) {
     float acc = 0.0f;
     const MgLattice *A = T + N.base, *B = A + N.nlev;
+    /* two octaves per level in flight (the float path's code is small; its instruction cache is not the
+     * limit, unlike the double branch's) */
     for (int k = 0; k < N.nlev; k++) {
         double f = N.freq[k];
         acc += N.amp_f[k] * oct_f(A + k, a, b, f, N.fexp[k], z0);
@@ -621,17 +623,17 @@ static __device__ __noinline__ float nn_f_legacy_y0(const MgNoise &N, const MgLa
 /* double branch: (first + second) * valueFactor; input (a, 0, b), or (a, b, 0) when z0 */
 static __device__ __noinline__ double nn_d(const MgNoise &N, const MgLattice *__restrict__ T, double a, double b,
                                            double ac, double bc, bool z0) {
-    double s1 = 0.0, s2 = 0.0;
-    const MgLattice *A = T + N.base, *B = A + N.nlev;
-    /* the two stacks' sums advance together (two independent octaves in flight); each keeps its order */
-    for (int k = 0; k < N.nlev; k++) {
-        const double f = N.freq[k];
-        const double oa = oct_d(A + k, a, b, f, N.fexp[k], z0);
-        const double ob = oct_d(B + k, ac, bc, f, N.fexp[k], z0);
-        s1 += N.amp_d[k] * oa * N.vf_d[k];
-        s2 += N.amp_d[k] * ob * N.vf_d[k];
+    double s[2] = {0.0, 0.0};
+    const MgLattice *A = T + N.base;
+    /* the two stacks' sums advance together in one loop (one copy of the octave code); each keeps its order */
+    for (int j = 0; j < 2 * N.nlev; j++) {
+        const int k = j >> 1, st = j & 1;
+        const double o = oct_d(A + st * N.nlev + k, st ? ac : a, st ? bc : b, N.freq[k], N.fexp[k], z0);
+        const double t = N.amp_d[k] * o * N.vf_d[k];
+        if (st) s[1] += t;
+        else s[0] += t;
     }
-    return (s1 + s2) * N.vfac;
+    return (s[0] + s[1]) * N.vfac;
 }
 __device__ __forceinline__ double nn_d_y0(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
                                           double xc, double zc) {
@@ -651,28 +653,29 @@ __device__ __forceinline__ double nn_d_z0(const MgNoise &N, const MgLattice *__r
 template <bool Z0>
 static __device__ __noinline__ int64_t nn_q(const MgNoise &N, const MgLattice *__restrict__ T, double a, double b,
                                             double ac, double bc) {
-    int64_t acc = 0;
+    int64_t acc = 0, lev = 0;
     const MgLattice *A = T + N.base;
-    /* per level, the two stacks' octaves (independent: two dependency chains in flight), then one product
-     * with the level's constant (the sum is exact, so its order is free) */
-    for (int k = 0; k < N.nlev; k++) {
+    /* one loop over both stacks' levels, one copy of the octave code (the kernels' hot code stays small);
+     * a level's two octaves are summed before the product with the level's constant (the sum is exact, so
+     * its order is free) */
+    for (int j = 0; j < 2 * N.nlev; j++) {
+        const int k = j >> 1, st = j & 1;
+        const MgLattice *L = A + st * N.nlev + k;
         const double f = N.freq[k];
-        int64_t o[2];
-#pragma unroll
-        for (int st = 0; st < 2; st++) {
-            const MgLattice *L = A + st * N.nlev + k;
-            int ia, ib;
-            double fa, fb;
-            int64_t FA, FB;
-            split_dk(st ? ac : a, f, N.fexp[k], L->ox, ia, fa, FA);
-            split_dk(st ? bc : b, f, N.fexp[k], Z0 ? L->oy : L->oz, ib, fb, FB);
-            const int64_t F0 = Z0 ? L->Fz : L->Fy;
-            if ((FA | FB | F0) < 0) return MG_QFAIL;
-            const int64_t XA = FA << (MG_Q - 52), XB = FB << (MG_Q - 52), X0 = F0 << (MG_Q - 52);
-            o[st] = Z0 ? octave_qfix(PlainPerm{L->p}, ia, XA, ib, XB, fadeq(XB), L->iz, X0, L->z0.q.uz)
-                       : octave_qfix(PlainPerm{L->p}, ia, XA, L->iy, X0, L->z0.q.uy, ib, XB, fadeq(XB));
+        int ia, ib;
+        double fa, fb;
+        int64_t FA, FB;
+        split_dk(st ? ac : a, f, N.fexp[k], L->ox, ia, fa, FA);
+        split_dk(st ? bc : b, f, N.fexp[k], Z0 ? L->oy : L->oz, ib, fb, FB);
+        const int64_t F0 = Z0 ? L->Fz : L->Fy;
+        if ((FA | FB | F0) < 0) return MG_QFAIL;
+        const int64_t XA = FA << (MG_Q - 52), XB = FB << (MG_Q - 52), X0 = F0 << (MG_Q - 52);
+        lev += Z0 ? octave_qfix(PlainPerm{L->p}, ia, XA, ib, XB, fadeq(XB), L->iz, X0, L->z0.q.uz)
+                  : octave_qfix(PlainPerm{L->p}, ia, XA, L->iy, X0, L->z0.q.uy, ib, XB, fadeq(XB));
+        if (st) {
+            acc += mulq(N.cq[k], lev);
+            lev = 0;
         }
-        acc += mulq(N.cq[k], o[0] + o[1]);
     }
     return acc;
 }
