@@ -772,9 +772,10 @@ __device__ __forceinline__ uint64_t node_dist(const MgTreeNode &n, const int32_t
     return s;
 }
 /* Climate.RTree.SubTree.search, iterative: descend into a child iff its box distance is below the best
- * leaf distance so far; a leaf replaces the best iff strictly closer.  cand < 0: no candidate. */
-__device__ __forceinline__ int tree_search(const MgTreeNode *__restrict__ T, const int32_t *t, int cand,
-                                           uint64_t &best) {
+ * leaf distance so far; a leaf replaces the best iff strictly closer.  cand < 0: no candidate.  The
+ * general form (explicit stack, 64-bit distances); tree_search below is the fast one. */
+__device__ __forceinline__ int tree_search_stack(const MgTreeNode *__restrict__ T, const int32_t *t, int cand,
+                                                 uint64_t &best) {
     int res = cand;
     best = cand < 0 ? ~0ULL : node_dist(T[cand], t);
     int stk_node[10];
@@ -803,8 +804,8 @@ __device__ __forceinline__ int tree_search(const MgTreeNode *__restrict__ T, con
  * first leaf to reach the minimum in tree order is kept -- the leaf tree_search returns, since no leaf
  * before it in tree order is as close -- and the leaves at the minimum are counted (capped at 2; the
  * tie test of libmcgen/src/biome.c:76-85). */
-__device__ __forceinline__ int tree_search_tie(const MgTreeNode *__restrict__ T, const int32_t *t, uint64_t &best,
-                                               bool &tied) {
+__device__ __forceinline__ int tree_search_tie_stack(const MgTreeNode *__restrict__ T, const int32_t *t, uint64_t &best,
+                                                     bool &tied) {
     int stk_node[10], stk_next[10], sp = 1, res = -1, cnt = 0;
     best = ~0ULL;
     stk_node[0] = 0;
@@ -826,6 +827,77 @@ __device__ __forceinline__ int tree_search_tie(const MgTreeNode *__restrict__ T,
     tied = cnt >= 2;
     return res;
 }
+/* The same searches with the traversal unrolled over the tree's levels (no stack in local memory: every
+ * level's loop state stays in registers; leaves lie 3 to 5 levels below the root in every table, and
+ * MG_RT_LEVELS + 1 levels below the root are unrolled) and
+ * 32-bit box distances: each dimension's distance is clamped at MG_RT_CLAMP, so six squares still fit in
+ * 32 bits, and the offset term saturates below the initial bound.  A distance below MG_RT_CLAMP^2 is exact,
+ * and a node whose distance was clamped or saturated is at least MG_RT_CLAMP^2 away, so whenever the final
+ * best distance is below MG_RT_CLAMP^2 every comparison that decided the result was exact and the result
+ * is the 64-bit search's; otherwise (or for a tree deeper than the unrolled levels) the stack form runs. */
+#define MG_RT_CLAMP 26754
+#define MG_RT_LEVELS 4
+__device__ __forceinline__ uint32_t dim_sq32(int32_t t, int32_t lo, int32_t hi) {
+    const int32_t x = min(max(max(t - hi, lo - t), 0), MG_RT_CLAMP);
+    return (uint32_t)(x * x);
+}
+struct RtTarget {
+    int32_t t[6];
+};
+struct RtState {
+    uint32_t best;
+    int res, cnt;
+};
+template <int D, bool TIE>
+__device__ __forceinline__ bool rt_walk(const MgTreeNode *__restrict__ T, int first, int count, const RtTarget &q,
+                                        RtState &s) {
+    for (int ci = first; ci < first + count; ci++) {
+        const uint4 a = *reinterpret_cast<const uint4 *>(T + ci);      /* lo[0..5], hi[0..1] */
+        const uint4 b = *(reinterpret_cast<const uint4 *>(T + ci) + 1); /* hi[2..5], d7, first | count | biome */
+        uint32_t d = dim_sq32(q.t[0], lo16(a.x), lo16(a.w)) + dim_sq32(q.t[1], hi16(a.x), hi16(a.w)) +
+                     dim_sq32(q.t[2], lo16(a.y), lo16(b.x)) + dim_sq32(q.t[3], hi16(a.y), hi16(b.x)) +
+                     dim_sq32(q.t[4], lo16(a.z), lo16(b.y)) + dim_sq32(q.t[5], hi16(a.z), hi16(b.y));
+        d = d > 0xFFFFFFFEu - b.z ? 0xFFFFFFFEu : d + b.z;
+        if (TIE ? d > s.best : d >= s.best) continue;
+        const int cc = (int)((b.w >> 16) & 0xFFu);
+        if (cc == 0) {
+            if (!TIE || d < s.best) { s.best = d; s.res = ci; s.cnt = 1; }
+            else if (s.cnt < 2) s.cnt++;
+        } else {
+            if constexpr (D == 0) return false;
+            else if (!rt_walk<D - 1, TIE>(T, (int)(b.w & 0xFFFFu), cc, q, s)) return false;
+        }
+    }
+    return true;
+}
+template <bool TIE>
+static __device__ __noinline__ RtState rt_find(const MgTreeNode *__restrict__ T, RtTarget q) {
+    RtState s{0xFFFFFFFFu, -1, 0};
+    const uint32_t w = reinterpret_cast<const uint4 *>(T)[1].w;
+    if (!rt_walk<MG_RT_LEVELS, TIE>(T, (int)(w & 0xFFFFu), (int)((w >> 16) & 0xFFu), q, s)) s.res = -2;
+    return s;
+}
+__device__ __forceinline__ int tree_search(const MgTreeNode *__restrict__ T, const int32_t *t, int cand, uint64_t &best) {
+    if (cand < 0) {
+        const RtState s = rt_find<false>(T, RtTarget{{t[0], t[1], t[2], t[3], t[4], t[5]}});
+        if (s.res >= 0 && s.best < (uint32_t)MG_RT_CLAMP * MG_RT_CLAMP) {
+            best = s.best;
+            return s.res;
+        }
+    }
+    return tree_search_stack(T, t, cand, best);
+}
+__device__ __forceinline__ int tree_search_tie(const MgTreeNode *__restrict__ T, const int32_t *t, uint64_t &best,
+                                               bool &tied) {
+    const RtState s = rt_find<true>(T, RtTarget{{t[0], t[1], t[2], t[3], t[4], t[5]}});
+    if (s.res >= 0 && s.best < (uint32_t)MG_RT_CLAMP * MG_RT_CLAMP) {
+        best = s.best;
+        tied = s.cnt >= 2;
+        return s.res;
+    }
+    return tree_search_tie_stack(T, t, best, tied);
+}
+
 /* (long)(v * 10000f) */
 __device__ __forceinline__ int32_t quantize(float v) { return (int32_t)(int64_t)(v * 10000.0f); }
 
