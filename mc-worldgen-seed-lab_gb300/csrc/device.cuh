@@ -870,6 +870,44 @@ __device__ __forceinline__ bool rt_walk(const MgTreeNode *__restrict__ T, int fi
     }
     return true;
 }
+/* the same traversal as one loop with an explicit stack of (next child, end) per level: lanes of a warp
+ * whose searches take different paths stay in step (one loop body), which the unrolled form, with one loop
+ * per level, does not give when a warp's targets are unrelated (many seeds at scattered points) */
+#define MG_RT_STACK 8
+template <bool TIE>
+static __device__ __noinline__ RtState rt_find_flat(const MgTreeNode *__restrict__ T, RtTarget q) {
+    RtState s{0xFFFFFFFFu, -1, 0};
+    int nxt[MG_RT_STACK], end[MG_RT_STACK];
+    const uint32_t w = reinterpret_cast<const uint4 *>(T)[1].w;
+    int sp = 0;
+    nxt[0] = (int)(w & 0xFFFFu);
+    end[0] = nxt[0] + (int)((w >> 16) & 0xFFu);
+    while (sp >= 0) {
+        const int ci = nxt[sp];
+        if (ci >= end[sp]) { sp--; continue; }
+        nxt[sp] = ci + 1;
+        const uint4 a = *reinterpret_cast<const uint4 *>(T + ci);
+        const uint4 b = *(reinterpret_cast<const uint4 *>(T + ci) + 1);
+        uint32_t d = dim_sq32(q.t[0], lo16(a.x), lo16(a.w)) + dim_sq32(q.t[1], hi16(a.x), hi16(a.w)) +
+                     dim_sq32(q.t[2], lo16(a.y), lo16(b.x)) + dim_sq32(q.t[3], hi16(a.y), hi16(b.x)) +
+                     dim_sq32(q.t[4], lo16(a.z), lo16(b.y)) + dim_sq32(q.t[5], hi16(a.z), hi16(b.y));
+        d = d > 0xFFFFFFFEu - b.z ? 0xFFFFFFFEu : d + b.z;
+        if (TIE ? d > s.best : d >= s.best) continue;
+        const int cc = (int)((b.w >> 16) & 0xFFu);
+        if (cc == 0) {
+            if (!TIE || d < s.best) { s.best = d; s.res = ci; s.cnt = 1; }
+            else if (s.cnt < 2) s.cnt++;
+        } else if (sp + 1 < MG_RT_STACK) {
+            sp++;
+            nxt[sp] = (int)(b.w & 0xFFFFu);
+            end[sp] = nxt[sp] + cc;
+        } else {
+            s.res = -2; /* deeper than the stack: the 64-bit search decides */
+            return s;
+        }
+    }
+    return s;
+}
 template <bool TIE>
 static __device__ __noinline__ RtState rt_find(const MgTreeNode *__restrict__ T, RtTarget q) {
     RtState s{0xFFFFFFFFu, -1, 0};
@@ -877,15 +915,26 @@ static __device__ __noinline__ RtState rt_find(const MgTreeNode *__restrict__ T,
     if (!rt_walk<MG_RT_LEVELS, TIE>(T, (int)(w & 0xFFFFu), (int)((w >> 16) & 0xFFu), q, s)) s.res = -2;
     return s;
 }
-__device__ __forceinline__ int tree_search(const MgTreeNode *__restrict__ T, const int32_t *t, int cand, uint64_t &best) {
+/* tree_search / tree_search_tie for warps whose cells are neighbours (grids, batches: similar targets, so
+ * similar paths), tree_search_scattered for unrelated targets (many seeds, point lists, the seed search) */
+template <bool FLAT>
+__device__ __forceinline__ int tree_search_t(const MgTreeNode *__restrict__ T, const int32_t *t, int cand, uint64_t &best) {
     if (cand < 0) {
-        const RtState s = rt_find<false>(T, RtTarget{{t[0], t[1], t[2], t[3], t[4], t[5]}});
+        const RtTarget q{{t[0], t[1], t[2], t[3], t[4], t[5]}};
+        const RtState s = FLAT ? rt_find_flat<false>(T, q) : rt_find<false>(T, q);
         if (s.res >= 0 && s.best < (uint32_t)MG_RT_CLAMP * MG_RT_CLAMP) {
             best = s.best;
             return s.res;
         }
     }
     return tree_search_stack(T, t, cand, best);
+}
+__device__ __forceinline__ int tree_search(const MgTreeNode *__restrict__ T, const int32_t *t, int cand, uint64_t &best) {
+    return tree_search_t<false>(T, t, cand, best);
+}
+__device__ __forceinline__ int tree_search_scattered(const MgTreeNode *__restrict__ T, const int32_t *t, int cand,
+                                                     uint64_t &best) {
+    return tree_search_t<true>(T, t, cand, best);
 }
 __device__ __forceinline__ int tree_search_tie(const MgTreeNode *__restrict__ T, const int32_t *t, uint64_t &best,
                                                bool &tied) {

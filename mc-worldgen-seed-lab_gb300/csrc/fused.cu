@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(128) k_ow_finish_tree(const __grid_constant__ 
     if (FM) climate_finish_f(W, S, (float)v[0], (float)v[1], (float)v[2], (float)v[3], (float)v[4], by, tg);
     else climate_finish_d(W, S, (double)v[0], (double)v[1], (double)v[2], (double)v[3], (double)v[4], by, tg);
     uint64_t d;
-    const int leaf = tree_search(tree, tg, -1, d);
+    const int leaf = tree_search_scattered(tree, tg, -1, d);
     out[g] = tree[leaf].biome;
     if (targets)
         for (int k = 0; k < 6; k++) targets[g * 6 + k] = tg[k];

@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(128) k_points(const __grid_constant__ MgWorldD
     }
     cell_target<FM, DIM>(W, S, T, qx, qy, qz, tg);
     uint64_t d;
-    int leaf = tree_search(tree, tg, -1, d);
+    int leaf = tree_search_scattered(tree, tg, -1, d);
     out[g] = tree[leaf].biome;
     if (targets)
         for (int k = 0; k < 6; k++) targets[g * 6 + k] = tg[k];

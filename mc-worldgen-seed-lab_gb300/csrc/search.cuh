@@ -97,7 +97,7 @@ __device__ __forceinline__ void tree_ties(const MgTreeNode *__restrict__ T, cons
 __device__ __forceinline__ bool obs_accept(const MgObs &o, const MgTreeNode *__restrict__ T, const int32_t *tg, bool ties) {
     if (!ties) {
         uint64_t d;
-        return obs_in(o, T[tree_search(T, tg, -1, d)].biome);
+        return obs_in(o, T[tree_search_scattered(T, tg, -1, d)].biome);
     }
     uint64_t m[2];
     tree_ties(T, tg, m);
