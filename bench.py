@@ -530,9 +530,49 @@ def run_batch(args, rank, world, local_rank, mg, ge):
                                                "size, where the output no longer fits L2",
                                "work": f"{ops:.4g} FP64 ops per launch (per-sample model of the screened evaluation)",
                                "peak_source": "measured in-run (FP64 add pipe microbenchmark)"}
+        if args.split_classes:
+            out["classes"] = batch_classes(reqs, worlds, mg, dev, stream)
         if not args.skip_extras:
             out["cpu_baseline"] = cpu_baseline_batch(reqs, args.cpu_sample_s)
         print(json.dumps(out), flush=True)
+
+
+# code-path classes of the uneven batch (--split-classes): the double branch (26.1/26.2) and the float
+# branch (26.3) of the Overworld and the Nether, and the End
+BATCH_CLASSES = {
+    "overworld_double": lambda v, d: d.endswith("overworld") and v in DOUBLE_BRANCH,
+    "overworld_float": lambda v, d: d.endswith("overworld") and v not in DOUBLE_BRANCH,
+    "nether_double": lambda v, d: d.endswith("nether") and v in DOUBLE_BRANCH,
+    "nether_float": lambda v, d: d.endswith("nether") and v not in DOUBLE_BRANCH,
+    "end": lambda v, d: d.endswith("end"),
+}
+
+
+def batch_classes(reqs, worlds, mg, dev, stream) -> dict:
+    """Each class's requests as a plan of their own (autotuned), mean of 3 graph runs: where a step's time
+    goes."""
+    import torch
+
+    out = {}
+    for name, f in BATCH_CLASSES.items():
+        sub = [r for r in reqs if f(r[0], r[1])]
+        if not sub:
+            continue
+        plan = mg.Plan([(worlds[(v, d)], s, qx0, qz0, n, n, qy) for v, d, s, qx0, qz0, n, qy in sub])
+        d_out = torch.empty(plan.output_bytes, dtype=torch.uint8, device=dev)
+        plan.autotune(d_out.data_ptr(), reps=1)
+        plan.run_dev(d_out.data_ptr(), stream.cuda_stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            plan.run_dev(d_out.data_ptr(), stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / 3
+        out[name] = {"requests": len(sub), "samples": plan.output_bytes, "ms": round(ms, 3),
+                     "ns_per_sample": round(ms * 1e6 / plan.output_bytes, 4), "tile_shape": plan.shape}
+        plan.close()
+    return out
 
 
 def cpu_baseline_batch(reqs, budget_s: float) -> dict:
@@ -1069,6 +1109,8 @@ def main():
     ap.add_argument("--rates", default="500,1000,2000", help="serve: arrival rates (requests/s)")
     ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds per rate (60 = the configuration)")
     ap.add_argument("--requests", type=int, default=10000, help="batch10k: number of requests")
+    ap.add_argument("--split-classes", action="store_true",
+                    help="batch10k: also time each code-path class's requests as a plan of their own")
     ap.add_argument("--cpu-sample-s", type=float, default=12.0)
     ap.add_argument("--seeds", type=int, default=65536, help="seeds8: number of seeds (65536 = the configuration)")
     ap.add_argument("--skip-extras", action="store_true",

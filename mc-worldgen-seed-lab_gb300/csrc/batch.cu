@@ -179,7 +179,7 @@ __device__ __forceinline__ void batch_end(const MgWorldDesc &W, BatchSmem &sm, c
 }
 
 /* TILE_W: tile width in cells (tiles are 128 cells); MINB: resident CTAs per SM the register allocation
- * is sized for (4: 128 registers, 6: 80, 8: 64) */
+ * is sized for (6: 80 registers, 7: 72, 8: 64) */
 template <int TILE_W, int MINB>
 __global__ void __launch_bounds__(BNT, MINB) k_batch(const MgWorldDesc *__restrict__ worlds, const MgTreeNode *const *__restrict__ trees,
                                                const MgBatchReq *__restrict__ reqs, int nreq, long long ntiles,
@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(BNT, MINB) k_batch(const MgWorldDesc *__restri
 }
 
 /* ---------------------------------------------------------------- host side */
-/* tile shapes the autotuner chooses from: tile width, and the register budget (resident CTAs per SM: 8, 4,
+/* tile shapes the autotuner chooses from: tile width, and the register budget (resident CTAs per SM: 8, 7,
  * 6, 8) in k_batch's second template argument */
 const int kBatchTileWidths[BATCH_SHAPES] = {32, 8, 8, 8};
 static int g_resident[BATCH_SHAPES] = {0, 0, 0, 0}; /* CTAs per SM x SMs, per shape (batch_prepare) */
@@ -300,7 +300,7 @@ int batch_prepare(int *ctas_per_sm) {
         return 0;
     }
     int rc = prepare_t<32, 8>(0, sms);
-    if (!rc) rc = prepare_t<8, 4>(1, sms);
+    if (!rc) rc = prepare_t<8, 7>(1, sms);
     if (!rc) rc = prepare_t<8, 6>(2, sms);
     if (!rc) rc = prepare_t<8, 8>(3, sms);
     if (!rc) prepared_dev = dev;
@@ -322,7 +322,7 @@ int launch_batch(const MgWorldDesc *d_worlds, const MgTreeNode *const *d_trees, 
     ProfScope ps_(K_BATCH, st);
     const size_t sm = sizeof(BatchSmem);
     switch (shape) {
-    case 1: k_batch<8, 4><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
+    case 1: k_batch<8, 7><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
     case 2: k_batch<8, 6><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
     case 3: k_batch<8, 8><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
     default: k_batch<32, 8><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
