@@ -192,6 +192,12 @@ MCGEN_API int mcgen_gb300_check_noise(const McWorld *w, long long n, unsigned lo
  * float-branch, Nether and End worlds. */
 MCGEN_API int mcgen_gb300_check_climate(const McWorld *w, long long n, unsigned long long seed, long long *bad,
                                         long long *fallback);
+/* Device self-check of the R-tree searches of a world's tree (Overworld or Nether): the level-unrolled and
+ * single-loop searches with 32-bit box distances, and the tie search, against the 64-bit stack searches on
+ * n random targets (half of them beyond the 32-bit distances' clamp).  *bad_leaf counts differing leaves,
+ * *bad_other differing fitness values or tie flags.  MCGEN_E_ARG for End worlds. */
+MCGEN_API int mcgen_gb300_check_tree(const McWorld *w, long long n, unsigned long long seed, long long *bad_leaf,
+                                     long long *bad_other);
 
 /* Pipe microbenchmarks on the current device, in giga-operations per second:
  * 0 FP32 FMA, 1 FP64 FMA, 2 FP64 add, 3 int32 multiply-add, 4 double->int floor conversion,

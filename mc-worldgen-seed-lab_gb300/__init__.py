@@ -97,6 +97,8 @@ _PROTOS = {
                                           C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
     "mcgen_gb300_check_climate": (C.c_int, [_P, C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong),
                                             C.POINTER(C.c_longlong)]),
+    "mcgen_gb300_check_tree": (C.c_int, [_P, C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong),
+                                         C.POINTER(C.c_longlong)]),
     "mcgen_gb300_search": (C.c_int, [_P, C.c_int, _P, C.c_uint64, C.c_uint64, _P, C.c_int, C.c_int, _P, C.c_uint32,
                                      C.POINTER(C.c_uint32), _P, C.POINTER(C.c_double)]),
     "mcgen_gb300_obs_end_radius": (C.c_int, [_P, _P]),
@@ -251,6 +253,14 @@ def check_climate(world: "World", n: int, seed: int = 1) -> tuple[int, int]:
     b, c = C.c_longlong(), C.c_longlong()
     _check(load().mcgen_gb300_check_climate(world.handle, n, seed, C.byref(b), C.byref(c)),
            "mcgen_gb300_check_climate")
+    return b.value, c.value
+
+
+def check_tree(world: "World", n: int, seed: int = 1) -> tuple[int, int]:
+    """(differing leaves, differing fitness values or tie flags) of the 32-bit R-tree searches against the
+    64-bit stack searches on n random targets of the world's tree."""
+    b, c = C.c_longlong(), C.c_longlong()
+    _check(load().mcgen_gb300_check_tree(world.handle, n, seed, C.byref(b), C.byref(c)), "mcgen_gb300_check_tree")
     return b.value, c.value
 
 

@@ -8,7 +8,8 @@
  * BiomeManager's zoom (zoom_pick) against the double-precision choice among all 8 candidates, the
  * fixed-point screen of the double branch's climate noises (nn_q + cast_settled) against the exact double
  * evaluation on a world's own seed lattices, and the double branch's whole Overworld climate as the kernels
- * compute it (climate_ow_d) against the plain double evaluation. */
+ * compute it (climate_ow_d) against the plain double evaluation, and the 32-bit R-tree searches against
+ * the 64-bit stack searches. */
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -228,7 +229,59 @@ __global__ void k_check_climate(const __grid_constant__ MgWorldDesc W, const MgL
     atomicAdd(&out[1], left);
 }
 
+/* R-tree searches: the level-unrolled and single-loop 32-bit searches (ENGINE rule) and the unrolled tie
+ * search against the 64-bit stack searches, on random targets: quantised climate values in [-12000, 12000]
+ * (the tables' range) for half of the cases, in [-40000, 40000] (beyond the 32-bit clamp, where the exact
+ * 64-bit search must take over) for the other half, and neighbours of the previous case's target (small
+ * moves, many ties) for a quarter.  out: differing leaves, differing fitness or tie flags. */
+__global__ void k_check_tree(const MgTreeNode *__restrict__ T, long long n, uint64_t seed, unsigned long long *out) {
+    unsigned long long bad_leaf = 0, bad_other = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        uint64_t r = mix64(seed ^ mix64((uint64_t)i));
+        const int range = (r & 1) ? 40000 : 12000;
+        const bool near = ((r >> 1) & 3) == 0;
+        int32_t t[6];
+        for (int k = 0; k < 6; k++) {
+            r = mix64(r);
+            t[k] = near ? (int32_t)(r % 2001) - 1000 + (int32_t)((r >> 20) % 7) * 1500 - 4500
+                        : (int32_t)(r % (uint64_t)(2 * range + 1)) - range;
+        }
+        uint64_t d0, d1, d2, d3, d4;
+        bool tie0, tie1;
+        const int l0 = mgd::tree_search_stack(T, t, -1, d0);
+        const int l1 = mgd::tree_search(T, t, -1, d1);
+        const int l2 = mgd::tree_search_scattered(T, t, -1, d2);
+        const int l3 = mgd::tree_search_tie_stack(T, t, d3, tie0);
+        const int l4 = mgd::tree_search_tie(T, t, d4, tie1);
+        bad_leaf += (l1 != l0) + (l2 != l0) + (l3 != l0) + (l4 != l0);
+        bad_other += (d1 != d0) + (d2 != d0) + (d3 != d0) + (d4 != d0) + (tie0 != tie1);
+    }
+    atomicAdd(&out[0], bad_leaf);
+    atomicAdd(&out[1], bad_other);
+}
+
 }  // namespace
+
+extern "C" MCGEN_API int mcgen_gb300_check_tree(const McWorld *w, long long n, unsigned long long seed, long long *bad_leaf,
+                                                long long *bad_other) {
+    if (!w || n < 0 || !bad_leaf || !bad_other) return MCGEN_E_ARG;
+    if (w->desc.dim == MG_END) return MCGEN_E_ARG; /* the End has no climate tree */
+    std::lock_guard<std::mutex> lk(mg::abi_lock());
+    if (!mg::abi_device_ready()) return MCGEN_E_UNSUPPORTED;
+    int rc = mg::abi_world_device(const_cast<McWorld *>(w));
+    if (rc) return rc;
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, 2 * sizeof(unsigned long long)) != cudaSuccess) return MCGEN_E_NOMEM;
+    cudaMemset(d, 0, 2 * sizeof(unsigned long long));
+    k_check_tree<<<152 * 4, 128>>>(w->d_tree, n, seed, d);
+    unsigned long long h[2] = {0, 0};
+    cudaError_t e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return MCGEN_E_INTERNAL;
+    *bad_leaf = (long long)h[0];
+    *bad_other = (long long)h[1];
+    return MCGEN_OK;
+}
 
 extern "C" MCGEN_API int mcgen_gb300_check_climate(const McWorld *w, long long n, unsigned long long seed, long long *bad,
                                                    long long *fallback) {

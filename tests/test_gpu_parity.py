@@ -239,6 +239,20 @@ def test_climate_screen(gens, mg, version, preset):
         assert fallback < (1 << 21) // 10
 
 
+@pytest.mark.parametrize("version", ["26.1", "26.3"])
+@pytest.mark.parametrize("preset", ["normal", "large_biomes"])
+@pytest.mark.parametrize("dim", ["minecraft:overworld", "minecraft:the_nether"])
+def test_tree_search_32bit(gens, mg, version, preset, dim):
+    """The level-unrolled and single-loop R-tree searches with 32-bit clamped box distances, and the tie
+    search, return the 64-bit stack searches' leaf, fitness and tie flag on 2^20 random targets, half of
+    them beyond the clamp (where the 64-bit search takes over)."""
+    if dim.endswith("nether") and preset != "normal":
+        pytest.skip("the Nether has no presets")
+    w = gens[version].world(dim, preset, 1)
+    bad_leaf, bad_other = mg.check_tree(w, 1 << 20, 77)
+    assert bad_leaf == 0 and bad_other == 0
+
+
 def test_chunk_mode_grid_hashes(gens, mg):
     """The six golden 26.3 "chunk" digests through mcgen_gb300_quart_grid with MCGEN_TIE_CHUNK_ORDER, and an
     unaligned grid (partial chunks on every side) against the oracle."""
