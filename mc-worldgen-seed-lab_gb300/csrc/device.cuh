@@ -762,13 +762,13 @@ __device__ __forceinline__ uint64_t dim_sq(int32_t t, int32_t lo, int32_t hi) {
 __device__ __forceinline__ uint64_t node_dist(const MgTreeNode &n, const int32_t *t) {
     const uint4 a = *reinterpret_cast<const uint4 *>(&n);                              /* lo[0..5], hi[0..1] */
     const uint4 b = *(reinterpret_cast<const uint4 *>(&n) + 1);                        /* hi[2..5], d7, links */
-    uint64_t s = b.z;
-    s += dim_sq(t[0], lo16(a.x), lo16(a.w));
-    s += dim_sq(t[1], hi16(a.x), hi16(a.w));
-    s += dim_sq(t[2], lo16(a.y), lo16(b.x));
-    s += dim_sq(t[3], hi16(a.y), hi16(b.x));
-    s += dim_sq(t[4], lo16(a.z), lo16(b.y));
-    s += dim_sq(t[5], hi16(a.z), hi16(b.y));
+    uint64_t s = b.z; /* upper bounds are stored negated */
+    s += dim_sq(t[0], lo16(a.x), -lo16(a.w));
+    s += dim_sq(t[1], hi16(a.x), -hi16(a.w));
+    s += dim_sq(t[2], lo16(a.y), -lo16(b.x));
+    s += dim_sq(t[3], hi16(a.y), -hi16(b.x));
+    s += dim_sq(t[4], lo16(a.z), -lo16(b.y));
+    s += dim_sq(t[5], hi16(a.z), -hi16(b.y));
     return s;
 }
 /* Climate.RTree.SubTree.search, iterative: descend into a child iff its box distance is below the best
@@ -829,21 +829,47 @@ __device__ __forceinline__ int tree_search_tie_stack(const MgTreeNode *__restric
 }
 /* The same searches with the traversal unrolled over the tree's levels (no stack in local memory: every
  * level's loop state stays in registers; leaves lie 3 to 5 levels below the root in every table, and
- * MG_RT_LEVELS + 1 levels below the root are unrolled) and
- * 32-bit box distances: each dimension's distance is clamped at MG_RT_CLAMP, so six squares still fit in
- * 32 bits, and the offset term saturates below the initial bound.  A distance below MG_RT_CLAMP^2 is exact,
- * and a node whose distance was clamped or saturated is at least MG_RT_CLAMP^2 away, so whenever the final
- * best distance is below MG_RT_CLAMP^2 every comparison that decided the result was exact and the result
- * is the 64-bit search's; otherwise (or for a tree deeper than the unrolled levels) the stack form runs. */
+ * MG_RT_LEVELS + 1 levels below the root are unrolled) and 32-bit box distances from packed 16-bit pairs:
+ * each dimension's distance is clamped at MG_RT_CLAMP, so six squares still fit in 32 bits, and the offset
+ * term saturates below the initial bound.  A distance below MG_RT_CLAMP^2 is exact, and a node whose
+ * distance was clamped or saturated is at least MG_RT_CLAMP^2 away, so whenever the final best distance is
+ * below MG_RT_CLAMP^2 every comparison that decided the result was exact and the result is the 64-bit
+ * search's; otherwise (or for a tree deeper than the unrolled levels, a tree whose bounds exceed the packed
+ * range, or a target outside it) the stack form runs. */
 #define MG_RT_CLAMP 26754
 #define MG_RT_LEVELS 4
-__device__ __forceinline__ uint32_t dim_sq32(int32_t t, int32_t lo, int32_t hi) {
-    const int32_t x = min(max(max(t - hi, lo - t), 0), MG_RT_CLAMP);
-    return (uint32_t)(x * x);
-}
+/* A target's coordinates as packed 16-bit pairs (t and -t): with every bound within +-12767 (the tree's
+ * MG_TREE_PACKED flag) and |t| <= 20000, t - hi and lo - t fit 16 bits, and per pair of dimensions two
+ * add-max instructions give max(lo - t, t - hi, 0) and one min the clamp. */
 struct RtTarget {
-    int32_t t[6];
+    uint32_t p[3], n[3];
 };
+__device__ __forceinline__ uint32_t pack16(int32_t lo, int32_t hi) { return (uint32_t)(lo & 0xFFFF) | ((uint32_t)hi << 16); }
+/* false when a coordinate is outside +-(32767 - MG_TREE_PACKED_BOUND) */
+__device__ __forceinline__ bool rt_target(const int32_t *t, RtTarget &q) {
+    const int32_t lim = 32767 - MG_TREE_PACKED_BOUND;
+    bool ok = true;
+    for (int k = 0; k < 6; k++) ok &= t[k] >= -lim && t[k] <= lim;
+    for (int k = 0; k < 3; k++) {
+        q.p[k] = pack16(t[2 * k], t[2 * k + 1]);
+        q.n[k] = pack16(-t[2 * k], -t[2 * k + 1]);
+    }
+    return ok;
+}
+/* clamped squared distances of one pair of dimensions: lo = (lo_a, lo_b), nhi = (-hi_a, -hi_b) */
+__device__ __forceinline__ uint32_t pair_sq(uint32_t lo, uint32_t nhi, uint32_t tp, uint32_t tn) {
+    const uint32_t th = __viaddmax_s16x2(tp, nhi, 0x80008000u);   /* t - hi */
+    uint32_t d = __viaddmax_s16x2_relu(lo, tn, th);                /* max(lo - t, t - hi, 0) */
+    d = __vimin_s16x2_relu(d, (uint32_t)MG_RT_CLAMP * 0x10001u);   /* min(., clamp) */
+    const uint32_t d0 = d & 0xFFFFu, d1 = d >> 16;
+    return d0 * d0 + d1 * d1;
+}
+/* the node's clamped squared distance, the offset term saturating below the initial bound */
+__device__ __forceinline__ uint32_t rt_dist(const uint4 &a, const uint4 &b, const RtTarget &q) {
+    const uint32_t d = pair_sq(a.x, a.w, q.p[0], q.n[0]) + pair_sq(a.y, b.x, q.p[1], q.n[1]) +
+                       pair_sq(a.z, b.y, q.p[2], q.n[2]);
+    return d > 0xFFFFFFFEu - b.z ? 0xFFFFFFFEu : d + b.z;
+}
 struct RtState {
     uint32_t best;
     int res, cnt;
@@ -854,10 +880,7 @@ __device__ __forceinline__ bool rt_walk(const MgTreeNode *__restrict__ T, int fi
     for (int ci = first; ci < first + count; ci++) {
         const uint4 a = *reinterpret_cast<const uint4 *>(T + ci);      /* lo[0..5], hi[0..1] */
         const uint4 b = *(reinterpret_cast<const uint4 *>(T + ci) + 1); /* hi[2..5], d7, first | count | biome */
-        uint32_t d = dim_sq32(q.t[0], lo16(a.x), lo16(a.w)) + dim_sq32(q.t[1], hi16(a.x), hi16(a.w)) +
-                     dim_sq32(q.t[2], lo16(a.y), lo16(b.x)) + dim_sq32(q.t[3], hi16(a.y), hi16(b.x)) +
-                     dim_sq32(q.t[4], lo16(a.z), lo16(b.y)) + dim_sq32(q.t[5], hi16(a.z), hi16(b.y));
-        d = d > 0xFFFFFFFEu - b.z ? 0xFFFFFFFEu : d + b.z;
+        const uint32_t d = rt_dist(a, b, q);
         if (TIE ? d > s.best : d >= s.best) continue;
         const int cc = (int)((b.w >> 16) & 0xFFu);
         if (cc == 0) {
@@ -888,10 +911,7 @@ static __device__ __noinline__ RtState rt_find_flat(const MgTreeNode *__restrict
         nxt[sp] = ci + 1;
         const uint4 a = *reinterpret_cast<const uint4 *>(T + ci);
         const uint4 b = *(reinterpret_cast<const uint4 *>(T + ci) + 1);
-        uint32_t d = dim_sq32(q.t[0], lo16(a.x), lo16(a.w)) + dim_sq32(q.t[1], hi16(a.x), hi16(a.w)) +
-                     dim_sq32(q.t[2], lo16(a.y), lo16(b.x)) + dim_sq32(q.t[3], hi16(a.y), hi16(b.x)) +
-                     dim_sq32(q.t[4], lo16(a.z), lo16(b.y)) + dim_sq32(q.t[5], hi16(a.z), hi16(b.y));
-        d = d > 0xFFFFFFFEu - b.z ? 0xFFFFFFFEu : d + b.z;
+        const uint32_t d = rt_dist(a, b, q);
         if (TIE ? d > s.best : d >= s.best) continue;
         const int cc = (int)((b.w >> 16) & 0xFFu);
         if (cc == 0) {
@@ -917,10 +937,13 @@ static __device__ __noinline__ RtState rt_find(const MgTreeNode *__restrict__ T,
 }
 /* tree_search / tree_search_tie for warps whose cells are neighbours (grids, batches: similar targets, so
  * similar paths), tree_search_scattered for unrelated targets (many seeds, point lists, the seed search) */
+__device__ __forceinline__ bool rt_packed(const MgTreeNode *__restrict__ T) {
+    return (reinterpret_cast<const uint4 *>(T)[1].w >> 24) == MG_TREE_PACKED;
+}
 template <bool FLAT>
 __device__ __forceinline__ int tree_search_t(const MgTreeNode *__restrict__ T, const int32_t *t, int cand, uint64_t &best) {
-    if (cand < 0) {
-        const RtTarget q{{t[0], t[1], t[2], t[3], t[4], t[5]}};
+    RtTarget q;
+    if (cand < 0 && rt_packed(T) && rt_target(t, q)) {
         const RtState s = FLAT ? rt_find_flat<false>(T, q) : rt_find<false>(T, q);
         if (s.res >= 0 && s.best < (uint32_t)MG_RT_CLAMP * MG_RT_CLAMP) {
             best = s.best;
@@ -938,11 +961,14 @@ __device__ __forceinline__ int tree_search_scattered(const MgTreeNode *__restric
 }
 __device__ __forceinline__ int tree_search_tie(const MgTreeNode *__restrict__ T, const int32_t *t, uint64_t &best,
                                                bool &tied) {
-    const RtState s = rt_find<true>(T, RtTarget{{t[0], t[1], t[2], t[3], t[4], t[5]}});
-    if (s.res >= 0 && s.best < (uint32_t)MG_RT_CLAMP * MG_RT_CLAMP) {
-        best = s.best;
-        tied = s.cnt >= 2;
-        return s.res;
+    RtTarget q;
+    if (rt_packed(T) && rt_target(t, q)) {
+        const RtState s = rt_find<true>(T, q);
+        if (s.res >= 0 && s.best < (uint32_t)MG_RT_CLAMP * MG_RT_CLAMP) {
+            best = s.best;
+            tied = s.cnt >= 2;
+            return s.res;
+        }
     }
     return tree_search_tie_stack(T, t, best, tied);
 }

@@ -56,16 +56,21 @@ typedef struct __attribute__((aligned(16))) {
 
 /* R-tree node on the device (32 bytes, two 16-byte loads): children of a subtree are contiguous
  * [first, first+count); a leaf has count == 0.  Bounds of the six climate dimensions are quantised values
- * (|v| <= 12000 in every table); the seventh dimension ("offset") always meets a target coordinate of 0, so
- * its squared distance max(-hi, lo, 0)^2 is stored instead of its bounds. */
+ * (|v| <= 12000 in every table), the upper bounds stored negated (nhi = -hi: packed 16-bit add-max
+ * instructions then form t - hi); the seventh dimension ("offset") always meets a target coordinate of 0,
+ * so its squared distance max(-hi, lo, 0)^2 is stored instead of its bounds.  The root is never a leaf;
+ * its biome byte holds MG_TREE_PACKED when every bound lies within +-MG_TREE_PACKED_BOUND (the packed
+ * 16-bit distances are then exact for targets within +-(32767 - MG_TREE_PACKED_BOUND)). */
 typedef struct __attribute__((aligned(16))) {
     int16_t lo[6];
-    int16_t hi[6];
+    int16_t nhi[6];
     uint32_t d7;
     uint16_t first;
     uint8_t count;
     uint8_t biome;
 } MgTreeNode;
+#define MG_TREE_PACKED 1
+#define MG_TREE_PACKED_BOUND 12767
 
 /* Seed-independent world description, copied once to the device. */
 typedef struct {

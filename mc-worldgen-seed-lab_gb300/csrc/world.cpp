@@ -492,6 +492,7 @@ static int load_tree(const char *root, int version, int dim, std::vector<MgTreeN
     std::vector<int> src;
     src.push_back(root_id);
     out->push_back(MgTreeNode());
+    bool packed = true; /* every bound within +-MG_TREE_PACKED_BOUND (the root's flag) */
     for (size_t h = 0; h < src.size(); h++) {
         const BNode &b = tb.nodes[(size_t)src[h]];
         MgTreeNode &o = (*out)[h];
@@ -499,13 +500,16 @@ static int load_tree(const char *root, int version, int dim, std::vector<MgTreeN
         for (int d = 0; d < MG_TREE_DIMS; d++) {
             int64_t lo = b.lo[d], hi = b.hi[d];
             if (version >= MG_V26_4) hi -= 1; /* exclusive upper bound (engine/mc_data.h:178-180) */
-            if (lo < -32768 || lo > 32767 || hi < -32768 || hi > 32767) {
+            if (lo < -32768 || lo > 32767 || hi < -32767 || hi > 32767) {
                 *err = "biome parameter outside the 16-bit node range";
                 return MCGEN_E_DATA;
             }
             if (d < 6) {
                 o.lo[d] = (int16_t)lo;
-                o.hi[d] = (int16_t)hi;
+                o.nhi[d] = (int16_t)(-hi);
+                if (lo < -MG_TREE_PACKED_BOUND || lo > MG_TREE_PACKED_BOUND || hi < -MG_TREE_PACKED_BOUND ||
+                    hi > MG_TREE_PACKED_BOUND)
+                    packed = false;
             } else {
                 int64_t x = std::max(std::max(-hi, lo), (int64_t)0);
                 o.d7 = (uint32_t)(x * x);
@@ -521,6 +525,7 @@ static int load_tree(const char *root, int version, int dim, std::vector<MgTreeN
             for (int k : b.kids) { src.push_back(k); out->push_back(MgTreeNode()); }
         }
     }
+    if (!out->empty() && (*out)[0].count > 0 && packed) (*out)[0].biome = MG_TREE_PACKED;
     return MCGEN_OK;
 }
 
