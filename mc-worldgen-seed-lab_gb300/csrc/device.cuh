@@ -123,10 +123,12 @@ __device__ __forceinline__ int64_t mulq(int64_t a, int64_t b) {
     const uint64_t hi = (uint64_t)__mul64hi(a, b), lo = (uint64_t)a * (uint64_t)b;
     return (int64_t)((hi << (64 - MG_Q)) | (lo >> MG_Q));
 }
-/* smoothstep t^3 (t (6 t - 15) + 10) of 0 <= t < 1 */
+/* smoothstep t^3 (6 t^2 - 15 t + 10) of 0 <= t < 1: three products (t^2, t^3, t^3 p); 6 t^2 and 15 t are
+ * shifts and adds */
 __device__ __forceinline__ int64_t fadeq(int64_t t) {
-    const int64_t p = mulq(6 * t - (15LL << MG_Q), t) + (10LL << MG_Q);
-    return mulq(mulq(mulq(t, t), t), p);
+    const int64_t t2 = mulq(t, t);
+    const int64_t p = (t2 << 2) + (t2 << 1) - ((t << 4) - t) + (10LL << MG_Q);
+    return mulq(mulq(t2, t), p);
 }
 
 /* ------------------------------------------------------------------ lattice header */
