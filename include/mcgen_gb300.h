@@ -77,7 +77,7 @@ MCGEN_API int mcgen_gb300_plan_new(const McGb300Request *reqs, int n, int tie_ru
 MCGEN_API void mcgen_gb300_plan_free(McGb300Plan *p);
 MCGEN_API long long mcgen_gb300_plan_output_bytes(const McGb300Plan *p);
 MCGEN_API long long mcgen_gb300_plan_output_offset(const McGb300Plan *p, int i);
-/* the tile shape in use (cells x rows, resident CTAs per SM): 0 (32 x 4, 8), 1 (8 x 16, 7), 2 (8 x 16, 6),
+/* the tile shape in use (cells x rows, resident CTAs per SM): 0 (8 x 16, 9), 1 (8 x 16, 7), 2 (8 x 16, 6),
  * 3 (8 x 16, 8) */
 MCGEN_API int mcgen_gb300_plan_shape(const McGb300Plan *p);
 MCGEN_API int mcgen_gb300_plan_set_shape(McGb300Plan *p, int shape);

@@ -1,8 +1,8 @@
 /* batch.cu -- many biome-map requests of uneven size in one persistent launch.
  *
  * A request is (world: version + dimension + preset, seed, quart region qx0..qx0+nx-1 x qz0..qz0+nz-1 at
- * quart y, tie rule).  The host splits every request into tiles -- 128 quart cells (32 x 4, 16 x 8, 64 x 2
- * or 8 x 16: the autotuner picks the shape) for Overworld and Nether, 8 x 8 chunks (32 x 32 quart cells)
+ * quart y, tie rule).  The host splits every request into tiles -- 128 quart cells (8 x 16; the autotuner
+ * picks the register budget) for Overworld and Nether, 8 x 8 chunks (32 x 32 quart cells)
  * for the End -- and numbers them.  k_batch runs one CTA per
  * SM slot for the whole batch; each CTA takes the next tile from a device counter (the work queue), finds
  * its request by binary search over the requests' first-tile numbers, stages that request's seed lattices
@@ -179,7 +179,7 @@ __device__ __forceinline__ void batch_end(const MgWorldDesc &W, BatchSmem &sm, c
 }
 
 /* TILE_W: tile width in cells (tiles are 128 cells); MINB: resident CTAs per SM the register allocation
- * is sized for (6: 80 registers, 7: 72, 8: 64) */
+ * is sized for (6: 80 registers, 7: 72, 8: 64, 9: 56) */
 template <int TILE_W, int MINB>
 __global__ void __launch_bounds__(BNT, MINB) k_batch(const MgWorldDesc *__restrict__ worlds, const MgTreeNode *const *__restrict__ trees,
                                                const MgBatchReq *__restrict__ reqs, int nreq, long long ntiles,
@@ -250,9 +250,9 @@ __global__ void __launch_bounds__(BNT, MINB) k_batch(const MgWorldDesc *__restri
 }
 
 /* ---------------------------------------------------------------- host side */
-/* tile shapes the autotuner chooses from: tile width, and the register budget (resident CTAs per SM: 8, 7,
+/* tile shapes the autotuner chooses from: tile width, and the register budget (resident CTAs per SM: 9, 7,
  * 6, 8) in k_batch's second template argument */
-const int kBatchTileWidths[BATCH_SHAPES] = {32, 8, 8, 8};
+const int kBatchTileWidths[BATCH_SHAPES] = {8, 8, 8, 8};
 static int g_resident[BATCH_SHAPES] = {0, 0, 0, 0}; /* CTAs per SM x SMs, per shape (batch_prepare) */
 
 long long batch_tiles(int dim, int qx0, int qz0, int nx, int nz, int shape) {
@@ -299,7 +299,7 @@ int batch_prepare(int *ctas_per_sm) {
         if (ctas_per_sm) *ctas_per_sm = g_resident[0] / (sms > 0 ? sms : 1);
         return 0;
     }
-    int rc = prepare_t<32, 8>(0, sms);
+    int rc = prepare_t<8, 9>(0, sms);
     if (!rc) rc = prepare_t<8, 7>(1, sms);
     if (!rc) rc = prepare_t<8, 6>(2, sms);
     if (!rc) rc = prepare_t<8, 8>(3, sms);
@@ -325,7 +325,7 @@ int launch_batch(const MgWorldDesc *d_worlds, const MgTreeNode *const *d_trees, 
     case 1: k_batch<8, 7><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
     case 2: k_batch<8, 6><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
     case 3: k_batch<8, 8><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
-    default: k_batch<32, 8><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
+    default: k_batch<8, 9><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
     }
     count_launch_external();
     return (int)cudaGetLastError();
