@@ -199,16 +199,20 @@ static int64_t q59_product(double a, double b, double c) {
  *    E + 210u.  The three lerp levels (E = 0, then 210u, 420u) give 630u; 640u is used.
  * Each level's term (amp * o) * vf adds 2 roundings, each running sum of a stack one per level, the stack sum,
  * the value factor product and the conversion of the fixed-point sum one each, on magnitudes below
- * 2.1 * sum|c|.  The fixed-point evaluation itself is within 1e-16 per level.  The bound is taken 25 %
- * larger, and cast_settled's two roundings of a +- err are added.  Negative: not screened (sum too large for
- * the fixed point's range). */
+ * 2.1 * sum|c|.  The fixed-point evaluation itself (unit q = 2^-59, every product truncated by at most one
+ * unit): a smoothstep is within 27 q (t^2, t^3 and the final product; the factor 6t^2 - 15t + 10 <= 10
+ * carries six times t^2's error), a lerp adds 4 x its weight's error plus one unit to the larger of its
+ * inputs' errors, so an octave is within 3 x (4 x 27 + 1) = 327 q and a level's product with its constant
+ * within (654 |c| + 6) q.  The bound is taken 25 % larger, and cast_settled's two roundings of a +- err are
+ * added.  Negative: not screened (sum too large for the fixed point's range). */
 static double screen_bound(const MgNoise *s) {
     const double u = 0x1.0p-53;
     double c = 0.0;
     for (int k = 0; k < s->nlev; k++) c += fabs(s->amp_d[k] * s->vf_d[k] * s->vfac);
     const double vmax = 2.1 * 2.0 * c;
     if (vmax * 1.01 >= 15.0) return -1.0;
-    const double e = 2.0 * c * (640.0 * u + 4.2 * u) + (2.0 * s->nlev + 6.0) * u * vmax + 2.0 * s->nlev * 1e-16;
+    const double e = 2.0 * c * (640.0 * u + 4.2 * u) + (2.0 * s->nlev + 6.0) * u * vmax +
+                     (654.0 * c + 6.0 * s->nlev) * 0x1.0p-59;
     return 1.25 * e + 4.0 * u * vmax;
 }
 /* PerlinNoise/NormalNoise constants of 26.1/26.2 (engine/mc_noise.h:178-196) */
