@@ -181,6 +181,18 @@ __device__ __forceinline__ T gdot(int h, T x, T y, T z) {
     T v = h < 4 ? y : ((h == 12 || h == 14) ? x : z);
     return ((h & 1) ? -u : u) + ((h & 2) ? -v : v);
 }
+/* The float branch (bound by the integer ALU pipe) takes the vector from a 256-byte table through L1 and
+ * forms the dot on the FMA pipe: gy*y is exact, fma(gx, x, .) and fma(gz, z, .) each round at most once
+ * and, with exactly two non-zero components, exactly one of them rounds -- the reference's one rounded
+ * sum of two exact products (up to the sign of an exactly-zero result, as above). */
+__device__ const float4 kGradF[16] = {{1, 1, 0, 0},  {-1, 1, 0, 0}, {1, -1, 0, 0}, {-1, -1, 0, 0}, {1, 0, 1, 0},  {-1, 0, 1, 0},
+                                      {1, 0, -1, 0}, {-1, 0, -1, 0}, {0, 1, 1, 0},  {0, -1, 1, 0},  {0, 1, -1, 0}, {0, -1, -1, 0},
+                                      {1, 1, 0, 0},  {0, -1, 1, 0},  {-1, 1, 0, 0}, {0, -1, -1, 0}};
+template <>
+__device__ __forceinline__ float gdot<float>(int h, float x, float y, float z) {
+    const float4 g = __ldg(&kGradF[h & 15]);
+    return __fmaf_rn(g.z, z, __fmaf_rn(g.x, x, g.y * y));
+}
 template <typename T>
 __device__ __forceinline__ T fade(T t) {
     return t * t * t * (t * (t * (T)6 - (T)15) + (T)10);
@@ -264,11 +276,14 @@ __device__ __forceinline__ T octave_z0(const P &p, const H &h, int ix, T fx, int
  * lerp products and sums stay on the FP64 pipe (36 instead of 50 FP64 operations per octave sample).
  * Integer and FP64 results differ at most in the sign of an exactly-zero corner value, which no later
  * step observes (as for gdot). */
+__device__ const int4 kGradI[16] = {{1, 1, 0, 0},  {-1, 1, 0, 0}, {1, -1, 0, 0}, {-1, -1, 0, 0}, {1, 0, 1, 0},  {-1, 0, 1, 0},
+                                    {1, 0, -1, 0}, {-1, 0, -1, 0}, {0, 1, 1, 0},  {0, -1, 1, 0},  {0, 1, -1, 0}, {0, -1, -1, 0},
+                                    {1, 1, 0, 0},  {0, -1, 1, 0},  {-1, 1, 0, 0}, {0, -1, -1, 0}};
+/* the vector from the table, the dot as 64-bit products with the small components (the integer
+ * multiply-add pipe) instead of 64-bit selects and negations on the ALU pipe; exact either way */
 __device__ __forceinline__ int64_t gdot_i(int h, int64_t x, int64_t y, int64_t z) {
-    h &= 15;
-    const int64_t u = h < 8 ? x : y;
-    const int64_t v = h < 4 ? y : ((h == 12 || h == 14) ? x : z);
-    return ((h & 1) ? -u : u) + ((h & 2) ? -v : v);
+    const int4 g = __ldg(&kGradI[h & 15]);
+    return x * (int64_t)g.x + y * (int64_t)g.y + z * (int64_t)g.z;
 }
 /* D * 2^-52 rounded to the nearest double, ties to even (|D| < 2^54; exact below 2^53) */
 __device__ __forceinline__ double fix_to_d(int64_t D) {
