@@ -119,16 +119,18 @@ __device__ __forceinline__ int64_t lfloor(double v) { return __double2ll_rd(v); 
  * differs from the exact value by far more (the bound used by the screen, MgNoise::fix_err), so the
  * approximation decides the reference's float result except near a float rounding boundary. */
 #define MG_Q 59
-__device__ __forceinline__ int64_t mulq(int64_t a, int64_t b) {
-    const uint64_t hi = (uint64_t)__mul64hi(a, b), lo = (uint64_t)a * (uint64_t)b;
+/* a * b * 2^-59 rounded toward minus infinity, for non-negative operands (the unsigned high product: a
+ * signed one costs two sign corrections more) */
+__device__ __forceinline__ int64_t mulq_u(int64_t a, int64_t b) {
+    const uint64_t hi = __umul64hi((uint64_t)a, (uint64_t)b), lo = (uint64_t)a * (uint64_t)b;
     return (int64_t)((hi << (64 - MG_Q)) | (lo >> MG_Q));
 }
-/* smoothstep t^3 (6 t^2 - 15 t + 10) of 0 <= t < 1: three products (t^2, t^3, t^3 p); 6 t^2 and 15 t are
- * shifts and adds */
+/* smoothstep t^3 (6 t^2 - 15 t + 10) of 0 <= t < 1: three products of non-negative values (t^2, t^3, and
+ * t^3 p with p in [1, 10]); 6 t^2 and 15 t are shifts and adds */
 __device__ __forceinline__ int64_t fadeq(int64_t t) {
-    const int64_t t2 = mulq(t, t);
+    const int64_t t2 = mulq_u(t, t);
     const int64_t p = (t2 << 2) + (t2 << 1) - ((t << 4) - t) + (10LL << MG_Q);
-    return mulq(mulq(t2, t), p);
+    return mulq_u(mulq_u(t2, t), p);
 }
 
 /* ------------------------------------------------------------------ lattice header */
@@ -355,8 +357,15 @@ __device__ __forceinline__ T octave(const uint8_t *__restrict__ p, int ix, T fx,
     return octave_p<T>(PlainPerm{p}, ix, fx, iy, fy, iz, fz);
 }
 
-/* the octave in the 59-bit fixed point of mulq / fadeq */
-__device__ __forceinline__ int64_t lerpq(int64_t t, int64_t a, int64_t b) { return a + mulq(t, b - a); }
+/* mulq_u for a non-negative weight t and a signed value s: the unsigned high product of t and s's two's
+ * complement bits is the signed one plus t when s < 0 (one correction instead of a signed product's two) */
+__device__ __forceinline__ int64_t mulq_us(int64_t t, int64_t s) {
+    const uint64_t hi = __umul64hi((uint64_t)t, (uint64_t)s) - (s < 0 ? (uint64_t)t : 0ULL);
+    const uint64_t lo = (uint64_t)t * (uint64_t)s;
+    return (int64_t)((hi << (64 - MG_Q)) | (lo >> MG_Q));
+}
+/* the octave in the 59-bit fixed point of mulq_u / fadeq (the weights t are smoothsteps in [0, 1]) */
+__device__ __forceinline__ int64_t lerpq(int64_t t, int64_t a, int64_t b) { return a + mulq_us(t, b - a); }
 /* fractions X, Y, Z and smoothsteps V, W (of Y, Z) in the fixed point */
 template <typename P>
 __device__ __forceinline__ int64_t octave_qfix(const P &p, int ix, int64_t X, int iy, int64_t Y, int64_t V, int iz,
@@ -679,7 +688,8 @@ static __device__ __noinline__ int64_t nn_q(const MgNoise &N, const MgLattice *_
         lev += Z0 ? octave_qfix(PlainPerm{L->p}, ia, XA, ib, XB, fadeq(XB), L->iz, X0, L->z0.q.uz)
                   : octave_qfix(PlainPerm{L->p}, ia, XA, L->iy, X0, L->z0.q.uy, ib, XB, fadeq(XB));
         if (st) {
-            acc += mulq(N.cq[k], lev);
+            const int64_t c = N.cq[k], m = mulq_us(c < 0 ? -c : c, lev);
+            acc += c < 0 ? -m : m;
             lev = 0;
         }
     }
