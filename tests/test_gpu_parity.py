@@ -239,8 +239,8 @@ def test_climate_screen(gens, mg, version, preset):
         assert fallback < (1 << 21) // 10
 
 
-@pytest.mark.parametrize("version", ["26.1", "26.3"])
-@pytest.mark.parametrize("preset", ["normal", "large_biomes"])
+@pytest.mark.parametrize("version", ["26.1", "26.3", "26.4-snapshot-2"])
+@pytest.mark.parametrize("preset", ["normal", "large_biomes", "amplified"])
 @pytest.mark.parametrize("dim", ["minecraft:overworld", "minecraft:the_nether"])
 def test_tree_search_32bit(gens, mg, version, preset, dim):
     """The level-unrolled and single-loop R-tree searches with 32-bit clamped box distances, and the tie
