@@ -2,12 +2,12 @@
  *
  * A request is (world: version + dimension + preset, seed, quart region qx0..qx0+nx-1 x qz0..qz0+nz-1 at
  * quart y, tie rule).  The host splits every request into tiles -- 128 quart cells (8 x 16; the autotuner
- * picks the register budget) for Overworld and Nether, 8 x 8 chunks (32 x 32 quart cells)
- * for the End -- and numbers them.  k_batch runs one CTA per
- * SM slot for the whole batch; each CTA takes the next tile from a device counter (the work queue), finds
- * its request by binary search over the requests' first-tile numbers, stages that request's seed lattices
- * and its world's offset spline in shared memory when they differ from the previous tile's, and computes
- * the tile.  Uneven requests therefore cost no idle SMs and no per-request launches.
+ * picks the register budget) for Overworld and Nether, 8 x 8 chunks (32 x 32 quart cells) for the End --
+ * and numbers them.  k_batch runs one CTA per SM slot for the whole batch; each CTA takes the next tile
+ * from a device counter (the work queue), finds its request among the requests' first-tile numbers, stages
+ * that request's seed lattices in shared memory when they differ from the previous tile's, and computes the
+ * tile (for a double-branch Overworld tile, first the shift noises' per-column and per-row splits).  Uneven
+ * requests therefore cost no idle SMs and no per-request launches.
  *
  * The seed lattices of every (world, seed) of the batch are built beforehand by k_setup_list_* into a
  * state pool (the served form keeps that pool across batches as a device cache).
@@ -129,26 +129,33 @@ __global__ void __launch_bounds__(LNT) k_setup_list_end(const MgSetupEntry *__re
 }
 
 /* ---------------------------------------------------------------- the persistent batch kernel */
-/* The lattices of an Overworld/Nether request and the End's scratch are never live in the same tile, so
- * they share storage: 24.6 KB per CTA, which leaves the register budget as the occupancy limit. */
+/* The lattices of an Overworld/Nether request (with a double-branch Overworld tile's shift table) and the
+ * End's scratch are never live in the same tile, so they share storage: 21 KB per CTA, which leaves the
+ * register budget as the occupancy limit (up to 9 CTAs per SM). */
 struct BatchEnd {
     uint8_t endp[256];
     EndTile tile;
 };
+/* the lattices of an Overworld/Nether request, and the shift table of a double-branch Overworld tile */
+struct BatchLat {
+    MgLattice lat[MG_MAX_TABLES];
+    ShiftTable<8, BNT / 8> shift;
+};
 struct BatchSmem {
-    MgSpline spline;
     union {
-        MgLattice lat[MG_MAX_TABLES];
+        BatchLat o;
         BatchEnd end;
     };
-    int tile, req, state, world;
+    int tile, req, state;
 };
 
+/* tab: the tile's shift table (double-branch Overworld, ENGINE rule) or null */
 template <bool FM, int DIM, int TILE_W>
 __device__ __forceinline__ void batch_cells(const MgWorldDesc &W, const MgSpline &S, const MgLattice *T,
                                             const MgTreeNode *tree, const MgBatchReq &R, int tx0, int tz0,
-                                            uint8_t *out) {
-    const int ix = tx0 + (threadIdx.x % TILE_W), iz = tz0 + (threadIdx.x / TILE_W);
+                                            const ShiftTable<8, BNT / 8> *tab, uint8_t *out) {
+    const int col = threadIdx.x % TILE_W, row = threadIdx.x / TILE_W;
+    const int ix = tx0 + col, iz = tz0 + row;
     if (ix >= R.nx || iz >= R.nz) return;
     const int qx = R.qx0 + ix, qz = R.qz0 + iz;
     uint8_t b;
@@ -156,7 +163,8 @@ __device__ __forceinline__ void batch_cells(const MgWorldDesc &W, const MgSpline
         b = (uint8_t)cell_chunk<FM, DIM>(W, S, T, tree, qx, R.qy, qz);
     } else {
         int32_t tg[6];
-        cell_target<FM, DIM>(W, S, T, qx, R.qy, qz, tg);
+        if (!FM && DIM == MG_OVERWORLD && TILE_W == 8 && tab) climate_ow_d_tab(W, S, T, *tab, col, row, qx, R.qy, qz, tg);
+        else cell_target<FM, DIM>(W, S, T, qx, R.qy, qz, tg);
         uint64_t d;
         b = tree[tree_search(tree, tg, -1, d)].biome;
     }
@@ -204,7 +212,7 @@ __global__ void __launch_bounds__(BNT, MINB) k_batch(const MgWorldDesc *__restri
                                                uint8_t *__restrict__ out) {
     extern __shared__ uint4 smem_raw[];
     BatchSmem &sm = *reinterpret_cast<BatchSmem *>(smem_raw);
-    if (threadIdx.x == 0) { sm.state = -1; sm.world = -1; }
+    if (threadIdx.x == 0) sm.state = -1;
     for (;;) {
         __syncthreads();
         if (threadIdx.x < 32) { /* warp 0 takes the next tile and finds its request */
@@ -222,24 +230,20 @@ __global__ void __launch_bounds__(BNT, MINB) k_batch(const MgWorldDesc *__restri
         if (r < 0) return;
         const MgBatchReq R = reqs[r];
         const MgWorldDesc &W = worlds[R.world];
-        /* stage the world's spline and the request's lattices when they change */
-        const bool new_world = R.world != sm.world, new_state = R.state != sm.state;
-        if (new_world && W.dim == MG_OVERWORLD) {
-            const uint4 *c = reinterpret_cast<const uint4 *>(&W.spline);
-            uint4 *d = reinterpret_cast<uint4 *>(&sm.spline);
-            for (int i = threadIdx.x; i < (int)(sizeof(MgSpline) / 16); i += BNT) d[i] = c[i];
-        }
+        /* stage the request's lattices when they change (the world's offset spline, about 11 nodes read per
+         * sample, is read in place through L1: kept out of shared memory, it leaves room for 9 CTAs per SM) */
+        const bool new_state = R.state != sm.state;
         if (new_state) {
             if (W.dim == MG_END) {
                 for (int i = threadIdx.x; i < 256; i += BNT) sm.end.endp[i] = pool[R.state].p[i];
             } else {
                 const uint4 *a = reinterpret_cast<const uint4 *>(pool + R.state);
-                uint4 *b = reinterpret_cast<uint4 *>(sm.lat);
+                uint4 *b = reinterpret_cast<uint4 *>(sm.o.lat);
                 for (int i = threadIdx.x; i < W.ntables * (int)(sizeof(MgLattice) / 16); i += BNT) b[i] = a[i];
             }
         }
         __syncthreads();
-        if (threadIdx.x == 0) { sm.world = R.world; sm.state = R.state; }
+        if (threadIdx.x == 0) sm.state = R.state;
         const int tile = sm.tile;
         if (W.dim == MG_END) {
             const int ncx = ((R.qx0 + R.nx - 1) >> 2) - (R.qx0 >> 2) + 1;
@@ -253,11 +257,18 @@ __global__ void __launch_bounds__(BNT, MINB) k_batch(const MgWorldDesc *__restri
         const int tx0 = (tile % tw) * TILE_W, tz0 = (tile / tw) * TILE_H;
         const MgTreeNode *tree = trees[R.world];
         if (W.fmode) {
-            if (W.dim == MG_OVERWORLD) batch_cells<true, MG_OVERWORLD, TILE_W>(W, sm.spline, sm.lat, tree, R, tx0, tz0, out);
-            else batch_cells<true, MG_NETHER, TILE_W>(W, sm.spline, sm.lat, tree, R, tx0, tz0, out);
+            if (W.dim == MG_OVERWORLD) batch_cells<true, MG_OVERWORLD, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, out);
+            else batch_cells<true, MG_NETHER, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, out);
+        } else if (W.dim == MG_OVERWORLD) {
+            /* the tile's shift splits, computed once per column and row (ENGINE rule) */
+            const bool tab = TILE_W == 8 && R.tie != MG_TIE_CHUNK_CELL && shift_table_ok(W);
+            if (tab) {
+                shift_table_fill<8, BNT / 8, BNT>(W.noise[0], sm.o.lat, R.qx0 + tx0, R.qz0 + tz0, sm.o.shift);
+                __syncthreads();
+            }
+            batch_cells<false, MG_OVERWORLD, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, tab ? &sm.o.shift : nullptr, out);
         } else {
-            if (W.dim == MG_OVERWORLD) batch_cells<false, MG_OVERWORLD, TILE_W>(W, sm.spline, sm.lat, tree, R, tx0, tz0, out);
-            else batch_cells<false, MG_NETHER, TILE_W>(W, sm.spline, sm.lat, tree, R, tx0, tz0, out);
+            batch_cells<false, MG_NETHER, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, out);
         }
     }
 }

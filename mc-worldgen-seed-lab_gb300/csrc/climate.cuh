@@ -88,16 +88,11 @@ __device__ __forceinline__ void ridge_float(const MgWorldDesc &W, const MgLattic
     rff = (float)ridges_folded_d(W, rv);
 }
 
-/* double branch of the Overworld climate, out of line (the kernels reach the climate from two sites each:
- * the cell itself and the tie chain).  The shift noises stay exact in double: their value moves the climate
- * noises' input coordinates, and the kernels' integer pipes (which carry the screened climate noises) are
- * busier than the FP64 pipe, so a fixed-point shift measured slower. */
-static __device__ __noinline__ void climate_ow_d(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
-                                                 double X, double Z, double Xc, double Zc, int by, int32_t *tg) {
-    double sx = nn_d_y0(W.noise[0], T, X, Z, Xc, Zc) * 4.0;
-    double sz = nn_d_z0(W.noise[0], T, Z, X, Zc, Xc) * 4.0;
-    double x = X + sx, z = Z + sz;
-    double xc = x * MG_SECOND_STACK, zc = z * MG_SECOND_STACK;
+/* double branch of the Overworld climate after the shift: the climate noises screened at the exact shifted
+ * coordinates, the finish (out of line: reached from the per-cell and the per-tile shift forms) */
+static __device__ __noinline__ void climate_ow_d_rest(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
+                                                      double x, double z, int by, int32_t *tg) {
+    const double xc = x * MG_SECOND_STACK, zc = z * MG_SECOND_STACK;
     const float tf = nn_d_y0_float(W.noise[1], T, x, z, xc, zc);
     const float hf = nn_d_y0_float(W.noise[2], T, x, z, xc, zc);
     const float cf = nn_d_y0_float(W.noise[3], T, x, z, xc, zc);
@@ -105,6 +100,104 @@ static __device__ __noinline__ void climate_ow_d(const MgWorldDesc &W, const MgS
     float rvf, rff;
     ridge_float(W, T, x, z, xc, zc, rvf, rff);
     climate_finish_df(W, S, tf, hf, cf, ef, rvf, rff, by, tg);
+}
+/* double branch of the Overworld climate, out of line (the kernels reach the climate from two sites each:
+ * the cell itself and the tie chain).  The shift noises stay exact in double: their value moves the climate
+ * noises' input coordinates, and the kernels' integer pipes (which carry the screened climate noises) are
+ * busier than the FP64 pipe, so a fixed-point shift measured slower. */
+static __device__ __noinline__ void climate_ow_d(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
+                                                 double X, double Z, double Xc, double Zc, int by, int32_t *tg) {
+    const double sx = nn_d_y0(W.noise[0], T, X, Z, Xc, Zc) * 4.0;
+    const double sz = nn_d_z0(W.noise[0], T, Z, X, Zc, Xc) * 4.0;
+    climate_ow_d_rest(W, S, T, X + sx, Z + sz, by, tg);
+}
+
+/* Shift noises of a tile, double branch.  Every input of ShiftA (x, 0, z) and ShiftB (z, x, 0) depends on
+ * one coordinate: X f + o or Z f + o (first stack), X c f + o or Z c f + o (second stack).  So the cells of a
+ * tile column share their X-side splits and smoothsteps, the cells of a row their Z-side ones, and the CTA
+ * computes them once per tile into a table (entry (lattice, family, column or row); families: X with the
+ * lattice's x offset (ShiftA's x input), X with its y offset (ShiftB's y input), Z with its z offset
+ * (ShiftA's z input), Z with its x offset (ShiftB's x input)).  Each cell then runs only the octaves'
+ * gradient sums and lerps: the splits and smoothsteps are the per-cell functions' values on the same
+ * inputs, so the result is the same to the bit. */
+#define SHIFT_MAXLEV 3                        /* levels of the shift noise the table serves (26.x: 3) */
+struct ShiftSplit {
+    int64_t pk;                               /* fraction in units of 2^-52 | (cell & 255) << 52; -1: not a multiple */
+    double u;                                 /* smoothstep of the fraction */
+};
+template <int TW, int TH>
+struct ShiftTable {
+    ShiftSplit e[2 * SHIFT_MAXLEV][2 * TW + 2 * TH]; /* per lattice: X+ox, X+oy (TW each), Z+oz, Z+ox (TH each) */
+};
+/* true when the world's shift noise fits the table */
+__device__ __forceinline__ bool shift_table_ok(const MgWorldDesc &W) { return W.noise[0].nlev <= SHIFT_MAXLEV; }
+/* the table of the tile whose first cell is (qx0, qz0); all threads of the block take part */
+template <int TW, int TH, int NT>
+__device__ __forceinline__ void shift_table_fill(const MgNoise &N, const MgLattice *__restrict__ T, int qx0, int qz0,
+                                                 ShiftTable<TW, TH> &tab) {
+    const int per = 2 * TW + 2 * TH, nl = 2 * N.nlev;
+    const MgLattice *A = T + N.base;
+    for (int e = threadIdx.x; e < nl * per; e += NT) {
+        const int j = e / per, r = e % per; /* r: the entry's place in the lattice's row of the table */
+        const int fam = r < 2 * TW ? r / TW : 2 + (r - 2 * TW) / TH;
+        const int idx = r < 2 * TW ? r % TW : (r - 2 * TW) % TH;
+        const int st = j >= N.nlev, k = j - st * N.nlev;
+        const MgLattice *L = A + j;
+        double c = fam < 2 ? (double)(qx0 + idx) : (double)(qz0 + idx);
+        if (st) c = c * MG_SECOND_STACK;
+        const double off = fam == 0 ? L->ox : (fam == 1 ? L->oy : (fam == 2 ? L->oz : L->ox));
+        int i;
+        double fr;
+        int64_t F;
+        split_dk(c, N.freq[k], N.fexp[k], off, i, fr, F);
+        ShiftSplit &o = tab.e[j][r];
+        o.pk = F < 0 ? -1 : (F | ((int64_t)(i & 255) << 52));
+        o.u = F < 0 ? 0.0 : fade<double>(fr);
+    }
+}
+struct ShiftPair {
+    double a, b; /* ShiftA, ShiftB */
+    bool ok;
+};
+/* both shift noises of the cell in column col and row row from the table (same sums as nn_d); ok false when
+ * an entry or a zero coordinate's split is not a multiple of 2^-52 (the per-cell form handles the cell) */
+template <int TW, int TH>
+static __device__ __noinline__ ShiftPair shift_from_table(const MgNoise &N, const MgLattice *__restrict__ T,
+                                                          const ShiftTable<TW, TH> &tab, int col, int row) {
+    const int64_t M52 = (1LL << 52) - 1;
+    double sa[2] = {0.0, 0.0}, sb[2] = {0.0, 0.0};
+    const MgLattice *A = T + N.base;
+    for (int q = 0; q < 2 * N.nlev; q++) {
+        const int k = q >> 1, st = q & 1, j = st * N.nlev + k;
+        const MgLattice *L = A + j;
+        const ShiftSplit ex = tab.e[j][col], ey = tab.e[j][TW + col], ez = tab.e[j][2 * TW + row],
+                         ew = tab.e[j][2 * TW + TH + row];
+        if ((ex.pk | ey.pk | ez.pk | ew.pk | L->Fy | L->Fz) < 0) return ShiftPair{0.0, 0.0, false};
+        const PlainPerm p{L->p};
+        /* ShiftA (x, 0, z): x input X-side, z input Z-side, y from the header */
+        const double oa = octave_dfix_u(p, (int)(ex.pk >> 52), ex.pk & M52, ex.u, L->iy, L->Fy, L->uyd, (int)(ez.pk >> 52),
+                                        ez.pk & M52, ez.u);
+        /* ShiftB (z, x, 0): x input Z-side, y input X-side, z from the header */
+        const double ob = octave_dfix_u(p, (int)(ew.pk >> 52), ew.pk & M52, ew.u, (int)(ey.pk >> 52), ey.pk & M52, ey.u,
+                                        L->iz, L->Fz, L->uzd);
+        const double ta = N.amp_d[k] * oa * N.vf_d[k], tb = N.amp_d[k] * ob * N.vf_d[k];
+        if (st) { sa[1] += ta; sb[1] += tb; }
+        else { sa[0] += ta; sb[0] += tb; }
+    }
+    return ShiftPair{(sa[0] + sa[1]) * N.vfac, (sb[0] + sb[1]) * N.vfac, true};
+}
+/* the double branch's Overworld climate of a tile cell, the shifts from the tile's table */
+template <int TW, int TH>
+__device__ __forceinline__ void climate_ow_d_tab(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
+                                                 const ShiftTable<TW, TH> &tab, int col, int row, int qx, int qy, int qz,
+                                                 int32_t *tg) {
+    const ShiftPair sp = shift_from_table(W.noise[0], T, tab, col, row);
+    const double X = (double)qx, Z = (double)qz;
+    if (!sp.ok) {
+        climate_ow_d(W, S, T, X, Z, X * MG_SECOND_STACK, Z * MG_SECOND_STACK, qy * 4, tg);
+        return;
+    }
+    climate_ow_d_rest(W, S, T, X + sp.a * 4.0, Z + sp.b * 4.0, qy * 4, tg);
 }
 
 /* Overworld climate of quart cell (qx, qy, qz) -> 6 quantised targets (engine/mc_climate.h:113-170). */

@@ -307,20 +307,25 @@ __device__ __forceinline__ double fix_to_d(int64_t D) {
 __device__ __forceinline__ double fix_lerp(double u, int64_t A, int64_t B) {
     return fix_to_d(A) + u * fix_to_d(B - A);
 }
+/* the same with the smoothstep u of the x fraction given (a precomputed split) */
 template <typename P>
-__device__ __forceinline__ double octave_dfix(const P &p, int ix, double fx, int64_t FX, int iy, int64_t FY, double v,
-                                              int iz, int64_t FZ, double w) {
+__device__ __forceinline__ double octave_dfix_u(const P &p, int ix, int64_t FX, double u, int iy, int64_t FY, double v,
+                                                int iz, int64_t FZ, double w) {
     const int64_t ONE = 1LL << 52;
     const int a = p(ix), b = p(ix + 1);
     const int aa = p(a + iy), ab = p(a + iy + 1);
     const int ba = p(b + iy), bb = p(b + iy + 1);
     const int64_t GX = FX - ONE, GY = FY - ONE, GZ = FZ - ONE;
-    const double u = fade<double>(fx);
     const double x00 = fix_lerp(u, gdot_i(p(aa + iz), FX, FY, FZ), gdot_i(p(ba + iz), GX, FY, FZ));
     const double x10 = fix_lerp(u, gdot_i(p(ab + iz), FX, GY, FZ), gdot_i(p(bb + iz), GX, GY, FZ));
     const double x01 = fix_lerp(u, gdot_i(p(aa + iz + 1), FX, FY, GZ), gdot_i(p(ba + iz + 1), GX, FY, GZ));
     const double x11 = fix_lerp(u, gdot_i(p(ab + iz + 1), FX, GY, GZ), gdot_i(p(bb + iz + 1), GX, GY, GZ));
     return lerp<double>(w, lerp<double>(v, x00, x10), lerp<double>(v, x01, x11));
+}
+template <typename P>
+__device__ __forceinline__ double octave_dfix(const P &p, int ix, double fx, int64_t FX, int iy, int64_t FY, double v,
+                                              int iz, int64_t FZ, double w) {
+    return octave_dfix_u(p, ix, FX, fade<double>(fx), iy, FY, v, iz, FZ, w);
 }
 /* the plain double octave, for a fraction that is not a multiple of 2^-52 (rare): out of line for a plain
  * table, inline for the interleaved shared layout */
