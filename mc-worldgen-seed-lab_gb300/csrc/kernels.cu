@@ -204,12 +204,24 @@ __global__ void __launch_bounds__(128) k_grid(const __grid_constant__ MgWorldDes
     MgSpline *S = reinterpret_cast<MgSpline *>(smem_raw);
     MgLattice *T = reinterpret_cast<MgLattice *>(S + 1);
     stage(W, state, W.ntables, T, S, DIM == MG_OVERWORLD);
+    /* 8 x 16-cell tiles: a double-branch Overworld tile computes its shift noises' splits once per column and
+     * row (shift_table_fill) */
+    const int tw = (nx + 7) / 8;
+    const int col = threadIdx.x % 8, row = threadIdx.x / 8;
+    const int tx0 = (int)(blockIdx.x % (unsigned)tw) * 8, tz0 = (int)(blockIdx.x / (unsigned)tw) * 16;
+    ShiftTable<8, 16> *tab = nullptr;
+    if (!FM && DIM == MG_OVERWORLD && shift_table_ok(W)) {
+        tab = reinterpret_cast<ShiftTable<8, 16> *>(T + W.ntables);
+        __syncthreads(); /* the lattices are staged */
+        shift_table_fill<8, 16, 128>(W.noise[0], T, qx0 + tx0, qz0 + tz0, *tab);
+    }
     __syncthreads();
-    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= (long long)nx * nz) return;
-    const int ix = (int)(g % nx), iz = (int)(g / nx);
+    const int ix = tx0 + col, iz = tz0 + row;
+    if (ix >= nx || iz >= nz) return;
+    const long long g = (long long)iz * nx + ix;
     int32_t tg[6];
-    cell_target<FM, DIM>(W, *S, T, qx0 + ix, qy, qz0 + iz, tg);
+    if (!FM && DIM == MG_OVERWORLD && tab) climate_ow_d_tab(W, *S, T, *tab, col, row, qx0 + ix, qy, qz0 + iz, tg);
+    else cell_target<FM, DIM>(W, *S, T, qx0 + ix, qy, qz0 + iz, tg);
     uint64_t d;
     if (CHAIN) {
         bool tied;
@@ -324,6 +336,10 @@ static unsigned end_tiles(int ncx, int ncz) {
     return (unsigned)(((long long)(ncx + END_TC - 1) / END_TC) * ((ncz + END_TC - 1) / END_TC));
 }
 static size_t grid_smem(const MgWorldDesc &W) { return sizeof(MgSpline) + (size_t)W.ntables * sizeof(MgLattice); }
+/* k_grid's: the double-branch Overworld adds its tiles' shift table */
+static size_t grid_smem_k(const MgWorldDesc &W) {
+    return grid_smem(W) + (W.dim == MG_OVERWORLD && !W.fmode ? sizeof(ShiftTable<8, 16>) : 0);
+}
 
 int launch_setup(const MgWorldDesc &W, const int64_t *d_seeds, int ns, MgLattice *d_states, cudaStream_t st) {
     if (ns <= 0) return 0;
@@ -364,9 +380,10 @@ int launch_points(const MgWorldDesc &W, const MgTreeNode *tree, const MgLattice 
 template <bool FM, int DIM, bool CHAIN>
 static void grid_t(const MgWorldDesc &W, const MgTreeNode *tree, const MgLattice *state, int qx0, int qz0, int nx, int nz,
                    int qy, uint8_t *out, ChainRec *rec, cudaStream_t st) {
-    size_t sm = grid_smem(W);
+    size_t sm = grid_smem_k(W);
     cudaFuncSetAttribute(k_grid<FM, DIM, CHAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    { ProfScope ps_(K_GRID, st); k_grid<FM, DIM, CHAIN><<<blocks_for((long long)nx * nz, 128), 128, sm, st>>>(W, tree, state, qx0, qz0, nx, nz, qy, out, rec); }
+    const long long tiles = (long long)((nx + 7) / 8) * ((nz + 15) / 16);
+    { ProfScope ps_(K_GRID, st); k_grid<FM, DIM, CHAIN><<<(unsigned)tiles, 128, sm, st>>>(W, tree, state, qx0, qz0, nx, nz, qy, out, rec); }
 }
 __global__ void k_end_lookup(const __grid_constant__ MgWorldDesc W, const uint8_t *__restrict__ cls, int cx0, int cz0,
                              int ncx, int qx0, int qz0, int nx, int nz, uint8_t *__restrict__ out) {
