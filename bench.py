@@ -188,13 +188,14 @@ def gpu_peaks(mg) -> dict:
 OCTAVES_PER_SAMPLE = {"minecraft:overworld": 52, "minecraft:the_nether": 8, "minecraft:the_end": 0}
 # FP64 operations per sample as the kernels compute them.  Float branch (26.3+): the two rounded coordinate
 # adds of every octave sample (Overworld 52 x 2, Nether 8 x 2).  Double branch (26.1/26.2), Overworld: the
-# shift noise's 12 octave samples exactly in double (36 each: 2 coordinate adds, 2 smoothsteps of 7, the four
-# first-level lerps' product and sum, 3 more lerps of 3, the amplitude products and sum), the 40 climate
-# octave samples in 59-bit fixed point with only their 2 coordinate adds on the FP64 pipe, and per climate
-# noise the conversion of the fixed-point sum (2) and the screen's two adds and two conversions (4), plus
-# ridges_folded (3 + 4): 432 + 80 + 37 = 549.  Nether: 8 x 2 + 2 x 6 = 28.  The rare values the screen leaves
-# to the exact double path and the End's simplex are left out, so the model is a lower bound.
-FP64_PER_SAMPLE = {("double", "minecraft:overworld"): 549, ("double", "minecraft:the_nether"): 28,
+# shift noise's 12 octave samples exactly in double, their splits and smoothsteps taken from the tile's
+# table (20 each: 4 first-level lerp products and sums, 3 lerps of 3, the amplitude products and sum), the
+# table itself (6 lattices x 48 entries of 8 per 128-cell tile: 18 per sample), the 40 climate octave
+# samples in 59-bit fixed point with only their 2 coordinate adds on the FP64 pipe, and per climate noise
+# the conversion of the fixed-point sum (2) and the screen's two adds and two conversions (4), plus
+# ridges_folded (3 + 4): 240 + 18 + 80 + 37 = 375.  Nether: 8 x 2 + 2 x 6 = 28.  The rare values the screen
+# leaves to the exact double path and the End's simplex are left out, so the model is a lower bound.
+FP64_PER_SAMPLE = {("double", "minecraft:overworld"): 375, ("double", "minecraft:the_nether"): 28,
                    ("float", "minecraft:overworld"): 104, ("float", "minecraft:the_nether"): 16,
                    ("double", "minecraft:the_end"): 0, ("float", "minecraft:the_end"): 0}
 DOUBLE_BRANCH = ("26.1", "26.2")
@@ -209,7 +210,7 @@ def batch_fp64_ops(reqs) -> float:
 # (work units per launch, unit name, pipe peak key).
 # DRAM bytes (read + write) per work unit of a launch, from one ncu capture each: k_batch per sample
 # (300-request prefix of the uneven batch), k_ow_seed_climate per seed (4,096 seeds x 8 points).
-DRAM_BYTES_PER_UNIT = {"k_batch": (4048128 + 2564608) / 10987120, "k_ow_seed_climate": 85504 / 4096}
+DRAM_BYTES_PER_UNIT = {"k_batch": (4094720 + 3446528) / 10987120, "k_ow_seed_climate": 85248 / 4096}
 
 
 def kernel_work(kernel: str, seeds8: bool, ns: int, np_: int, ntables: int) -> tuple[float, str, str] | None:
@@ -530,7 +531,7 @@ def run_batch(args, rank, world, local_rank, mg, ge):
                                                "size, where the output no longer fits L2",
                                "work": f"{ops:.4g} FP64 ops per launch (per-sample model of the screened evaluation)",
                                "peak_source": "measured in-run (FP64 add pipe microbenchmark)",
-                               "binding_pipes": {"fp64": 0.520, "integer_alu": 0.505, "issue_active": 0.597,
+                               "binding_pipes": {"fp64": 0.430, "integer_alu": 0.492, "issue_active": 0.594,
                                                  "source": "ncu sm__inst_executed_pipe_* of a 300-request launch "
                                                            "(profiles/k_batch_uneven_batch.md)"}}
         if args.split_classes:
