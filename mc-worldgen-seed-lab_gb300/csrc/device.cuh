@@ -287,27 +287,16 @@ __device__ __forceinline__ int64_t gdot_i(int h, int64_t x, int64_t y, int64_t z
     const int4 g = __ldg(&kGradI[h & 15]);
     return x * (int64_t)g.x + y * (int64_t)g.y + z * (int64_t)g.z;
 }
-/* D * 2^-52 rounded to the nearest double, ties to even (|D| < 2^54; exact below 2^53) */
-__device__ __forceinline__ double fix_to_d(int64_t D) {
-    if (D == 0) return 0.0;
-    const uint64_t sign = (uint64_t)D & 0x8000000000000000ULL;
-    uint64_t x = D < 0 ? (uint64_t)0 - (uint64_t)D : (uint64_t)D;
-    int L = 64 - __clzll((long long)x); /* 1 .. 54 */
-    uint64_t mant;
-    if (L <= 53) {
-        mant = x << (53 - L);
-    } else {
-        mant = x >> 1;
-        if ((x & 1) && (mant & 1)) mant++;
-        if (mant >> 53) { mant >>= 1; L++; }
-    }
-    return __longlong_as_double((long long)(sign | ((uint64_t)(L + 970) << 52) | (mant & ((1ULL << 52) - 1))));
+/* lerp(u, a, b) = a + u * (b - a) for a = A * 2^-52, b = B * 2^-52, scaled by 2^52: the hardware's
+ * round-to-nearest-even conversions of A (|A| <= 2^53: exact) and of B - A (|B - A| < 2^55: rounded as the
+ * reference's subtraction b - a rounds), then the product and the sum.  Scaling by a power of two commutes
+ * with every rounding while the values stay normal (here they are integers or products of a smoothstep
+ * above 2^-160 with them), so the scaled lerps give 2^52 times the reference's lerps exactly. */
+__device__ __forceinline__ double fix_lerp52(double u, int64_t A, int64_t B) {
+    return __ll2double_rn(A) + u * __ll2double_rn(B - A);
 }
-/* lerp(u, a, b) = a + u * (b - a) for a = A * 2^-52, b = B * 2^-52 */
-__device__ __forceinline__ double fix_lerp(double u, int64_t A, int64_t B) {
-    return fix_to_d(A) + u * fix_to_d(B - A);
-}
-/* the same with the smoothstep u of the x fraction given (a precomputed split) */
+/* the same with the smoothstep u of the x fraction given (a precomputed split); the second and third lerp
+ * levels run on the scaled values and one product by 2^-52 (exact) undoes the scale */
 template <typename P>
 __device__ __forceinline__ double octave_dfix_u(const P &p, int ix, int64_t FX, double u, int iy, int64_t FY, double v,
                                                 int iz, int64_t FZ, double w) {
@@ -316,11 +305,11 @@ __device__ __forceinline__ double octave_dfix_u(const P &p, int ix, int64_t FX, 
     const int aa = p(a + iy), ab = p(a + iy + 1);
     const int ba = p(b + iy), bb = p(b + iy + 1);
     const int64_t GX = FX - ONE, GY = FY - ONE, GZ = FZ - ONE;
-    const double x00 = fix_lerp(u, gdot_i(p(aa + iz), FX, FY, FZ), gdot_i(p(ba + iz), GX, FY, FZ));
-    const double x10 = fix_lerp(u, gdot_i(p(ab + iz), FX, GY, FZ), gdot_i(p(bb + iz), GX, GY, FZ));
-    const double x01 = fix_lerp(u, gdot_i(p(aa + iz + 1), FX, FY, GZ), gdot_i(p(ba + iz + 1), GX, FY, GZ));
-    const double x11 = fix_lerp(u, gdot_i(p(ab + iz + 1), FX, GY, GZ), gdot_i(p(bb + iz + 1), GX, GY, GZ));
-    return lerp<double>(w, lerp<double>(v, x00, x10), lerp<double>(v, x01, x11));
+    const double x00 = fix_lerp52(u, gdot_i(p(aa + iz), FX, FY, FZ), gdot_i(p(ba + iz), GX, FY, FZ));
+    const double x10 = fix_lerp52(u, gdot_i(p(ab + iz), FX, GY, FZ), gdot_i(p(bb + iz), GX, GY, FZ));
+    const double x01 = fix_lerp52(u, gdot_i(p(aa + iz + 1), FX, FY, GZ), gdot_i(p(ba + iz + 1), GX, FY, GZ));
+    const double x11 = fix_lerp52(u, gdot_i(p(ab + iz + 1), FX, GY, GZ), gdot_i(p(bb + iz + 1), GX, GY, GZ));
+    return lerp<double>(w, lerp<double>(v, x00, x10), lerp<double>(v, x01, x11)) * 0x1.0p-52;
 }
 template <typename P>
 __device__ __forceinline__ double octave_dfix(const P &p, int ix, double fx, int64_t FX, int iy, int64_t FY, double v,
