@@ -191,12 +191,11 @@ OCTAVES_PER_SAMPLE = {"minecraft:overworld": 52, "minecraft:the_nether": 8, "min
 # shift noise's 12 octave samples exactly in double, their splits and smoothsteps taken from the tile's
 # table (29 each: 8 conversions of the exact gradient sums and differences, 4 first-level lerp products and
 # sums, 3 lerps of 3, the product undoing the 2^52 scale, the amplitude products and sum), the table itself
-# (6 lattices x 48 entries of 8 per 128-cell tile: 18 per sample), the 40 climate octave samples in 59-bit
-# fixed point with only their 2 coordinate adds on the FP64 pipe, and per climate noise the conversion of
-# the fixed-point sum (2) and the screen's two adds and two conversions (4), plus ridges_folded (3 + 4):
-# 348 + 18 + 80 + 37 = 483.  Nether: 8 x 2 + 2 x 6 = 28.  The rare values the screen
-# leaves to the exact double path and the End's simplex are left out, so the model is a lower bound.
-FP64_PER_SAMPLE = {("double", "minecraft:overworld"): 483, ("double", "minecraft:the_nether"): 28,
+# (6 lattices x 48 entries of 8 per 128-cell tile: 18 per sample), and the 40 climate octave samples in
+# 59-bit fixed point with only their 2 coordinate adds on the FP64 pipe (the screens and ridges_folded run
+# on the integer and conversion pipes): 348 + 18 + 80 = 446.  Nether: 8 x 2 = 16.  The rare values the
+# screen leaves to the exact double path and the End's simplex are left out, so the model is a lower bound.
+FP64_PER_SAMPLE = {("double", "minecraft:overworld"): 446, ("double", "minecraft:the_nether"): 16,
                    ("float", "minecraft:overworld"): 104, ("float", "minecraft:the_nether"): 16,
                    ("double", "minecraft:the_end"): 0, ("float", "minecraft:the_end"): 0}
 DOUBLE_BRANCH = ("26.1", "26.2")

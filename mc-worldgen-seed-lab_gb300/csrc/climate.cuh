@@ -56,32 +56,36 @@ __device__ __forceinline__ void climate_finish_df(const MgWorldDesc &W, const Mg
 __device__ __forceinline__ float nn_d_y0_float(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
                                                double xc, double zc) {
     float f;
-    if (N.fix_err >= 0.0) {
+    if (N.fix_eq >= 0) {
         const int64_t q = nn_q<false>(N, T, x, z, xc, zc);
-        if (q != MG_QFAIL && cast_settled((double)q * 0x1.0p-59, N.fix_err, f)) return f;
+        if (q != MG_QFAIL && cast_settled_q(q, N.fix_eq, f)) return f;
     }
     return (float)nn_d_y0(N, T, x, z, xc, zc);
 }
-/* ridges_folded (|(|r| + c0)| + c1) * c2 of a ridge value.  ridges_folded of two doubles within d of each
- * other, each step rounded, differ by at most |c2| (d + 1e-14) (values below 17 before the product), so the
- * screen's bound for it, from a ridge value within err of the reference's, is |c2| (err + 1e-14) + 1e-13. */
+/* ridges_folded (|(|r| + c0)| + c1) * c2 of a ridge value (the exact path) */
 __device__ __forceinline__ double ridges_folded_d(const MgWorldDesc &W, double r) {
     return (fabs(fabs(r) + W.rf_d[0]) + W.rf_d[1]) * W.rf_d[2];
 }
-__device__ __forceinline__ double ridges_folded_err(const MgWorldDesc &W, double err) {
-    return fabs(W.rf_d[2]) * (err + 1e-14) + 1e-13;
+/* the float of ridges_folded from a fixed-point ridge value q (units of 2^-59) within the ridge screen's
+ * bound: the constants are multiples of 2^-59 (W.rf_eq >= 0), so the sums are exact and the product rounds
+ * down by less than one unit (it runs for sums below 4; others go to the exact path).  ridges_folded of two
+ * values within d of each other differ by at most |c2| d, and the reference's three roundings of it (values
+ * below 17) by less than |c2| 1e-14 + 1e-13, so W.rf_eq is |c2| (err + 1e-14) + 1e-13 plus one unit. */
+__device__ __forceinline__ bool ridges_folded_settled(const MgWorldDesc &W, int64_t q, float &f) {
+    int64_t v = (q < 0 ? -q : q) + W.rf_q[0];
+    v = (v < 0 ? -v : v) + W.rf_q[1];
+    if (v >= (4LL << MG_Q) || v <= -(4LL << MG_Q)) return false;
+    const int64_t c = W.rf_q[2], m = mulq_us(c < 0 ? -c : c, v);
+    return cast_settled_q(c < 0 ? -m : m, W.rf_eq, f);
 }
 /* ridge noise and ridges_folded as floats */
 __device__ __forceinline__ void ridge_float(const MgWorldDesc &W, const MgLattice *__restrict__ T, double x, double z,
                                             double xc, double zc, float &rvf, float &rff) {
     const MgNoise &N = W.noise[5];
-    if (N.fix_err >= 0.0) {
+    if (W.rf_eq >= 0) {
         const int64_t q = nn_q<false>(N, T, x, z, xc, zc);
-        if (q != MG_QFAIL) {
-            const double a = (double)q * 0x1.0p-59;
-            if (cast_settled(a, N.fix_err, rvf) && cast_settled(ridges_folded_d(W, a), ridges_folded_err(W, N.fix_err), rff))
-                return;
-        }
+        if (q != MG_QFAIL && cast_settled_q(q, N.fix_eq, rvf) && ridges_folded_settled(W, q, rff))
+            return;
     }
     const double rv = nn_d_y0(N, T, x, z, xc, zc);
     rvf = (float)rv;

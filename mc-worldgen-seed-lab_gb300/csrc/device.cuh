@@ -689,12 +689,15 @@ static __device__ __noinline__ int64_t nn_q(const MgNoise &N, const MgLattice *_
     }
     return acc;
 }
-/* the float the reference's double value rounds to, from an approximation a within err of that value: true
- * when every double in [a - err, a + err] rounds to the same float (rounding is monotone; err includes the
- * rounding of a +- err) */
-__device__ __forceinline__ bool cast_settled(double a, double err, float &f) {
-    const float lo = __double2float_rn(a - err), hi = __double2float_rn(a + err);
-    f = lo;
+/* the float the reference's double value rounds to, from a fixed-point approximation q (units of 2^-59)
+ * within eq units of that value: true when every real in [q - eq, q + eq] 2^-59 rounds to the same float.
+ * No FP64 pipe: the hardware's s64 -> f32 conversion rounds the integers q - eq and q + eq to
+ * nearest (the scale 2^-59 is exact and keeps the order, so equal roundings of the two ends settle the
+ * rounding of every value between them); the float is the rounded end times 2^-59 (normal: |q - eq| >= 1
+ * when the ends agree, since eq > 0) */
+__device__ __forceinline__ bool cast_settled_q(int64_t q, int64_t eq, float &f) {
+    const float lo = __ll2float_rn(q - eq), hi = __ll2float_rn(q + eq);
+    f = lo * 0x1.0p-59f;
     return lo == hi;
 }
 

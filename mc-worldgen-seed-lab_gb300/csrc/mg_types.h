@@ -36,9 +36,11 @@ typedef struct {
     double vfac;                   /* double branch: NormalNoise value factor */
     float amp_f[MG_MAX_OCT];       /* float branch: layer amplitude */
     /* double branch, screened evaluation: amp_d[k] * vf_d[k] * vfac times 2^59, and the bound on the
-     * difference between the fixed-point value and the reference's double value (< 0: not screened) */
+     * difference between the fixed-point value and the reference's double value (< 0: not screened), as a
+     * double and in units of 2^-59 (rounded up) */
     int64_t cq[MG_MAX_OCT];
     double fix_err;
+    int64_t fix_eq;
 } MgNoise;
 
 /* Offset spline (CubicSpline over continents, erosion, ridges, ridges_folded), float.
@@ -83,6 +85,10 @@ typedef struct {
     int32_t grad_from_y, grad_to_y;
     double grad_from_d, grad_to_d, off_d;
     double rf_d[3];
+    /* ridges_folded's constants times 2^59 and the screen's bound for it in units of 2^-59 (rounded up;
+     * < 0: a constant is not a multiple of 2^-59 below 8, and the ridge noise is not screened) */
+    int64_t rf_q[3];
+    int64_t rf_eq;
     float grad_from_f, grad_to_f, off_f;
     float rf_f[3];
     int32_t end_ids[5];            /* the_end, end_highlands, end_midlands, small_end_islands, end_barrens */

@@ -174,12 +174,11 @@ __global__ void k_check_noise(const __grid_constant__ MgWorldDesc W, const MgLat
             const double a = (double)q * 0x1.0p-59;
             const double ratio = fabs(a - e) / N.fix_err;
             worst = ratio > worst ? ratio : worst;
-            if (!mgd::cast_settled(a, N.fix_err, f)) { left++; continue; }
+            if (!mgd::cast_settled_q(q, N.fix_eq, f)) { left++; continue; }
             bad += f != (float)e;
             if (W.dim == MG_OVERWORLD && j == 4) {
-                const double rfa = (fabs(fabs(a) + W.rf_d[0]) + W.rf_d[1]) * W.rf_d[2];
                 const double rfe = (fabs(fabs(e) + W.rf_d[0]) + W.rf_d[1]) * W.rf_d[2];
-                if (!mgd::cast_settled(rfa, fabs(W.rf_d[2]) * (N.fix_err + 1e-14) + 1e-13, f)) { left++; continue; }
+                if (W.rf_eq < 0 || !mg::ridges_folded_settled(W, q, f)) { left++; continue; }
                 bad += f != (float)rfe;
             }
         }
@@ -215,9 +214,8 @@ __global__ void k_check_climate(const __grid_constant__ MgWorldDesc W, const MgL
             v[j] = mgd::nn_d_y0(N, T, x, z, xc, zc);
             const int64_t q = N.fix_err < 0.0 ? MG_QFAIL : mgd::nn_q<false>(N, T, x, z, xc, zc);
             float f;
-            exact |= q == MG_QFAIL || !mgd::cast_settled((double)q * 0x1.0p-59, N.fix_err, f);
-            if (j == 4 && !exact)
-                exact |= !mgd::cast_settled(mg::ridges_folded_d(W, (double)q * 0x1.0p-59), mg::ridges_folded_err(W, N.fix_err), f);
+            exact |= q == MG_QFAIL || !mgd::cast_settled_q(q, N.fix_eq, f);
+            if (j == 4 && !exact) exact |= W.rf_eq < 0 || !mg::ridges_folded_settled(W, q, f);
         }
         mg::climate_finish_d(W, W.spline, v[0], v[1], v[2], v[3], v[4], by, want);
         bool diff = false;

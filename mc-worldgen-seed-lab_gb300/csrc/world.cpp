@@ -240,6 +240,7 @@ static void noise_double(MgNoise *s, const NoiseParams &P, int legacy) {
     }
     for (int k = 0; k < s->nlev; k++) s->cq[k] = q59_product(s->amp_d[k], s->vf_d[k], s->vfac);
     s->fix_err = screen_bound(s);
+    s->fix_eq = s->fix_err < 0.0 ? -1 : (int64_t)ceil(s->fix_err * 0x1.0p59);
     octave_seeds(s);
 }
 
@@ -638,6 +639,24 @@ int build_world(const char *root, int version, int dim, const char *preset, MgWo
     }
     if (nt > MG_MAX_TABLES) { *err = "too many octaves"; return MCGEN_E_DATA; }
     D->ntables = nt;
+    /* ridges_folded in fixed point (the screen of the ridge noise): the constants must be multiples of 2^-59
+     * below 8 in magnitude; its bound from the ridge value's is |c2| (err + 1e-14) + 1e-13 (the reference's
+     * three roundings), plus one unit for the fixed-point product */
+    D->rf_eq = -1;
+    if (dim == MG_OVERWORLD && !D->fmode && D->noise[5].fix_err >= 0.0) {
+        const MgNoise &R = D->noise[5];
+        double csum = 0.0;
+        for (int k = 0; k < R.nlev; k++) csum += fabs(R.amp_d[k] * R.vf_d[k] * R.vfac);
+        /* |ridge| below 4.2 csum (as in screen_bound): the sums stay below 15; the product runs only for
+         * sums below 4 (ridges_folded_settled), so |c2| < 3.75 keeps it below 15 */
+        bool exact = 4.2 * csum + fabs(D->rf_d[0]) + fabs(D->rf_d[1]) < 15.0 && fabs(D->rf_d[2]) < 3.75;
+        for (int i = 0; i < 3; i++) {
+            const double c = D->rf_d[i];
+            exact = exact && fabs(c) < 8.0 && ldexp(floor(ldexp(c, 59)), -59) == c;
+            D->rf_q[i] = exact ? (int64_t)ldexp(c, 59) : 0;
+        }
+        if (exact) D->rf_eq = (int64_t)ceil((fabs(D->rf_d[2]) * (D->noise[5].fix_err + 1e-14) + 1e-13) * 0x1.0p59) + 1;
+    }
     int nleaf = 0;
     int rc = load_tree(root, version, dim, tree, &nleaf, err);
     if (rc) return rc;

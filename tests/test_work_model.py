@@ -29,8 +29,8 @@ def test_fp64_model_covers_versions():
     reqs = [("26.1", "minecraft:overworld", 1, 0, 0, 16, 16), ("26.3", "minecraft:the_nether", 2, 0, 0, 8, 16),
             ("26.2", "minecraft:the_end", 3, 0, 0, 16, 16), ("26.4-snapshot-2", "minecraft:overworld", 4, 0, 0, 2, 16),
             ("26.2", "minecraft:the_nether", 5, 0, 0, 4, 16)]
-    assert bench.batch_fp64_ops(reqs) == 256 * 483 + 64 * 8 * 2 + 0 + 4 * 52 * 2 + 16 * 28
+    assert bench.batch_fp64_ops(reqs) == 256 * 446 + 64 * 8 * 2 + 0 + 4 * 52 * 2 + 16 * 16
     # the double branch's model: 12 shift octave samples in double with tabled splits and smoothsteps, the
-    # per-tile table (6 x 48 entries of 8 over 128 cells), 40 fixed-point ones, per-noise screen
-    assert bench.FP64_PER_SAMPLE[("double", "minecraft:overworld")] == 12 * 29 + 6 * 48 * 8 // 128 + 40 * 2 + 5 * 6 + 7
+    # per-tile table (6 x 48 entries of 8 over 128 cells), 40 fixed-point ones (screens off the FP64 pipe)
+    assert bench.FP64_PER_SAMPLE[("double", "minecraft:overworld")] == 12 * 29 + 6 * 48 * 8 // 128 + 40 * 2
     assert bench.FP64_PER_SAMPLE[("float", "minecraft:overworld")] == bench.OCTAVES_PER_SAMPLE["minecraft:overworld"] * 2
