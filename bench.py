@@ -210,7 +210,7 @@ def batch_fp64_ops(reqs) -> float:
 # (work units per launch, unit name, pipe peak key).
 # DRAM bytes (read + write) per work unit of a launch, from one ncu capture each: k_batch per sample
 # (300-request prefix of the uneven batch), k_ow_seed_climate per seed (4,096 seeds x 8 points).
-DRAM_BYTES_PER_UNIT = {"k_batch": (4094720 + 3446528) / 10987120, "k_ow_seed_climate": 85248 / 4096}
+DRAM_BYTES_PER_UNIT = {"k_batch": (4063744 + 3648512) / 10987120, "k_ow_seed_climate": 85248 / 4096}
 
 
 def kernel_work(kernel: str, seeds8: bool, ns: int, np_: int, ntables: int) -> tuple[float, str, str] | None:
@@ -531,7 +531,7 @@ def run_batch(args, rank, world, local_rank, mg, ge):
                                                "size, where the output no longer fits L2",
                                "work": f"{ops:.4g} FP64 ops per launch (per-sample model of the screened evaluation)",
                                "peak_source": "measured in-run (FP64 add pipe microbenchmark)",
-                               "binding_pipes": {"fp64": 0.430, "integer_alu": 0.492, "issue_active": 0.594,
+                               "binding_pipes": {"fp64": 0.518, "integer_alu": 0.511, "issue_active": 0.611,
                                                  "source": "ncu sm__inst_executed_pipe_* of a 300-request launch "
                                                            "(profiles/k_batch_uneven_batch.md)"}}
         if args.split_classes:
