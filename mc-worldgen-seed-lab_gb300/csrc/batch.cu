@@ -146,14 +146,16 @@ struct BatchSmem {
         BatchLat o;
         BatchEnd end;
     };
+    double depth_g; /* the double-branch Overworld tile's depth gradient (depth_grad_d) */
     int tile, req, state;
 };
 
-/* tab: the tile's shift table (double-branch Overworld, ENGINE rule) or null */
+/* tab: the tile's shift table (double-branch Overworld, ENGINE rule) or null; g: with a table, the tile's
+ * depth gradient */
 template <bool FM, int DIM, int TILE_W>
 __device__ __forceinline__ void batch_cells(const MgWorldDesc &W, const MgSpline &S, const MgLattice *T,
                                             const MgTreeNode *tree, const MgBatchReq &R, int tx0, int tz0,
-                                            const ShiftTable<8, BNT / 8> *tab, uint8_t *out) {
+                                            const ShiftTable<8, BNT / 8> *tab, double g, uint8_t *out) {
     const int col = threadIdx.x % TILE_W, row = threadIdx.x / TILE_W;
     const int ix = tx0 + col, iz = tz0 + row;
     if (ix >= R.nx || iz >= R.nz) return;
@@ -163,7 +165,7 @@ __device__ __forceinline__ void batch_cells(const MgWorldDesc &W, const MgSpline
         b = (uint8_t)cell_chunk<FM, DIM>(W, S, T, tree, qx, R.qy, qz);
     } else {
         int32_t tg[6];
-        if (!FM && DIM == MG_OVERWORLD && TILE_W == 8 && tab) climate_ow_d_tab(W, S, T, *tab, col, row, qx, R.qy, qz, tg);
+        if (!FM && DIM == MG_OVERWORLD && TILE_W == 8 && tab) climate_ow_d_tab(W, S, T, *tab, col, row, qx, R.qy, qz, g, tg);
         else cell_target<FM, DIM>(W, S, T, qx, R.qy, qz, tg);
         uint64_t d;
         b = tree[tree_search(tree, tg, -1, d)].biome;
@@ -257,18 +259,20 @@ __global__ void __launch_bounds__(BNT, MINB) k_batch(const MgWorldDesc *__restri
         const int tx0 = (tile % tw) * TILE_W, tz0 = (tile / tw) * TILE_H;
         const MgTreeNode *tree = trees[R.world];
         if (W.fmode) {
-            if (W.dim == MG_OVERWORLD) batch_cells<true, MG_OVERWORLD, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, out);
-            else batch_cells<true, MG_NETHER, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, out);
+            if (W.dim == MG_OVERWORLD) batch_cells<true, MG_OVERWORLD, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, 0.0, out);
+            else batch_cells<true, MG_NETHER, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, 0.0, out);
         } else if (W.dim == MG_OVERWORLD) {
             /* the tile's shift splits, computed once per column and row (ENGINE rule) */
             const bool tab = TILE_W == 8 && R.tie != MG_TIE_CHUNK_CELL && shift_table_ok(W);
             if (tab) {
                 shift_table_fill<8, BNT / 8, BNT>(W.noise[0], sm.o.lat, R.qx0 + tx0, R.qz0 + tz0, sm.o.shift);
+                if (threadIdx.x == BNT - 1) sm.depth_g = depth_grad_d(W, R.qy * 4); /* a thread with fewer entries */
                 __syncthreads();
             }
-            batch_cells<false, MG_OVERWORLD, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, tab ? &sm.o.shift : nullptr, out);
+            batch_cells<false, MG_OVERWORLD, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, tab ? &sm.o.shift : nullptr,
+                                                     tab ? sm.depth_g : 0.0, out);
         } else {
-            batch_cells<false, MG_NETHER, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, out);
+            batch_cells<false, MG_NETHER, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, 0.0, out);
         }
     }
 }

@@ -25,28 +25,29 @@ __device__ __forceinline__ void climate_finish_f(const MgWorldDesc &W, const MgS
     tg[0] = quantize(tv); tg[1] = quantize(hv); tg[2] = quantize(cv);
     tg[3] = quantize(ev); tg[4] = quantize(depth); tg[5] = quantize(rv);
 }
+/* the double branch's depth gradient at block y, clamped (y_clamped_gradient): a function of y alone, which
+ * the tile kernels compute once per tile (an IEEE double division and conversions: about 20 FP64 operations) */
+__device__ __forceinline__ double depth_grad_d(const MgWorldDesc &W, int by) {
+    const double fac = ((double)by - (double)W.grad_from_y) / ((double)W.grad_to_y - (double)W.grad_from_y);
+    return fac < 0.0 ? W.grad_from_d : (fac > 1.0 ? W.grad_to_d : W.grad_from_d + fac * (W.grad_to_d - W.grad_from_d));
+}
 /* the same in the double branch */
 __device__ __forceinline__ void climate_finish_d(const MgWorldDesc &W, const MgSpline &S, double tv, double hv, double cv,
                                                  double ev, double rv, int by, int32_t tg[6]) {
     double rf = (fabs(fabs(rv) + W.rf_d[0]) + W.rf_d[1]) * W.rf_d[2];
     float co[4] = {(float)cv, (float)ev, (float)rv, (float)rf};
     double off = 0.0 + (W.off_d + (double)spline_eval(S, co)) * 1.0;
-    double fac = ((double)by - (double)W.grad_from_y) / ((double)W.grad_to_y - (double)W.grad_from_y);
-    double g = fac < 0.0 ? W.grad_from_d
-                         : (fac > 1.0 ? W.grad_to_d : W.grad_from_d + fac * (W.grad_to_d - W.grad_from_d));
-    double depth = g + off;
+    double depth = depth_grad_d(W, by) + off;
     tg[0] = quantize((float)tv); tg[1] = quantize((float)hv); tg[2] = quantize((float)cv);
     tg[3] = quantize((float)ev); tg[4] = quantize((float)depth); tg[5] = quantize((float)rv);
 }
 
-/* the same from the float values the reference takes of the five noises and of ridges_folded */
+/* the same from the float values the reference takes of the five noises and of ridges_folded, with the
+ * depth gradient g = depth_grad_d(W, by) given */
 __device__ __forceinline__ void climate_finish_df(const MgWorldDesc &W, const MgSpline &S, float tf, float hf, float cf,
-                                                  float ef, float rvf, float rff, int by, int32_t tg[6]) {
+                                                  float ef, float rvf, float rff, double g, int32_t tg[6]) {
     float co[4] = {cf, ef, rvf, rff};
     double off = 0.0 + (W.off_d + (double)spline_eval(S, co)) * 1.0;
-    double fac = ((double)by - (double)W.grad_from_y) / ((double)W.grad_to_y - (double)W.grad_from_y);
-    double g = fac < 0.0 ? W.grad_from_d
-                         : (fac > 1.0 ? W.grad_to_d : W.grad_from_d + fac * (W.grad_to_d - W.grad_from_d));
     double depth = g + off;
     tg[0] = quantize(tf); tg[1] = quantize(hf); tg[2] = quantize(cf);
     tg[3] = quantize(ef); tg[4] = quantize((float)depth); tg[5] = quantize(rvf);
@@ -95,7 +96,7 @@ __device__ __forceinline__ void ridge_float(const MgWorldDesc &W, const MgLattic
 /* double branch of the Overworld climate after the shift: the climate noises screened at the exact shifted
  * coordinates, the finish (out of line: reached from the per-cell and the per-tile shift forms) */
 static __device__ __noinline__ void climate_ow_d_rest(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
-                                                      double x, double z, int by, int32_t *tg) {
+                                                      double x, double z, double g, int32_t *tg) {
     const double xc = x * MG_SECOND_STACK, zc = z * MG_SECOND_STACK;
     const float tf = nn_d_y0_float(W.noise[1], T, x, z, xc, zc);
     const float hf = nn_d_y0_float(W.noise[2], T, x, z, xc, zc);
@@ -103,7 +104,7 @@ static __device__ __noinline__ void climate_ow_d_rest(const MgWorldDesc &W, cons
     const float ef = nn_d_y0_float(W.noise[4], T, x, z, xc, zc);
     float rvf, rff;
     ridge_float(W, T, x, z, xc, zc, rvf, rff);
-    climate_finish_df(W, S, tf, hf, cf, ef, rvf, rff, by, tg);
+    climate_finish_df(W, S, tf, hf, cf, ef, rvf, rff, g, tg);
 }
 /* double branch of the Overworld climate, out of line (the kernels reach the climate from two sites each:
  * the cell itself and the tie chain).  The shift noises stay exact in double: their value moves the climate
@@ -113,7 +114,7 @@ static __device__ __noinline__ void climate_ow_d(const MgWorldDesc &W, const MgS
                                                  double X, double Z, double Xc, double Zc, int by, int32_t *tg) {
     const double sx = nn_d_y0(W.noise[0], T, X, Z, Xc, Zc) * 4.0;
     const double sz = nn_d_z0(W.noise[0], T, Z, X, Zc, Xc) * 4.0;
-    climate_ow_d_rest(W, S, T, X + sx, Z + sz, by, tg);
+    climate_ow_d_rest(W, S, T, X + sx, Z + sz, depth_grad_d(W, by), tg);
 }
 
 /* Shift noises of a tile, double branch.  Every input of ShiftA (x, 0, z) and ShiftB (z, x, 0) depends on
@@ -190,18 +191,19 @@ static __device__ __noinline__ ShiftPair shift_from_table(const MgNoise &N, cons
     }
     return ShiftPair{(sa[0] + sa[1]) * N.vfac, (sb[0] + sb[1]) * N.vfac, true};
 }
-/* the double branch's Overworld climate of a tile cell, the shifts from the tile's table */
+/* the double branch's Overworld climate of a tile cell, the shifts from the tile's table; g the tile's depth
+ * gradient, depth_grad_d(W, 4 qy) */
 template <int TW, int TH>
 __device__ __forceinline__ void climate_ow_d_tab(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
                                                  const ShiftTable<TW, TH> &tab, int col, int row, int qx, int qy, int qz,
-                                                 int32_t *tg) {
+                                                 double g, int32_t *tg) {
     const ShiftPair sp = shift_from_table(W.noise[0], T, tab, col, row);
     const double X = (double)qx, Z = (double)qz;
     if (!sp.ok) {
         climate_ow_d(W, S, T, X, Z, X * MG_SECOND_STACK, Z * MG_SECOND_STACK, qy * 4, tg);
         return;
     }
-    climate_ow_d_rest(W, S, T, X + sp.a * 4.0, Z + sp.b * 4.0, qy * 4, tg);
+    climate_ow_d_rest(W, S, T, X + sp.a * 4.0, Z + sp.b * 4.0, g, tg);
 }
 
 /* Overworld climate of quart cell (qx, qy, qz) -> 6 quantised targets (engine/mc_climate.h:113-170). */

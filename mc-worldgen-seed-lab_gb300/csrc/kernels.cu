@@ -210,17 +210,19 @@ __global__ void __launch_bounds__(128) k_grid(const __grid_constant__ MgWorldDes
     const int col = threadIdx.x % 8, row = threadIdx.x / 8;
     const int tx0 = (int)(blockIdx.x % (unsigned)tw) * 8, tz0 = (int)(blockIdx.x / (unsigned)tw) * 16;
     ShiftTable<8, 16> *tab = nullptr;
+    __shared__ double depth_g; /* with a table: the depth gradient at qy (depth_grad_d), once per CTA */
     if (!FM && DIM == MG_OVERWORLD && shift_table_ok(W)) {
         tab = reinterpret_cast<ShiftTable<8, 16> *>(T + W.ntables);
         __syncthreads(); /* the lattices are staged */
         shift_table_fill<8, 16, 128>(W.noise[0], T, qx0 + tx0, qz0 + tz0, *tab);
+        if (threadIdx.x == 127) depth_g = depth_grad_d(W, qy * 4);
     }
     __syncthreads();
     const int ix = tx0 + col, iz = tz0 + row;
     if (ix >= nx || iz >= nz) return;
     const long long g = (long long)iz * nx + ix;
     int32_t tg[6];
-    if (!FM && DIM == MG_OVERWORLD && tab) climate_ow_d_tab(W, *S, T, *tab, col, row, qx0 + ix, qy, qz0 + iz, tg);
+    if (!FM && DIM == MG_OVERWORLD && tab) climate_ow_d_tab(W, *S, T, *tab, col, row, qx0 + ix, qy, qz0 + iz, depth_g, tg);
     else cell_target<FM, DIM>(W, *S, T, qx0 + ix, qy, qz0 + iz, tg);
     uint64_t d;
     if (CHAIN) {
