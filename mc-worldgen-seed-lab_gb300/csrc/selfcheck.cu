@@ -6,7 +6,7 @@
  * offsets at 0, near 256 and on integers.  Also: the double branch's fixed-point octave (octave_dfix)
  * against the plain double octave on random permutations and fractions, the single-precision screen of
  * BiomeManager's zoom (zoom_pick) against the double-precision choice among all 8 candidates, the
- * fixed-point screen of the double branch's climate noises (nn_q + cast_settled) against the exact double
+ * fixed-point screen of the double branch's climate noises (nn_q + cast_settled_q) against the exact double
  * evaluation on a world's own seed lattices, and the double branch's whole Overworld climate as the kernels
  * compute it (climate_ow_d) against the plain double evaluation, and the 32-bit R-tree searches against
  * the 64-bit stack searches. */

@@ -203,8 +203,9 @@ static int64_t q59_product(double a, double b, double c) {
  * unit): a smoothstep is within 27 q (t^2, t^3 and the final product; the factor 6t^2 - 15t + 10 <= 10
  * carries six times t^2's error), a lerp adds 4 x its weight's error plus one unit to the larger of its
  * inputs' errors, so an octave is within 3 x (4 x 27 + 1) = 327 q and a level's product with its constant
- * within (654 |c| + 6) q.  The bound is taken 25 % larger, and cast_settled's two roundings of a +- err are
- * added.  Negative: not screened (sum too large for the fixed point's range). */
+ * within (654 |c| + 6) q.  The bound is taken 25 % larger, plus 4u times the value's range as a margin (the
+ * screen, cast_settled_q, compares exact integer ends: nothing of its own to add).  Negative: not screened (sum
+ * too large for the fixed point's range). */
 static double screen_bound(const MgNoise *s) {
     const double u = 0x1.0p-53;
     double c = 0.0;
