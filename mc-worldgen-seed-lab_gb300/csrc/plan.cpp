@@ -51,6 +51,36 @@ namespace {
 
 int cuda_rc(cudaError_t e) { return e == cudaSuccess ? MCGEN_OK : e == cudaErrorMemoryAllocation ? MCGEN_E_NOMEM : MCGEN_E_INTERNAL; }
 
+/* Device memory of plans and of the host-buffer run's output: a stream-ordered pool of the library's that
+ * keeps up to 4 GiB of freed memory mapped for the next plan (the device's default pool returns it at every
+ * synchronisation, and a plan's arena plus a run's output are hundreds of MB: mapping them again each time
+ * cost milliseconds per call).  Created on first use, under the ABI lock. */
+cudaMemPool_t g_pool = nullptr;
+int g_pool_dev = -1;
+cudaError_t plan_pool(cudaMemPool_t *out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e) return e;
+    if (!g_pool || g_pool_dev != dev) {
+        cudaMemPoolProps props;
+        memset(&props, 0, sizeof props);
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        if ((e = cudaMemPoolCreate(&pool, &props))) return e;
+        uint64_t keep = 4ULL << 30;
+        if ((e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep))) {
+            cudaMemPoolDestroy(pool);
+            return e;
+        }
+        g_pool = pool; /* a pool of another device stays alive: memory of plans made there returns to it */
+        g_pool_dev = dev;
+    }
+    *out = g_pool;
+    return cudaSuccess;
+}
+
 int enqueue(McGb300Plan *p, uint8_t *d_out, int shape, cudaStream_t st) {
     for (int d = 0; d < 3; d++) {
         if (!p->nent[d]) continue;
@@ -64,7 +94,12 @@ int enqueue(McGb300Plan *p, uint8_t *d_out, int shape, cudaStream_t st) {
 void free_plan(McGb300Plan *p) {
     if (p->exec) cudaGraphExecDestroy(p->exec);
     if (p->cap) cudaStreamDestroy(p->cap);
-    cudaFree(p->d_arena);
+    if (p->d_arena) {
+        /* runs may still be in flight on any stream (cudaFree would wait for them too): wait, then return the
+         * arena to the pool in stream order */
+        cudaDeviceSynchronize();
+        cudaFreeAsync(p->d_arena, mg::abi_stream());
+    }
     delete p;
 }
 
@@ -88,27 +123,32 @@ MCGEN_API int mcgen_gb300_plan_new(const McGb300Request *reqs, int n, int tie_ru
     /* distinct worlds; each must have its device copy (tree) */
     std::map<const McWorld *, int> widx;
     std::vector<const McWorld *> worlds;
-    for (int i = 0; i < n; i++)
-        if (!widx.count(reqs[i].world)) { widx[reqs[i].world] = (int)worlds.size(); worlds.push_back(reqs[i].world); }
+    std::vector<int> wof((size_t)n); /* world index of each request */
+    for (int i = 0; i < n; i++) {
+        auto it = widx.find(reqs[i].world);
+        if (it == widx.end()) it = widx.emplace(reqs[i].world, (int)worlds.size()).first, worlds.push_back(reqs[i].world);
+        wof[(size_t)i] = it->second;
+    }
     for (auto *w : worlds) {
         int rc = mg::abi_world_device(const_cast<McWorld *>(w));
         if (rc) { free_plan(p); return rc; }
     }
     /* distinct (world, seed) -> pool slots, grouped by dimension */
     std::map<std::pair<int, int64_t>, int> slot_of;
+    std::vector<int> slot((size_t)n); /* pool slot of each request */
     std::vector<MgSetupEntry> ent[3];
     std::vector<int> first;
     long long pool = 0, ow = 0;
     for (int i = 0; i < n; i++) {
-        const int wi = widx[reqs[i].world];
-        auto key = std::make_pair(wi, (int64_t)reqs[i].seed);
-        if (slot_of.count(key)) continue;
+        const int wi = wof[(size_t)i];
+        auto ins = slot_of.emplace(std::make_pair(wi, (int64_t)reqs[i].seed), (int)pool);
+        slot[(size_t)i] = ins.first->second;
+        if (!ins.second) continue;
         const MgWorldDesc &W = worlds[(size_t)wi]->desc;
         MgSetupEntry e;
         e.seed = reqs[i].seed;
         e.world = wi;
         e.slot = (int32_t)pool;
-        slot_of[key] = (int)pool;
         if (W.dim == MG_OVERWORLD) { first.push_back((int)ow); ow += W.ntables; }
         ent[W.dim].push_back(e);
         pool += W.ntables;
@@ -131,22 +171,20 @@ MCGEN_API int mcgen_gb300_plan_new(const McGb300Request *reqs, int n, int tie_ru
      * dimension and branch; mixing them thrashes the instruction cache) and the light tiles come last */
     std::vector<int> order((size_t)n);
     for (int i = 0; i < n; i++) order[(size_t)i] = i;
-    auto weight = [&](int i) {
-        const MgWorldDesc &W = worlds[(size_t)widx[reqs[i].world]]->desc;
-        return W.dim * 2 + (W.fmode ? 1 : 0);
-    };
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        const int wa = weight(a), wb = weight(b);
-        return wa != wb ? wa < wb : widx[reqs[a].world] < widx[reqs[b].world];
-    });
+    std::vector<int> key((size_t)n); /* code path, then world */
+    for (int i = 0; i < n; i++) {
+        const MgWorldDesc &W = worlds[(size_t)wof[(size_t)i]]->desc;
+        key[(size_t)i] = (W.dim * 2 + (W.fmode ? 1 : 0)) * (int)(worlds.size() + 1) + wof[(size_t)i];
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[(size_t)a] < key[(size_t)b]; });
     for (int s = 0; s < BATCH_SHAPES; s++) {
         long long tiles = 0;
         for (int i : order) {
             const McGb300Request &r = reqs[i];
-            const int wi = widx[r.world];
+            const int wi = wof[(size_t)i];
             MgBatchReq b;
             b.world = wi;
-            b.state = slot_of[std::make_pair(wi, (int64_t)r.seed)];
+            b.state = slot[(size_t)i];
             b.qx0 = r.qx0; b.qz0 = r.qz0; b.nx = r.nx; b.nz = r.nz; b.qy = r.qy;
             b.tie = worlds[(size_t)wi]->desc.dim == MG_END ? MG_TIE_ENGINE : tie_rule;
             b.tile0 = tiles;
@@ -183,8 +221,12 @@ MCGEN_API int mcgen_gb300_plan_new(const McGb300Request *reqs, int n, int tie_ru
     for (const Part &q : parts) memcpy(host.data() + q.off, q.src, q.bytes);
     const size_t pool_off = (at + 255) & ~(size_t)255;
     const size_t counter_off = pool_off + sizeof(MgLattice) * (size_t)pool;
-    cudaError_t e = cudaMalloc(&p->d_arena, counter_off + sizeof(unsigned long long));
-    if (!e && staged) e = cudaMemcpy(p->d_arena, host.data(), staged, cudaMemcpyHostToDevice);
+    cudaMemPool_t mp = nullptr;
+    cudaStream_t ast = mg::abi_stream();
+    cudaError_t e = plan_pool(&mp);
+    if (!e) e = cudaMallocFromPoolAsync(&p->d_arena, counter_off + sizeof(unsigned long long), mp, ast);
+    if (!e && staged) e = cudaMemcpyAsync(p->d_arena, host.data(), staged, cudaMemcpyHostToDevice, ast);
+    if (!e) e = cudaStreamSynchronize(ast); /* the arena is ready for any stream */
     if (!e) {
         uint8_t *base = (uint8_t *)p->d_arena;
         for (const Part &q : parts) *q.dst = base + q.off;
@@ -290,7 +332,13 @@ MCGEN_API int mcgen_gb300_plan_run(McGb300Plan *p, uint8_t *out) {
     if (!p->nreq) return MCGEN_OK;
     uint8_t *d_out = nullptr;
     cudaStream_t st = mg::abi_stream();
-    cudaError_t e = cudaMallocAsync((void **)&d_out, (size_t)p->out_bytes, st);
+    cudaMemPool_t mp = nullptr;
+    cudaError_t e;
+    {
+        std::lock_guard<std::mutex> lk(mg::abi_lock());
+        e = plan_pool(&mp);
+    }
+    if (!e) e = cudaMallocFromPoolAsync((void **)&d_out, (size_t)p->out_bytes, mp, st);
     if (e) return cuda_rc(e);
     int rc = mcgen_gb300_plan_run_dev_direct(p, d_out, st);
     if (!rc) rc = cuda_rc(cudaMemcpyAsync(out, d_out, (size_t)p->out_bytes, cudaMemcpyDeviceToHost, st));
