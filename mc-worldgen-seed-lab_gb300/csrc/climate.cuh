@@ -20,8 +20,7 @@ __device__ __forceinline__ void climate_finish_f(const MgWorldDesc &W, const MgS
     float off = W.off_f + spline_eval(S, co);
     int lo = min(W.grad_from_y, W.grad_to_y), hi = max(W.grad_from_y, W.grad_to_y);
     int yy = by < lo ? lo : (by > hi ? hi : by);
-    float fac = (W.grad_to_f - W.grad_from_f) / (float)(W.grad_to_y - W.grad_from_y);
-    float depth = (W.grad_from_f + (float)(yy - W.grad_from_y) * fac) + off;
+    float depth = (W.grad_from_f + (float)(yy - W.grad_from_y) * W.grad_fac_f) + off;
     tg[0] = quantize(tv); tg[1] = quantize(hv); tg[2] = quantize(cv);
     tg[3] = quantize(ev); tg[4] = quantize(depth); tg[5] = quantize(rv);
 }

@@ -89,7 +89,7 @@ typedef struct {
      * < 0: a constant is not a multiple of 2^-59 below 8, and the ridge noise is not screened) */
     int64_t rf_q[3];
     int64_t rf_eq;
-    float grad_from_f, grad_to_f, off_f;
+    float grad_from_f, grad_to_f, off_f, grad_fac_f;
     float rf_f[3];
     int32_t end_ids[5];            /* the_end, end_highlands, end_midlands, small_end_islands, end_barrens */
     double end_f2, end_g2;         /* 2-D simplex skew 0.5*(sqrt(3)-1) and unskew (3-sqrt(3))/6 */

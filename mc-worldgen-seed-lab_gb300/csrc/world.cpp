@@ -593,6 +593,9 @@ int build_world(const char *root, int version, int dim, const char *preset, MgWo
             D->grad_from_f = strtof(t[4].c_str(), nullptr);
             D->grad_to_f = strtof(t[5].c_str(), nullptr);
             D->off_f = strtof(t[6].c_str(), nullptr);
+            /* the float branch's gradient slope, the same IEEE single-precision operations the reference
+             * makes per sample (GradientFunction.ClampedSampler, engine/mc_climate.h:154-160), once */
+            D->grad_fac_f = (D->grad_to_f - D->grad_from_f) / (float)(D->grad_to_y - D->grad_from_y);
             have_depth = true;
         } else if (t[0] == "offset_spline" && t.size() >= 3 && t[1] == want) {
             std::vector<std::string> tok(t.begin() + 2, t.end());
