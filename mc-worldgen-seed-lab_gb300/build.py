@@ -17,6 +17,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmcgen_gb300.so")
+# the reference library's name, for C callers that link with -lmcgen: a symbolic link to LIB (no soname is
+# set, so a program linked against either name records that name and loads it at run time)
+DROPIN = os.path.join(HERE, "libmcgen.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
@@ -38,10 +41,19 @@ def _deps() -> list[str]:
     return out + [os.path.abspath(__file__)]
 
 
+def _dropin_link() -> None:
+    if os.path.islink(DROPIN) and os.readlink(DROPIN) == os.path.basename(LIB):
+        return
+    if os.path.lexists(DROPIN):
+        os.remove(DROPIN)
+    os.symlink(os.path.basename(LIB), DROPIN)
+
+
 def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     if os.path.exists(LIB) and not ptxas_info:
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) <= t for d in _deps()):
+            _dropin_link()
             return LIB
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
@@ -68,6 +80,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         print(" ".join(cmd), file=sys.stderr)
     subprocess.check_call(cmd)
     os.replace(tmp, LIB)
+    _dropin_link()
     return LIB
 
 

@@ -25,6 +25,12 @@ struct McWorld {
     int dev_ready;
     MgTreeNode *d_tree;
     MgLattice *d_state;
+    /* identity that no other world of the process ever has (caches key on it, never on the address) */
+    uint64_t uid;
+    /* plans and pending served requests that use the world (under the ABI lock); mcgen_world_free while
+     * holds > 0 only marks it, and the last release frees it */
+    int holds;
+    int free_requested;
 };
 
 #include <cuda_runtime.h>
@@ -37,5 +43,12 @@ int abi_device();       /* the device the library runs on */
 int abi_device_ready();
 cudaStream_t abi_stream();
 int abi_world_device(McWorld *w);
+/* with abi_lock held: take / drop a reference that keeps a world (its description and device tree) alive
+ * past mcgen_world_free until the last reference is dropped */
+void abi_world_hold(McWorld *w);
+void abi_world_release(McWorld *w);
+/* a CUDA error code as the ABI reports it (MCGEN_E_NOMEM for an allocation failure, else MCGEN_E_INTERNAL;
+ * the text goes to mcgen_gb300_last_error), MCGEN_OK for cudaSuccess */
+int abi_cuda_code(int e);
 }  // namespace mg
 #endif

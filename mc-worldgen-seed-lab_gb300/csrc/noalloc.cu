@@ -41,12 +41,15 @@ extern "C" MCGEN_API int mcgen_gb300_seed_points_noalloc(const McWorld *w, const
     if (dev != mg::abi_device()) return MCGEN_E_ARG; /* the world's data lives on the library's device */
     if (!g_seed_scratch_addr[dev]) {
         void *p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_seed_scratch) != cudaSuccess || !p) return MCGEN_E_INTERNAL;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_seed_scratch);
+        if (e != cudaSuccess) return mg::abi_cuda_code((int)e);
+        if (!p) return MCGEN_E_INTERNAL;
         g_seed_scratch_addr[dev] = p;
     }
     MgLattice *states = (MgLattice *)g_seed_scratch_addr[dev];
     cudaStream_t st = (cudaStream_t)stream;
     int rc = mg::launch_setup(w->desc, d_seeds, ns, states, st);
     if (!rc) rc = mg::launch_points(w->desc, w->d_tree, states, ns, d_qxyz, np, d_out, d_targets, st);
-    return rc ? MCGEN_E_INTERNAL : MCGEN_OK;
+    /* a launch error is reported as mcgen_gb300_seed_points_dev reports it */
+    return mg::abi_cuda_code(rc);
 }

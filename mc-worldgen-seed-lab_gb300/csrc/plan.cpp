@@ -45,6 +45,11 @@ struct McGb300Plan {
     cudaGraphExec_t exec = nullptr;
     uint8_t *graph_out = nullptr;
     int graph_shape = -1;
+    /* completion of the latest run: runs share the lattice pool and the tile counter, so each run waits for
+     * the previous one whatever stream it is on, and freeing the plan waits for the last in stream order */
+    cudaEvent_t last_run = nullptr;
+    bool ran = false;
+    std::vector<McWorld *> held; /* worlds kept alive while the plan exists */
 };
 
 namespace {
@@ -91,15 +96,29 @@ int enqueue(McGb300Plan *p, uint8_t *d_out, int shape, cudaStream_t st) {
                             p->d_counter, d_out, p->ctas, shape, st);
 }
 
+/* Order a run on `st` after the plan's previous run (on any stream); caller holds the ABI lock. */
+int run_begin(McGb300Plan *p, cudaStream_t st) {
+    if (!p->ran) return MCGEN_OK;
+    return cuda_rc(cudaStreamWaitEvent(st, p->last_run, 0));
+}
+int run_end(McGb300Plan *p, cudaStream_t st) {
+    cudaError_t e = cudaEventRecord(p->last_run, st);
+    if (!e) p->ran = true;
+    return cuda_rc(e);
+}
+
+/* Caller holds the ABI lock.  Nothing here blocks the host: a graph or stream still in use is released by
+ * the driver when its work completes, and the arena returns to the pool after the last run. */
 void free_plan(McGb300Plan *p) {
     if (p->exec) cudaGraphExecDestroy(p->exec);
     if (p->cap) cudaStreamDestroy(p->cap);
     if (p->d_arena) {
-        /* runs may still be in flight on any stream (cudaFree would wait for them too): wait, then return the
-         * arena to the pool in stream order */
-        cudaDeviceSynchronize();
-        cudaFreeAsync(p->d_arena, mg::abi_stream());
+        cudaStream_t ast = mg::abi_stream();
+        if (p->ran) cudaStreamWaitEvent(ast, p->last_run, 0);
+        cudaFreeAsync(p->d_arena, ast);
     }
+    if (p->last_run) cudaEventDestroy(p->last_run);
+    for (McWorld *w : p->held) mg::abi_world_release(w);
     delete p;
 }
 
@@ -132,6 +151,13 @@ MCGEN_API int mcgen_gb300_plan_new(const McGb300Request *reqs, int n, int tie_ru
     for (auto *w : worlds) {
         int rc = mg::abi_world_device(const_cast<McWorld *>(w));
         if (rc) { free_plan(p); return rc; }
+        mg::abi_world_hold(const_cast<McWorld *>(w));
+        p->held.push_back(const_cast<McWorld *>(w));
+    }
+    if (cudaError_t ee = cudaEventCreateWithFlags(&p->last_run, cudaEventDisableTiming)) {
+        p->last_run = nullptr;
+        free_plan(p);
+        return cuda_rc(ee);
     }
     /* distinct (world, seed) -> pool slots, grouped by dimension */
     std::map<std::pair<int, int64_t>, int> slot_of;
@@ -283,15 +309,21 @@ MCGEN_API int mcgen_gb300_plan_run_dev(McGb300Plan *p, uint8_t *d_out, void *str
         p->graph_out = d_out;
         p->graph_shape = p->shape;
     }
-    return cuda_rc(cudaGraphLaunch(p->exec, st));
+    int rc = run_begin(p, st);
+    if (!rc) rc = cuda_rc(cudaGraphLaunch(p->exec, st));
+    if (!rc) rc = run_end(p, st);
+    return rc;
 }
 
 /* The same without a graph (each launch visible to the library's per-kernel profiler). */
 MCGEN_API int mcgen_gb300_plan_run_dev_direct(McGb300Plan *p, uint8_t *d_out, void *stream) {
     if (!p || (!d_out && p->out_bytes)) return MCGEN_E_ARG;
     std::lock_guard<std::mutex> lk(mg::abi_lock());
-    int rc = enqueue(p, d_out, p->shape, (cudaStream_t)stream);
-    return rc ? MCGEN_E_INTERNAL : MCGEN_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = run_begin(p, st);
+    if (rc) return rc;
+    if (enqueue(p, d_out, p->shape, st)) return MCGEN_E_INTERNAL;
+    return run_end(p, st);
 }
 
 /* Time every tile shape on the plan itself (reps runs each, after one warm-up) and keep the fastest.
@@ -305,7 +337,7 @@ MCGEN_API int mcgen_gb300_plan_autotune(McGb300Plan *p, uint8_t *d_out, int reps
     cudaEventCreate(&a);
     cudaEventCreate(&b);
     double best = 1e30;
-    int best_s = 0, rc = 0;
+    int best_s = 0, rc = run_begin(p, st);
     for (int s = 0; s < BATCH_SHAPES && !rc; s++) {
         rc = enqueue(p, d_out, s, st);
         cudaEventRecord(a, st);
@@ -316,6 +348,7 @@ MCGEN_API int mcgen_gb300_plan_autotune(McGb300Plan *p, uint8_t *d_out, int reps
         cudaEventElapsedTime(&ms, a, b);
         if (!rc && ms / reps < best) { best = ms / reps; best_s = s; }
     }
+    if (!rc) rc = run_end(p, st);
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     cudaStreamDestroy(st);

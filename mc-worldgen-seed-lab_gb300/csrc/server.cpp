@@ -9,8 +9,15 @@
  * every request its ids and wakes its waiters.
  *
  * Noise-state cache: per dimension a pool of fixed-size slots (46 lattices of 352 B for the Overworld, 8 for
- * the Nether, 1 for the End) carved from one HBM budget, keyed by (world, seed), evicted least recently
- * used among slots that no in-flight batch references.
+ * the Nether, 1 for the End) carved from one HBM budget, keyed by (world identity, seed) -- the world's
+ * process-unique id, never its address, which the heap may give to a later world -- and evicted least
+ * recently used among slots that no in-flight batch references.
+ *
+ * Failures: a batch that fails before its work is queued (an allocation, a copy or a launch) takes back the
+ * cache entries it had created, so no later request can hit lattices that were never built, and fails its
+ * own requests; an allocation failure leaves the server usable, any other error stops it: every pending
+ * and later request then fails with that error.  A pending request holds its world, so mcgen_world_free
+ * during serving defers the free until the request completes.
  */
 #include <cuda_runtime.h>
 #include <string.h>
@@ -35,15 +42,17 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+using Key = std::pair<uint64_t, int64_t>; /* (world uid, seed) */
+
 struct Pool { /* one dimension's slots */
     int lattices_per_slot = 0;
     int nslots = 0;
     MgLattice *base = nullptr;
     std::vector<int> free_slots;
-    std::list<std::pair<const McWorld *, int64_t>> lru; /* front = most recent */
+    std::list<Key> lru; /* front = most recent */
     /* builder: the batch slot whose setup launch is still filling this entry, -1 once it is complete */
-    struct Entry { int slot; int refs; int builder; std::list<std::pair<const McWorld *, int64_t>>::iterator it; };
-    std::map<std::pair<const McWorld *, int64_t>, Entry> map;
+    struct Entry { int slot; int refs; int builder; std::list<Key>::iterator it; };
+    std::map<Key, Entry> map;
 };
 
 struct Ticket {
@@ -60,7 +69,7 @@ struct Batch {
     cudaEvent_t setup_done = nullptr; /* after this batch's setup launches */
     bool busy = false;
     std::vector<long long> tickets;
-    std::vector<std::pair<int, std::pair<const McWorld *, int64_t>>> held; /* (dim, key) references */
+    std::vector<std::pair<int, Key>> held; /* (dim, key) references */
     /* device and pinned staging, grown as needed */
     MgBatchReq *d_reqs = nullptr; size_t cap_reqs = 0;
     MgSetupEntry *d_ent = nullptr; size_t cap_ent = 0;
@@ -88,6 +97,7 @@ struct McGb300Server {
     long long next_ticket = 1;
     McGb300ServerStats stats;
     int fatal = 0;
+    int fail_next = 0; /* testing aid: the next batch's allocation step fails with this code */
 };
 
 namespace {
@@ -111,8 +121,7 @@ cudaError_t grow_dev(T **p, size_t *cap, size_t n) {
 
 /* Reserve a cache slot for key in pool P (caller holds the server lock); -1 if every slot is in use.
  * *builder: the batch still building a hit entry (-1 when complete); a miss is built by batch `me`. */
-int cache_acquire(McGb300Server *s, Pool &P, const std::pair<const McWorld *, int64_t> &key, int me, bool *miss,
-                  int *builder) {
+int cache_acquire(McGb300Server *s, Pool &P, const Key &key, int me, bool *miss, int *builder) {
     auto it = P.map.find(key);
     if (it != P.map.end()) {
         it->second.refs++;
@@ -148,11 +157,33 @@ int cache_acquire(McGb300Server *s, Pool &P, const std::pair<const McWorld *, in
     s->stats.cache_misses++;
     return slot;
 }
-void cache_release(Pool &P, const std::pair<const McWorld *, int64_t> &key, int me) {
+void cache_release(Pool &P, const Key &key, int me) {
     auto it = P.map.find(key);
     if (it == P.map.end()) return;
     if (it->second.refs > 0) it->second.refs--;
     if (it->second.builder == me) it->second.builder = -1; /* its batch has completed */
+}
+/* A batch that failed before its work was queued: entries it created were never built, so they leave the
+ * cache (their slots return to the free list); other entries just lose this batch's references.  No other
+ * batch can reference an entry this batch created: batches form one at a time under the server lock. */
+void cache_rollback(Pool &P, const Key &key, int me) {
+    auto it = P.map.find(key);
+    if (it == P.map.end()) return;
+    if (it->second.refs > 0) it->second.refs--;
+    if (it->second.builder == me) {
+        P.free_slots.push_back(it->second.slot);
+        P.lru.erase(it->second.it);
+        P.map.erase(it);
+    }
+}
+
+/* A request has completed or failed: record it and let go of its world (caller holds the server lock and
+ * the ABI lock). */
+void ticket_done(Ticket &T, int err, Clock::time_point now) {
+    T.state = err ? 3 : 2;
+    T.err = err;
+    T.t_done = now;
+    mg::abi_world_release(const_cast<McWorld *>(T.req.world));
 }
 
 /* Form and launch one batch from pending requests on batch slot b (server lock held). */
@@ -173,13 +204,12 @@ int launch_batch(McGb300Server *s, Batch &b) {
         Ticket &T = s->tickets[id];
         const McWorld *w = T.req.world;
         const int dim = w->desc.dim;
-        auto key = std::make_pair(w, (int64_t)T.req.seed);
+        const Key key = std::make_pair(w->uid, (int64_t)T.req.seed);
         Pool &P = s->pool[dim];
         if (w->desc.ntables > P.lattices_per_slot) { /* cannot happen with the shipped tables */
             s->pending.pop_front();
-            T.state = 3;
-            T.err = MCGEN_E_DATA;
-            T.t_done = Clock::now();
+            ticket_done(T, MCGEN_E_DATA, Clock::now());
+            s->cv_done.notify_all();
             continue;
         }
         bool miss = false;
@@ -249,6 +279,11 @@ int launch_batch(McGb300Server *s, Batch &b) {
     }
     if (!e && !b.d_counter) e = cudaMalloc(&b.d_counter, sizeof(unsigned long long));
     if (e) return crc(e);
+    if (s->fail_next) { /* injected failure of this step (tests of the failure path) */
+        const int f = s->fail_next;
+        s->fail_next = 0;
+        return f;
+    }
     /* small host->device copies of this batch's descriptors (pageable sources: staged by the driver) */
     cudaStream_t st = b.st;
     e = cudaMemcpyAsync(b.d_worlds, wd.data(), sizeof(MgWorldDesc) * wd.size(), cudaMemcpyHostToDevice, st);
@@ -284,24 +319,39 @@ int launch_batch(McGb300Server *s, Batch &b) {
     return 0;
 }
 
-/* Hand a finished batch's ids to its requests (server lock held). */
-void finish_batch(McGb300Server *s, Batch &b, int err) {
+/* Hand a finished batch's ids to its requests (server lock held).  launched: the batch's work was queued
+ * (false: it failed while forming, and the cache entries it created are taken back). */
+void finish_batch(McGb300Server *s, Batch &b, int err, bool launched) {
     const auto now = Clock::now();
+    std::lock_guard<std::mutex> glk(mg::abi_lock());
     for (size_t i = 0; i < b.tickets.size(); i++) {
         auto it = s->tickets.find(b.tickets[i]);
         if (it == s->tickets.end()) continue;
         Ticket &T = it->second;
         if (!err && T.out) memcpy(T.out, b.h_out + b.out_off[i], (size_t)T.req.nx * (size_t)T.req.nz);
-        T.state = err ? 3 : 2;
-        T.err = err;
-        T.t_done = now;
-        s->stats.samples_done += (long long)T.req.nx * T.req.nz;
+        ticket_done(T, err, now);
+        if (!err) s->stats.samples_done += (long long)T.req.nx * T.req.nz;
     }
     const int me = (int)(&b - s->batches.data());
-    for (auto &h : b.held) cache_release(s->pool[h.first], h.second, me);
+    for (auto &h : b.held) {
+        if (launched && !err) cache_release(s->pool[h.first], h.second, me);
+        else cache_rollback(s->pool[h.first], h.second, me);
+    }
     b.tickets.clear();
     b.held.clear();
     b.busy = false;
+    s->cv_done.notify_all();
+}
+
+/* After an error that stops the server: every pending request fails with it (server lock held). */
+void fail_pending(McGb300Server *s) {
+    const auto now = Clock::now();
+    std::lock_guard<std::mutex> glk(mg::abi_lock());
+    while (!s->pending.empty()) {
+        auto it = s->tickets.find(s->pending.front());
+        s->pending.pop_front();
+        if (it != s->tickets.end()) ticket_done(it->second, s->fatal, now);
+    }
     s->cv_done.notify_all();
 }
 
@@ -314,17 +364,28 @@ void worker_loop(McGb300Server *s) {
             if (!b.busy) continue;
             cudaError_t q = cudaEventQuery(b.done);
             if (q == cudaErrorNotReady) continue;
-            finish_batch(s, b, q == cudaSuccess ? 0 : MCGEN_E_INTERNAL);
+            if (q != cudaSuccess && !s->fatal) s->fatal = MCGEN_E_INTERNAL; /* the device failed the batch */
+            finish_batch(s, b, q == cudaSuccess ? 0 : MCGEN_E_INTERNAL, true);
+            progressed = true;
+        }
+        if (s->fatal && !s->pending.empty()) {
+            fail_pending(s);
             progressed = true;
         }
         /* admissions: every free stream takes the pending requests */
         for (auto &b : s->batches) {
-            if (b.busy || s->pending.empty()) continue;
-            std::lock_guard<std::mutex> glk(mg::abi_lock());
-            int rc = launch_batch(s, b);
-            if (rc) { /* fail the requests of this batch loudly */
-                finish_batch(s, b, rc);
-                s->fatal = rc;
+            if (b.busy || s->pending.empty() || s->fatal) continue;
+            int rc;
+            {
+                std::lock_guard<std::mutex> glk(mg::abi_lock());
+                rc = launch_batch(s, b);
+            }
+            if (rc) { /* fail the requests of this batch loudly; its cache entries are taken back */
+                finish_batch(s, b, rc, false);
+                if (rc != MCGEN_E_NOMEM) {
+                    s->fatal = rc;
+                    fail_pending(s);
+                }
                 progressed = true;
             } else if (b.busy) {
                 progressed = true;
@@ -433,13 +494,19 @@ MCGEN_API int mcgen_gb300_server_submit(McGb300Server *s, const McGb300Request *
         (long long)req->nx * req->nz > (1LL << 28))
         return MCGEN_E_ARG;
     {
-        /* the world's tree must be on the device before the worker references it */
+        /* the world's tree must be on the device before the worker references it, and the world stays alive
+         * until the request completes */
         std::lock_guard<std::mutex> glk(mg::abi_lock());
         int rc = mg::abi_world_device(const_cast<McWorld *>(req->world));
         if (rc) return rc;
+        mg::abi_world_hold(const_cast<McWorld *>(req->world));
     }
     std::lock_guard<std::mutex> lk(s->m);
-    if (s->fatal) return s->fatal;
+    if (s->fatal) {
+        std::lock_guard<std::mutex> glk(mg::abi_lock());
+        mg::abi_world_release(const_cast<McWorld *>(req->world));
+        return s->fatal;
+    }
     const long long id = s->next_ticket++;
     Ticket &T = s->tickets[id];
     T.req = *req;
@@ -465,6 +532,13 @@ MCGEN_API int mcgen_gb300_server_wait(McGb300Server *s, long long ticket, int ti
     const int err = T.state == 3 ? (T.err ? T.err : MCGEN_E_INTERNAL) : MCGEN_OK;
     s->tickets.erase(it);
     return err;
+}
+
+MCGEN_API int mcgen_gb300_server_fail_next(McGb300Server *s, int code) {
+    if (!s || code <= 0) return MCGEN_E_ARG;
+    std::lock_guard<std::mutex> lk(s->m);
+    s->fail_next = code;
+    return MCGEN_OK;
 }
 
 MCGEN_API int mcgen_gb300_server_stats(McGb300Server *s, McGb300ServerStats *out) {

@@ -40,6 +40,28 @@ def test_exports_every_declared_symbol(mg):
     assert not missing, missing
 
 
+def test_links_as_libmcgen(mg, tmp_path):
+    """A C caller of the reference library links with -lmcgen unchanged: build.py provides libmcgen.so,
+    and a program built against include/mcgen.h alone runs against it (host calls only, no device)."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    src = tmp_path / "caller.c"
+    src.write_text('#include <stdio.h>\n#include "mcgen.h"\n'
+                   'int main(void) { printf("%d %s\\n", mcgen_abi_version(), mcgen_version()); return 0; }\n')
+    lib_dir = os.path.dirname(mg.LIB_PATH)
+    assert os.path.exists(os.path.join(lib_dir, "libmcgen.so"))
+    exe = tmp_path / "caller"
+    subprocess.run([cc, str(src), "-I", os.path.join(REPO, "include"), "-L", lib_dir, "-lmcgen", "-o", str(exe)],
+                   check=True, capture_output=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, env={**os.environ, "LD_LIBRARY_PATH": lib_dir})
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.startswith("1 ") and "abi 1" in r.stdout
+
+
 def test_version(mg):
     L = mg.load()
     assert L.mcgen_abi_version() == 1

@@ -127,3 +127,29 @@ def test_batch_presets_versions_extremes(env):
             else:
                 exp = ow.quart_grid(s, qx0, qz0, nx, nz, qy, O.TIE_ENGINE)
             assert np.array_equal(got, exp), (k, s, qx0, qz0, nx, nz, rule)
+
+
+def test_plan_outlives_freed_world_and_orders_runs(env):
+    """A plan keeps its worlds alive past mcgen_world_free; runs of one plan on two streams with no ordering
+    between them are serialised by the library (they share the plan's lattice pool and tile counter), so
+    both outputs are exact; freeing the plan right after queuing runs does not block and leaves them exact."""
+    torch = pytest.importorskip("torch")
+    mg, gens, worlds = env
+    dev = torch.device("cuda", 0)
+    w = gens["26.2"].world("minecraft:overworld", "normal", 0)
+    reqs = [(w, 9000 + i, -300 + 37 * i, 200 - 11 * i, 50 + 7 * i, 33, 16) for i in range(12)]
+    plan = mg.Plan(reqs)
+    w.close()  # the plan still uses the world's description and tree
+    ow = O.World(ge.data_root(), "26.2", "overworld")
+    exp = np.concatenate([ow.quart_grid(s, qx0, qz0, nx, nz, qy, O.TIE_ENGINE).ravel()
+                          for _, s, qx0, qz0, nx, nz, qy in reqs])
+    a, b = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    oa = torch.zeros(plan.output_bytes, dtype=torch.uint8, device=dev)
+    ob = torch.zeros_like(oa)
+    for _ in range(3):
+        plan.run_dev(oa.data_ptr(), a.cuda_stream)
+        plan.run_dev(ob.data_ptr(), b.cuda_stream, graph=False)
+    plan.close()
+    torch.cuda.synchronize(dev)
+    assert np.array_equal(oa.cpu().numpy(), exp)
+    assert np.array_equal(ob.cpu().numpy(), exp)

@@ -119,3 +119,60 @@ def test_wait_timeout_and_ticket_rules(env):
     t = C.c_longlong()
     assert L.mcgen_gb300_server_submit(srv._h, C.byref(req), None, C.byref(t)) == mg.MCGEN_E_ARG
     srv.close()
+
+
+def test_failed_batch_leaves_no_partial_state(env):
+    """A batch that fails while forming (an allocation failure injected on the host) fails its own requests
+    and takes back the cache entries it had created: the same seeds asked again are rebuilt and exact, and no
+    request ever comes back MCGEN_OK with wrong ids.  A failure other than an allocation stops the server:
+    pending and later requests fail with it."""
+    mg, gens, worlds = env
+    w = worlds[("26.3", "minecraft:overworld")]
+    ow = O.World(ge.data_root(), "26.3", "overworld")
+    srv = mg.Server(hbm_budget_bytes=64 << 20, max_inflight=1)
+    seeds = [1111, -2222, 3333, 4444]
+    exp = {s: ow.quart_grid(s, -20, 12, 16, 16, 16, O.TIE_ENGINE) for s in seeds}
+    srv.fail_next(mg.MCGEN_E_NOMEM)
+    tickets = [(s, srv.submit(w, s, -20, 12, 16, 16, 16)) for s in seeds]
+    failed = 0
+    for s, t in tickets:
+        try:
+            ids, _ = srv.wait(t)
+        except mg.McError as e:
+            assert e.code == mg.MCGEN_E_NOMEM
+            failed += 1
+            continue
+        assert np.array_equal(ids, exp[s])
+    assert failed >= 1
+    for s in seeds:  # hits would read lattices that were never built if the entries had stayed
+        ids, _ = srv.wait(srv.submit(w, s, -20, 12, 16, 16, 16))
+        assert np.array_equal(ids, exp[s])
+    srv.fail_next(mg.MCGEN_E_INTERNAL)
+    with pytest.raises(mg.McError) as e:
+        srv.wait(srv.submit(w, seeds[0], -20, 12, 16, 16, 16))
+    assert e.value.code == mg.MCGEN_E_INTERNAL
+    with pytest.raises(mg.McError) as e:
+        srv.submit(w, seeds[1], -20, 12, 16, 16, 16)
+    assert e.value.code == mg.MCGEN_E_INTERNAL
+    srv.close()
+
+
+def test_world_freed_while_served(env):
+    """A world freed while its requests are pending stays alive until they complete; the cache is keyed by
+    the world's identity, so a new world (possibly at the same address) never hits the old one's lattices."""
+    mg, gens, worlds = env
+    srv = mg.Server(hbm_budget_bytes=64 << 20, max_inflight=2)
+    w = gens["26.1"].world("minecraft:overworld", "normal", 0)
+    t = [srv.submit(w, 77 + i, 100, -50, 40, 40, 16) for i in range(6)]
+    w.close()
+    ow = O.World(ge.data_root(), "26.1", "overworld")
+    for i, tk in enumerate(t):
+        ids, _ = srv.wait(tk)
+        assert np.array_equal(ids, ow.quart_grid(77 + i, 100, -50, 40, 40, 16, O.TIE_ENGINE))
+    # a world of another preset with the same seeds: its own lattices and tree, not the freed world's
+    w2 = gens["26.1"].world("minecraft:overworld", "large_biomes", 0)
+    lb = O.World(ge.data_root(), "26.1", "overworld", "large_biomes")
+    for i in range(3):
+        ids, _ = srv.wait(srv.submit(w2, 77 + i, 100, -50, 40, 40, 16))
+        assert np.array_equal(ids, lb.quart_grid(77 + i, 100, -50, 40, 40, 16, O.TIE_ENGINE))
+    srv.close()

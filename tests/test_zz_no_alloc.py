@@ -13,6 +13,7 @@ import numpy as np
 import pytest
 
 import __graft_entry__ as ge
+from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
@@ -21,8 +22,9 @@ def _call(mg, w, d_seeds, ns, d_pts, np_, d_out, d_tg, stream):
     return mg.load().mcgen_gb300_seed_points_noalloc(w.handle, d_seeds, ns, d_pts, np_, d_out, d_tg, stream)
 
 
-# 16 MiB // (lattices per seed x 352-byte lattice): 46 Overworld, 8 Nether lattices per seed
-@pytest.mark.parametrize("dim,max_seeds", [("minecraft:overworld", 1036), ("minecraft:the_nether", 5957)])
+# 16 MiB // (lattices per seed x 352-byte lattice): 46 Overworld, 8 Nether, 1 End lattice per seed
+@pytest.mark.parametrize("dim,max_seeds", [("minecraft:overworld", 1036), ("minecraft:the_nether", 5957),
+                                           ("minecraft:the_end", 47662)])
 def test_noalloc_matches_allocating_entry(dim, max_seeds):
     torch = pytest.importorskip("torch")
     mg = ge.package()
@@ -50,8 +52,15 @@ def test_noalloc_matches_allocating_entry(dim, max_seeds):
                    stream.cuda_stream)
         assert rc == mg.MCGEN_OK
         torch.cuda.synchronize(dev)
-        assert np.array_equal(d_out.cpu().numpy().reshape(ns, len(pts)), exp)
-        assert np.array_equal(d_tg.cpu().numpy().reshape(ns, len(pts), 6), exp_tg)
+        got = d_out.cpu().numpy().reshape(ns, len(pts))
+        got_tg = d_tg.cpu().numpy().reshape(ns, len(pts), 6)
+        assert np.array_equal(got, exp)
+        assert np.array_equal(got_tg, exp_tg)
+        # and the oracle on a stride sample of the seeds (about 64 of them)
+        pick = np.arange(0, ns, max(1, ns // 64))
+        ora, ora_tg = O.World(ge.data_root(), "26.3", dim.split(":")[1]).points(seeds[pick], pts, want_targets=True)
+        assert np.array_equal(got[pick], ora)
+        assert np.array_equal(got_tg[pick], ora_tg)
     # one seed more than the fixed scratch holds is refused, and nothing is written
     big = torch.zeros(max_seeds + 1, dtype=torch.int64, device=dev)
     d_out = torch.full(((max_seeds + 1) * len(pts),), 0xEE, dtype=torch.uint8, device=dev)
