@@ -46,6 +46,14 @@ MCGEN_API int mcgen_gb300_quart_grid(const McWorld *w, int qx0, int qz0, int nx,
 MCGEN_API int mcgen_gb300_seed_points(const McWorld *w, const int64_t *seeds, int ns, const int32_t *qxyz, int np,
                                       uint8_t *out, int32_t *targets);
 
+/* Overworld density functions at block points for `seed` (the world supplies version and preset):
+ * out[5i + k] for point xyz[3i..3i+2] = continents, erosion, ridges, offset, depth -- the values the climate
+ * sampler computes before it rounds them to floats for the biome search (double branch 26.1/26.2: the exact
+ * doubles; float branch: the floats, widened).  The reference computes them in its Java oracle ("df",
+ * oracle/gen_vectors.py:76-84; tests/vectors/<V>/df.tsv) and inside engine/mc_climate.h:113-164 at block
+ * coordinates.  MCGEN_E_ARG for Nether and End worlds. */
+MCGEN_API int mcgen_gb300_density_values(const McWorld *w, int64_t seed, int n, const int32_t *xyz, double *out);
+
 /* Device-pointer forms: every pointer is CUDA device memory, work is queued on `stream`
  * (a cudaStream_t, NULL = the legacy default stream) and the call returns without synchronising. */
 MCGEN_API int mcgen_gb300_seed_points_dev(const McWorld *w, const int64_t *d_seeds, int ns, const int32_t *d_qxyz,
@@ -73,6 +81,8 @@ typedef struct McGb300Request {
     int32_t qx0, qz0, nx, nz, qy;
 } McGb300Request;
 typedef struct McGb300Plan McGb300Plan;
+/* A plan keeps each of its worlds alive until mcgen_gb300_plan_free: mcgen_world_free on such a world only
+ * marks it, and the plan's free releases it (the plan reads the world's description and device tree). */
 MCGEN_API int mcgen_gb300_plan_new(const McGb300Request *reqs, int n, int tie_rule, McGb300Plan **out);
 MCGEN_API void mcgen_gb300_plan_free(McGb300Plan *p);
 MCGEN_API long long mcgen_gb300_plan_output_bytes(const McGb300Plan *p);
@@ -86,7 +96,10 @@ MCGEN_API long long mcgen_gb300_plan_h2d_bytes(const McGb300Plan *p);
 /* time the four tile shapes on this plan (reps runs each into d_out) and keep the fastest */
 MCGEN_API int mcgen_gb300_plan_autotune(McGb300Plan *p, uint8_t *d_out, int reps, double *best_ms);
 /* run into device memory on `stream` (graph replay) / without a graph / into host memory (direct launches,
- * outputs copied back, synchronous) */
+ * outputs copied back, synchronous).  Runs of one plan share its lattice pool and tile counter, so each run
+ * is ordered after the plan's previous run on the GPU (the library makes `stream` wait for it); runs of
+ * different plans are independent.  mcgen_gb300_plan_free does not block: the plan's device memory returns
+ * to the library's pool after its last run. */
 MCGEN_API int mcgen_gb300_plan_run_dev(McGb300Plan *p, uint8_t *d_out, void *stream);
 MCGEN_API int mcgen_gb300_plan_run_dev_direct(McGb300Plan *p, uint8_t *d_out, void *stream);
 MCGEN_API int mcgen_gb300_plan_run(McGb300Plan *p, uint8_t *out);
@@ -109,9 +122,16 @@ MCGEN_API int mcgen_gb300_server_new(long long hbm_budget_bytes, int max_infligh
 MCGEN_API void mcgen_gb300_server_free(McGb300Server *s); /* drains pending work first */
 MCGEN_API int mcgen_gb300_server_submit(McGb300Server *s, const McGb300Request *req, uint8_t *out, long long *ticket);
 /* wait for a ticket (timeout_ms < 0: no limit; MCGEN_E_CANCEL on timeout, the ticket stays valid);
- * latency_ms: submit to completion.  A ticket can be waited for once. */
+ * latency_ms: submit to completion.  A ticket can be waited for once.
+ * Errors: a batch that fails while forming (allocation, copy, launch) fails its requests with that error and
+ * leaves no partly built noise state in the cache; after an allocation failure (MCGEN_E_NOMEM) the server
+ * goes on serving, after any other error every pending and later request fails with it.  A submitted
+ * request keeps its world alive until it completes (mcgen_world_free meanwhile only marks the world). */
 MCGEN_API int mcgen_gb300_server_wait(McGb300Server *s, long long ticket, int timeout_ms, double *latency_ms);
 MCGEN_API int mcgen_gb300_server_stats(McGb300Server *s, McGb300ServerStats *out);
+/* Testing aid: the next batch the server forms fails at its device-allocation step with `code` (> 0), as if
+ * that allocation had failed; host-side only, no device fault. */
+MCGEN_API int mcgen_gb300_server_fail_next(McGb300Server *s, int code);
 
 /* ---- biome seed search: which candidate seeds produce the observed biomes ----
  * The reference's gb_search (crack/src/gpu_biomes/gpu_biomes.h:44-56, gpu_biomes.cu:245-278).  Candidates:

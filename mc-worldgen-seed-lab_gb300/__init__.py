@@ -125,6 +125,8 @@ _PROTOS.update({
     "mcgen_gb300_server_submit": (C.c_int, [_P, _P, _P, C.POINTER(C.c_longlong)]),
     "mcgen_gb300_server_wait": (C.c_int, [_P, C.c_longlong, C.c_int, C.POINTER(C.c_double)]),
     "mcgen_gb300_server_stats": (C.c_int, [_P, _P]),
+    "mcgen_gb300_server_fail_next": (C.c_int, [_P, C.c_int]),
+    "mcgen_gb300_density_values": (C.c_int, [_P, C.c_int64, C.c_int, _P, _P]),
     "mcgen_gb300_seed_points_noalloc": (C.c_int, [_P, _P, C.c_int, _P, C.c_int, _P, _P, _P]),
 })
 
@@ -424,6 +426,14 @@ class World:
                "mcgen_gb300_quart_grid")
         return out
 
+    def density(self, seed: int, xyz) -> np.ndarray:
+        """Overworld density functions at block points: [n, 5] continents, erosion, ridges, offset, depth."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.int32).reshape(-1, 3)
+        out = np.empty((len(xyz), 5), np.float64)
+        _check(load().mcgen_gb300_density_values(self._h, int(seed), len(xyz), _ptr(xyz), _ptr(out)),
+               "mcgen_gb300_density_values")
+        return out
+
     def seed_points(self, seeds, qxyz, want_targets: bool = False):
         seeds = np.ascontiguousarray(seeds, dtype=np.int64)
         qxyz = np.ascontiguousarray(qxyz, dtype=np.int32).reshape(-1, 3)
@@ -639,6 +649,10 @@ class Server:
         lat = C.c_double()
         _check(load().mcgen_gb300_server_wait(self._h, ticket, timeout_ms, C.byref(lat)), "mcgen_gb300_server_wait")
         return self._keep.pop(ticket), lat.value
+
+    def fail_next(self, code: int) -> None:
+        """Testing aid: the next batch fails at its allocation step with `code` (host-side injection)."""
+        _check(load().mcgen_gb300_server_fail_next(self._h, code), "mcgen_gb300_server_fail_next")
 
     def stats(self) -> dict:
         st = McGb300ServerStats()

@@ -11,6 +11,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -111,6 +112,15 @@ int world_device_locked(McWorld *w) {
     return MCGEN_OK;
 }
 
+/* cudaFree waits for the device work that may still read the tree */
+void world_destroy_locked(McWorld *w) {
+    if (w->d_tree) cudaFree(w->d_tree);
+    if (w->d_state) cudaFree(w->d_state);
+    delete w;
+}
+
+std::atomic<uint64_t> g_world_uid{1};
+
 int dim_of(const char *d) {
     if (!d) return -1;
     if (!strcmp(d, "minecraft:overworld") || !strcmp(d, "overworld")) return MG_OVERWORLD;
@@ -169,6 +179,12 @@ int abi_device() { return g_device; }
 int abi_device_ready() { return device_ready_locked(); }
 cudaStream_t abi_stream() { return g_stream; }
 int abi_world_device(McWorld *w) { return world_device_locked(w); }
+int abi_cuda_code(int e) { return cuda_code((cudaError_t)e); }
+void abi_world_hold(McWorld *w) { w->holds++; }
+void abi_world_release(McWorld *w) {
+    if (w->holds > 0) w->holds--;
+    if (w->holds == 0 && w->free_requested) world_destroy_locked(w);
+}
 }  // namespace mg
 
 /* ============================================================================ version, data */
@@ -241,6 +257,7 @@ MCGEN_API int mcgen_world_new(McGen *g, const char *dimension, const char *prese
     w->preset = pn;
     w->seeds = *seeds;
     w->zoom_seed = mg::obfuscate_seed(seeds->climate);
+    w->uid = g_world_uid.fetch_add(1);
     std::string e;
     int rc = mg::build_world(g->root.c_str(), g->version, d, pn.c_str(), &w->desc, &w->tree, &e);
     if (rc) {
@@ -251,14 +268,16 @@ MCGEN_API int mcgen_world_new(McGen *g, const char *dimension, const char *prese
     *out = w;
     return MCGEN_OK;
 }
+/* A world that a plan or a pending served request still uses is freed when the last of them lets go
+ * (mg::abi_world_release); its handle is invalid for the caller from this call on either way. */
 MCGEN_API void mcgen_world_free(McWorld *w) {
     if (!w) return;
-    {
-        std::lock_guard<std::mutex> lk(g_lock);
-        if (w->d_tree) cudaFree(w->d_tree);
-        if (w->d_state) cudaFree(w->d_state);
+    std::lock_guard<std::mutex> lk(g_lock);
+    if (w->holds > 0) {
+        w->free_requested = 1;
+        return;
     }
-    delete w;
+    world_destroy_locked(w);
 }
 MCGEN_API int mcgen_world_set_schedule(McWorld *w, const char *path, char *err, size_t errlen) {
     (void)w; (void)path;
@@ -519,6 +538,34 @@ MCGEN_API int mcgen_gb300_seed_points(const McWorld *w, const int64_t *seeds, in
     if ((e = cudaMemcpyAsync(out, d_out.p, n, cudaMemcpyDeviceToHost, g_stream))) return cuda_code(e);
     if (targets && (e = cudaMemcpyAsync(targets, d_tg.p, sizeof(int32_t) * 6 * n, cudaMemcpyDeviceToHost, g_stream)))
         return cuda_code(e);
+    return cuda_code(cudaStreamSynchronize(g_stream));
+}
+
+/* Overworld density functions at block points for an explicit seed (host buffers, synchronous). */
+MCGEN_API int mcgen_gb300_density_values(const McWorld *w, int64_t seed, int n, const int32_t *xyz, double *out) {
+    if (!w || n < 0 || (n > 0 && (!xyz || !out)) || n > (1 << 28)) return MCGEN_E_ARG;
+    if (w->desc.dim != MG_OVERWORLD) return MCGEN_E_ARG;
+    if (n == 0) return MCGEN_OK;
+    std::lock_guard<std::mutex> lk(g_lock);
+    if (!device_ready_locked()) return MCGEN_E_UNSUPPORTED;
+    int rc = world_device_locked(const_cast<McWorld *>(w));
+    if (rc) return rc;
+    cudaError_t e;
+    {
+        DevBuf d_seed(g_stream), d_lat(g_stream), d_xyz(g_stream), d_out(g_stream);
+        if ((e = d_seed.alloc(sizeof(int64_t))) || (e = d_lat.alloc(sizeof(MgLattice) * (size_t)w->desc.ntables)) ||
+            (e = d_xyz.alloc(sizeof(int32_t) * 3 * (size_t)n)) || (e = d_out.alloc(sizeof(double) * 5 * (size_t)n)))
+            return cuda_code(e);
+        if ((e = cudaMemcpyAsync(d_seed.p, &seed, sizeof(int64_t), cudaMemcpyHostToDevice, g_stream)) ||
+            (e = cudaMemcpyAsync(d_xyz.p, xyz, sizeof(int32_t) * 3 * (size_t)n, cudaMemcpyHostToDevice, g_stream)))
+            return cuda_code(e);
+        rc = mg::launch_setup(w->desc, (const int64_t *)d_seed.p, 1, (MgLattice *)d_lat.p, g_stream);
+        if (!rc) rc = mg::launch_density(w->desc, (const MgLattice *)d_lat.p, n, (const int32_t *)d_xyz.p,
+                                         (double *)d_out.p, g_stream);
+        if (rc) return cuda_code((cudaError_t)rc);
+        if ((e = cudaMemcpyAsync(out, d_out.p, sizeof(double) * 5 * (size_t)n, cudaMemcpyDeviceToHost, g_stream)))
+            return cuda_code(e);
+    }
     return cuda_code(cudaStreamSynchronize(g_stream));
 }
 

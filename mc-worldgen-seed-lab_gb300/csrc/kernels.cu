@@ -357,6 +357,47 @@ int launch_setup(const MgWorldDesc &W, const int64_t *d_seeds, int ns, MgLattice
     return (int)cudaGetLastError();
 }
 
+/* Overworld density functions at block points (x, y, z): out[5 i + k] = continents, erosion, ridges, offset,
+ * depth as the climate sampler computes them before it rounds them to floats (engine/mc_climate.h:113-164 at
+ * block coordinates; the reference Java oracle's "df" values, oracle/gen_vectors.py:76-84).  Double branch:
+ * every noise by the exact double evaluation (no screen: the doubles themselves are the result); float
+ * branch: the floats, widened.  One thread per point, one seed's lattices through L1. */
+template <bool FM>
+__global__ void __launch_bounds__(128) k_density(const __grid_constant__ MgWorldDesc W, const MgLattice *__restrict__ T,
+                                                 int n, const int32_t *__restrict__ xyz, double *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int bx = xyz[3 * i], by = xyz[3 * i + 1], bz = xyz[3 * i + 2];
+    const double X = bx * 0.25, Z = bz * 0.25, Xc = X * MG_SECOND_STACK, Zc = Z * MG_SECOND_STACK;
+    double v[5];
+    if (FM) {
+        const float sx = nn_f_y0(W.noise[0], T, X, Z, Xc, Zc) * 4.0f; /* ShiftA (x, 0, z) */
+        const float sz = nn_f_z0(W.noise[0], T, Z, X, Zc, Xc) * 4.0f; /* ShiftB (z, x, 0) */
+        const double x = X + (double)sx, z = Z + (double)sz, xc = x * MG_SECOND_STACK, zc = z * MG_SECOND_STACK;
+        const float c = nn_f_y0(W.noise[3], T, x, z, xc, zc);
+        const float e = nn_f_y0(W.noise[4], T, x, z, xc, zc);
+        const float r = nn_f_y0(W.noise[5], T, x, z, xc, zc);
+        const float a = fabsf(r) + W.rf_f[0];
+        const float co[4] = {c, e, r, (fabsf(a) + W.rf_f[1]) * W.rf_f[2]};
+        const float off = W.off_f + spline_eval(W.spline, co);
+        const int lo = min(W.grad_from_y, W.grad_to_y), hi = max(W.grad_from_y, W.grad_to_y);
+        const int yy = by < lo ? lo : (by > hi ? hi : by);
+        const float depth = (W.grad_from_f + (float)(yy - W.grad_from_y) * W.grad_fac_f) + off;
+        v[0] = c; v[1] = e; v[2] = r; v[3] = off; v[4] = depth;
+    } else {
+        const double x = X + nn_d_y0(W.noise[0], T, X, Z, Xc, Zc) * 4.0;
+        const double z = Z + nn_d_z0(W.noise[0], T, Z, X, Zc, Xc) * 4.0;
+        const double xc = x * MG_SECOND_STACK, zc = z * MG_SECOND_STACK;
+        const double c = nn_d_y0(W.noise[3], T, x, z, xc, zc);
+        const double e = nn_d_y0(W.noise[4], T, x, z, xc, zc);
+        const double r = nn_d_y0(W.noise[5], T, x, z, xc, zc);
+        const float co[4] = {(float)c, (float)e, (float)r, (float)ridges_folded_d(W, r)};
+        const double off = 0.0 + (W.off_d + (double)spline_eval(W.spline, co)) * 1.0;
+        v[0] = c; v[1] = e; v[2] = r; v[3] = off; v[4] = depth_grad_d(W, by) + off;
+    }
+    for (int k = 0; k < 5; k++) out[5 * (size_t)i + k] = v[k];
+}
+
 template <bool FM, int DIM>
 static void points_t(const MgWorldDesc &W, const MgTreeNode *tree, const MgLattice *states, int ns, const int32_t *pts,
                      int np, uint8_t *out, int32_t *tg, cudaStream_t st) {
@@ -374,6 +415,18 @@ int launch_points(const MgWorldDesc &W, const MgTreeNode *tree, const MgLattice 
         if (W.dim == MG_OVERWORLD) points_t<false, MG_OVERWORLD>(W, tree, states, ns, pts, np, out, tg, st);
         else if (W.dim == MG_NETHER) points_t<false, MG_NETHER>(W, tree, states, ns, pts, np, out, tg, st);
         else points_t<false, MG_END>(W, tree, states, ns, pts, np, out, tg, st);
+    }
+    count_launch();
+    return (int)cudaGetLastError();
+}
+
+int launch_density(const MgWorldDesc &W, const MgLattice *state, int n, const int32_t *xyz, double *out, cudaStream_t st) {
+    if (n <= 0) return 0;
+    if (W.dim != MG_OVERWORLD) return (int)cudaErrorInvalidValue;
+    {
+        ProfScope ps_(K_DENSITY, st);
+        if (W.fmode) k_density<true><<<blocks_for(n, 128), 128, 0, st>>>(W, state, n, xyz, out);
+        else k_density<false><<<blocks_for(n, 128), 128, 0, st>>>(W, state, n, xyz, out);
     }
     count_launch();
     return (int)cudaGetLastError();

@@ -46,6 +46,10 @@ int launch_block_biomes(const MgWorldDesc &W, const MgTreeNode *tree, const MgLa
                         int z0, int nx, int nz, int step, int y, const int32_t *xyz, uint8_t *out, void *scratch,
                         int ecx0, int ecz0, int encx, int encz, cudaStream_t st);
 
+/* Overworld density functions (continents, erosion, ridges, offset, depth) at n block points xyz[3i..3i+2] of
+ * one seed's lattices: out[5i + k] (cudaErrorInvalidValue for other dimensions) */
+int launch_density(const MgWorldDesc &W, const MgLattice *state, int n, const int32_t *xyz, double *out, cudaStream_t st);
+
 /* pipe microbenchmarks (pipes.cu) */
 int pipe_rate(int pipe, double *gops);
 

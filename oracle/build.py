@@ -17,7 +17,7 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_ROOT = "/root/reference"
+REFERENCE_ROOT = os.environ.get("MCGEN_REFERENCE_ROOT", "/root/reference")  # the reference source tree
 CFLAGS = ["-O2", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared"]
 
 

@@ -1054,8 +1054,16 @@ static void seed_init(const OrWorld *w, i64 seed, SeedState *st) {
 /* ------------------------------------------------------------------------------------------------
  * Climate (engine/mc_climate.h:108-170, mcg_host.c:63-74)
  * ---------------------------------------------------------------------------------------------- */
+static void climate_ow_df(const OrWorld *w, const SeedState *st, int bx, int by, int bz, float out[6],
+                          int64_t *spl_visits, double df[5]);
 static void climate_ow(const OrWorld *w, const SeedState *st, int bx, int by, int bz, float out[6],
                        int64_t *spl_visits) {
+    climate_ow_df(w, st, bx, by, bz, out, spl_visits, NULL);
+}
+/* the same, also giving the density functions the climate is built from (df: continents, erosion,
+ * ridges, offset, depth; double in the double branch, the float values in the float branch) */
+static void climate_ow_df(const OrWorld *w, const SeedState *st, int bx, int by, int bz, float out[6],
+                          int64_t *spl_visits, double df[5]) {
     if (!w->fmode) {
         double sx = noise_get_d(&st->n[0], &w->ns[0], bx * 0.25, 0.0 * 0.25, bz * 0.25) * 4.0;
         double sz = noise_get_d(&st->n[0], &w->ns[0], bz * 0.25, bx * 0.25, 0.0 * 0.25) * 4.0;
@@ -1076,6 +1084,7 @@ static void climate_ow(const OrWorld *w, const SeedState *st, int bx, int by, in
         double depth = g + off;
         out[0] = (float)t; out[1] = (float)h; out[2] = (float)c; out[3] = (float)e; out[4] = (float)depth;
         out[5] = (float)r;
+        if (df) { df[0] = c; df[1] = e; df[2] = r; df[3] = off; df[4] = depth; }
     } else {
         float sx = noise_get_f(&st->n[0], &w->ns[0], bx * 0.25, 0.0 * 0.25, bz * 0.25) * 4.0f;
         float sz = noise_get_f(&st->n[0], &w->ns[0], bz * 0.25, bx * 0.25, 0.0 * 0.25) * 4.0f;
@@ -1098,6 +1107,7 @@ static void climate_ow(const OrWorld *w, const SeedState *st, int bx, int by, in
         float fac = (w->grad_to_f - w->grad_from_f) / (float)range;
         float g = w->grad_from_f + (float)(yy - w->grad_from_y) * fac;
         out[0] = t; out[1] = h; out[2] = c; out[3] = e; out[4] = g + off; out[5] = r;
+        if (df) { df[0] = c; df[1] = e; df[2] = r; df[3] = off; df[4] = out[4]; }
     }
 }
 static void climate_nether(const OrWorld *w, const SeedState *st, int bx, int by, int bz, float out[6]) {
@@ -1441,6 +1451,22 @@ void or_cell_climate(const OrWorld *w, int64_t seed, int qx, int qy, int qz, flo
     free(st);
 }
 
+/* Overworld density functions at block points (the reference Java oracle's "df" command, which
+ * gen_vectors.py writes to tests/vectors/<V>/df.tsv): out[5 i + k] for continents, erosion, ridges, offset,
+ * depth at (xyz[3 i], xyz[3 i + 1], xyz[3 i + 2]); engine/mc_climate.h:113-164 evaluated at block
+ * coordinates.  Returns -1 for a world that is not the Overworld. */
+int or_density(const OrWorld *w, int64_t seed, int n, const int32_t *xyz, double *out) {
+    if (w->dim != OR_OVERWORLD) return -1;
+    SeedState *st = (SeedState *)malloc(sizeof(SeedState));
+    seed_init(w, seed, st);
+    for (int i = 0; i < n; i++) {
+        float v[6];
+        climate_ow_df(w, st, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], v, NULL, out + 5 * i);
+    }
+    free(st);
+    return 0;
+}
+
 int or_tree_find(const OrWorld *w, const int64_t tg6[6], int64_t *dist, int *nmin) {
     i64 tg[TDIM] = {tg6[0], tg6[1], tg6[2], tg6[3], tg6[4], tg6[5], 0};
     int l = tree_search(&w->tree, w->tree.root, tg, -1, NULL);
@@ -1449,6 +1475,22 @@ int or_tree_find(const OrWorld *w, const int64_t tg6[6], int64_t *dist, int *nmi
     if (nmin) *nmin = tree_count_at(&w->tree, w->tree.root, tg, d);
     return l;
 }
+/* The tree as built: per node 7 lower and 7 upper bounds, first child slot, child count, biome (-1 for a
+ * subtree); kids[] the child node indices.  Returns the root; NULL arrays are skipped. */
+int or_tree_export(const OrWorld *w, int64_t *lohi, int32_t *first_count_biome, int32_t *kids) {
+    const Tree *T = &w->tree;
+    for (int i = 0; i < T->n; i++) {
+        if (lohi) for (int d = 0; d < TDIM; d++) { lohi[i * 14 + d] = T->node[i].lo[d]; lohi[i * 14 + 7 + d] = T->node[i].hi[d]; }
+        if (first_count_biome) {
+            first_count_biome[i * 3] = T->node[i].first;
+            first_count_biome[i * 3 + 1] = T->node[i].count;
+            first_count_biome[i * 3 + 2] = T->node[i].biome;
+        }
+    }
+    if (kids) memcpy(kids, T->kid, sizeof(int) * (size_t)T->nkid);
+    return T->root;
+}
+int or_tree_kids(const OrWorld *w) { return w->tree.nkid; }
 int or_leaf_biome(const OrWorld *w, int leaf) {
     return (leaf >= 0 && leaf < w->tree.n) ? w->tree.node[leaf].biome : -1;
 }

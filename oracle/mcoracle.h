@@ -99,7 +99,13 @@ void or_cell_climate(const OrWorld *w, int64_t seed, int qx, int qy, int qz, flo
 /* R-tree helpers on a quantised target: first minimum leaf (ENGINE), its
  * fitness, and the number of leaves at that fitness (capped at 2). */
 int or_tree_find(const OrWorld *w, const int64_t tg[6], int64_t *dist, int *nmin);
+/* Overworld density functions at block points: out[5 i + k], k = continents, erosion, ridges, offset, depth
+ * (double branch: the doubles; float branch: the floats); -1 for other dimensions */
+int or_density(const OrWorld *w, int64_t seed, int n, const int32_t *xyz, double *out);
 int or_leaf_biome(const OrWorld *w, int leaf);
+/* the R-tree as built (node bounds, links, biomes; child index array); returns the root */
+int or_tree_export(const OrWorld *w, int64_t *lohi, int32_t *first_count_biome, int32_t *kids);
+int or_tree_kids(const OrWorld *w);
 
 /* Algorithmic work counters for one call of or_points on one seed: node-distance
  * evaluations in the R-tree search and octave samples, summed over the points.

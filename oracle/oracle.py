@@ -52,6 +52,12 @@ def lib():
         L.or_tree_find.argtypes = [vp, i64p, C.POINTER(C.c_int64), C.POINTER(C.c_int)]
         L.or_leaf_biome.restype = i32
         L.or_leaf_biome.argtypes = [vp, i32]
+        L.or_tree_export.restype = i32
+        L.or_tree_export.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.or_density.restype = i32
+        L.or_density.argtypes = [vp, i64, i32, i32p, C.c_void_p]
+        L.or_tree_kids.restype = i32
+        L.or_tree_kids.argtypes = [vp]
         L.or_points_work.argtypes = [vp, i64, i32p, i32, C.c_void_p]
         L.or_chunk_grid.argtypes = [vp, i64, i32, i32, i32, i32, i32, u8p, i32]
         L.or_fnv1a64_names.restype = C.c_uint64
@@ -125,6 +131,23 @@ class World:
     @property
     def tree_leaves(self) -> int:
         return lib().or_tree_leaves(self._h)
+
+    def density(self, seed: int, xyz) -> np.ndarray:
+        """Overworld density functions at block points: [n, 5] continents, erosion, ridges, offset, depth."""
+        xyz = np.ascontiguousarray(xyz, dtype=np.int32).reshape(-1, 3)
+        out = np.zeros((len(xyz), 5), np.float64)
+        if lib().or_density(self._h, seed, len(xyz), _ptr(xyz), _ptr(out)) != 0:
+            raise ValueError("density functions are defined for the Overworld")
+        return out
+
+    def tree(self):
+        """The R-tree as built: (root, lo[n,7], hi[n,7], first[n], count[n], biome[n], kids[])."""
+        n = lib().or_tree_nodes(self._h)
+        lohi = np.zeros((n, 14), np.int64)
+        fcb = np.zeros((n, 3), np.int32)
+        kids = np.zeros(max(1, lib().or_tree_kids(self._h)), np.int32)
+        root = lib().or_tree_export(self._h, _ptr(lohi), _ptr(fcb), _ptr(kids))
+        return root, lohi[:, :7], lohi[:, 7:], fcb[:, 0], fcb[:, 1], fcb[:, 2], kids
 
     def noise(self, seed: int, which: int, x: float, y: float, z: float) -> float:
         return lib().or_noise_value(self._h, seed, which, x, y, z)

@@ -3,7 +3,7 @@
 Sources (read-only, present only where the reference tree is mounted):
 
 * the reference's own golden vectors, produced by its Java oracle on real game code:
-  ``tests/vectors/<V>/{climate_overworld,climate_the_nether,climate_the_end,biome_grid_hashes}.tsv``,
+  ``tests/vectors/<V>/{climate_overworld,climate_the_nether,climate_the_end,biome_grid_hashes,df}.tsv``,
   the biome-path rows of ``noise.tsv`` and ``misc.jsonl`` (``hashed`` and ``blockbiome`` commands),
   and ``tests/unit/ref26{2,3}.txt`` (NormalNoise bit tables);
 * the reference engine's CPU path (``engine/cuda/mcg_host.c``) compiled from its own sources by
@@ -28,7 +28,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference"
+REF = os.environ.get("MCGEN_REFERENCE_ROOT", "/root/reference")  # the reference source tree
 VERSIONS = ["26.1", "26.2", "26.3"]
 BIOME_NOISES = {"minecraft:offset", "minecraft:temperature", "minecraft:vegetation", "minecraft:continentalness",
                 "minecraft:erosion", "minecraft:ridge", "minecraft:nether/temperature",
@@ -41,7 +41,7 @@ def copy_vectors() -> None:
         dst = os.path.join(HERE, "vectors", v)
         os.makedirs(dst, exist_ok=True)
         for f in ("climate_overworld.tsv", "climate_the_nether.tsv", "climate_the_end.tsv",
-                  "biome_grid_hashes.tsv"):
+                  "biome_grid_hashes.tsv", "df.tsv"):
             shutil.copyfile(os.path.join(src, f), os.path.join(dst, f))
         with open(os.path.join(src, "noise.tsv")) as fi, open(os.path.join(dst, "noise.tsv"), "w") as fo:
             for line in fi:

@@ -90,6 +90,36 @@ def test_golden_blockbiome(gens, version):
         assert NAMES[w.biome_at(d["x"], d["y"], d["z"])] == d["biome"], d
 
 
+
+DF_COLUMN = {"minecraft:overworld/continents": 0, "minecraft:overworld/erosion": 1, "minecraft:overworld/ridges": 2,
+             "minecraft:overworld/offset": 3, "minecraft:overworld/depth": 4}
+
+
+@pytest.mark.parametrize("version", VERSIONS)
+def test_golden_density_functions(gens, version):
+    """df.tsv: continents, erosion, ridges, offset and depth at block points, computed on the device through
+    the C ABI (mcgen_gb300_density_values): double and float bits exact, 200 rows per version; and the same
+    on random block points against the oracle."""
+    import struct
+    w = gens[version].world("minecraft:overworld", "normal", 0)
+    rows = {}
+    for r in tsv_rows(version, "df.tsv"):
+        rows.setdefault(int(r[1]), []).append((DF_COLUMN[r[2]], int(r[3]), int(r[4]), int(r[5]), int(r[7]), int(r[8])))
+    n = 0
+    for seed, rs in rows.items():
+        got = w.density(seed, [(x, y, z) for _, x, y, z, _, _ in rs])
+        for (col, x, y, z, db, fb), v in zip(rs, got):
+            assert struct.unpack("<q", struct.pack("<d", v[col]))[0] == db, (seed, col, x, y, z)
+            assert struct.unpack("<i", struct.pack("<f", v[col]))[0] == fb, (seed, col, x, y, z)
+            n += 1
+    assert n == 200
+    rng = np.random.default_rng(31)
+    ow = O.World(ge.data_root(), version, "overworld")
+    for seed in rng.integers(-2**63, 2**63 - 1, 4, dtype=np.int64):
+        xyz = np.stack([rng.integers(-2_000_000, 2_000_000, 512), rng.integers(-80, 340, 512),
+                        rng.integers(-2_000_000, 2_000_000, 512)], 1)
+        assert np.array_equal(w.density(int(seed), xyz).view(np.int64), ow.density(int(seed), xyz).view(np.int64))
+
 @pytest.mark.parametrize("version", ALL_VERSIONS)
 @pytest.mark.parametrize("dim", ["overworld", "the_nether", "the_end"])
 def test_biome_grid_dropin(gens, version, dim):

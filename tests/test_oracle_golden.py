@@ -80,6 +80,34 @@ def test_noise_rows(data_root, version):
     assert n == 400
 
 
+DF_COLUMN = {"minecraft:overworld/continents": 0, "minecraft:overworld/erosion": 1, "minecraft:overworld/ridges": 2,
+             "minecraft:overworld/offset": 3, "minecraft:overworld/depth": 4}
+
+
+def df_rows(version):
+    """df.tsv rows grouped by seed: {seed: [(column, x, y, z, dbits, fbits)]}."""
+    out = {}
+    for r in tsv_rows(version, "df.tsv"):
+        out.setdefault(int(r[1]), []).append((DF_COLUMN[r[2]], int(r[3]), int(r[4]), int(r[5]), int(r[7]), int(r[8])))
+    return out
+
+
+@pytest.mark.parametrize("version", VERSIONS)
+def test_density_function_bits(data_root, version):
+    """df.tsv: continents, erosion, ridges, offset and depth at block points (the reference Java oracle's
+    density functions, oracle/gen_vectors.py:76-84), double and float bits exact: the full-precision values
+    behind the quantised climate rows (the spline and depth outputs included)."""
+    w = O.World(data_root, version, "overworld")
+    n = 0
+    for seed, rows in df_rows(version).items():
+        got = w.density(seed, [(x, y, z) for _, x, y, z, _, _ in rows])
+        for (col, x, y, z, db, fb), v in zip(rows, got):
+            assert dbits(v[col]) == db, (seed, col, x, y, z)
+            assert fbits(v[col]) == fb, (seed, col, x, y, z)
+            n += 1
+    assert n == 200
+
+
 @pytest.mark.parametrize("version,fname", [("26.3", "ref263.txt"), ("26.1", "ref262.txt")])
 def test_unit_noise_bits(data_root, golden_dir, version, fname):
     """tests/unit/ref26x.txt: NormalNoise bits at raw-double coordinates (float bits for 26.3)."""
