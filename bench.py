@@ -12,9 +12,16 @@ Workloads (synthetic inputs with the shapes of the published configurations):
   batch10k (default) the uneven mixed batch: 10,000 SplitMix64(3) requests (versions 26.1/26.2/26.3,
            Overworld:Nether:End 6:2:2, side log-uniform in [16, 512) quart cells), one persistent launch, against
            the plain form (one setup + one grid launch per request).  e2e: per step a plan is built from the
-           host request list, run into pinned host memory and freed.
-  serve    open-loop Poisson streams at 500/1000/2000 requests/s (SplitMix64(4), Zipf(1.1) over 50,000
-           seeds) against the continuous-batching server; p50/p99 latency, cache hit rate.
+           host request list, run into pinned host memory and freed.  The default line also carries `configs`:
+           C1 (grid256 and its quart form), C2 (seeds8), C3 (dims4096) and C5 (serve at 2,000 requests/s for
+           60 s), each with value, e2e, cpu_baseline and parity (--no-configs: the headline only).
+  serve    open-loop Poisson streams at --rates requests/s for --duration s each (SplitMix64(4), Zipf(1.1) over
+           50,000 seeds) against the continuous-batching server; p50/p99 latency from each request's scheduled
+           arrival, cache hit rate, mean batch.
+
+Parity: the CPU-baseline leg runs the oracle (the reference algorithm restated) on a sample of the same
+workload; its outputs are also compared with the GPU's timed outputs (`parity`: compared samples and
+mismatches; every code-path class of the uneven batch).
 
 A step is one pass of the workload.  `value` times steps with inputs resident in HBM through the
 device-pointer entry points; `e2e` times the same work through the host-buffer C ABI calls
@@ -210,7 +217,11 @@ def batch_fp64_ops(reqs) -> float:
 # (work units per launch, unit name, pipe peak key).
 # DRAM bytes (read + write) per work unit of a launch, from one ncu capture each: k_batch per sample
 # (300-request prefix of the uneven batch), k_ow_seed_climate per seed (4,096 seeds x 8 points).
-DRAM_BYTES_PER_UNIT = {"k_batch": (4063744 + 3648512) / 10987120, "k_ow_seed_climate": 85248 / 4096}
+DRAM_BYTES_PER_UNIT = {"k_batch": (69171456 + 2403163904) / 147087943, "k_ow_seed_climate": 85248 / 4096}
+K_BATCH_TRAFFIC_NOTE = ("DRAM bytes read + written per sample in an ncu capture of one k_batch launch over the first "
+                        "4,000 requests (147 M samples, an output larger than L2) x this launch's samples")
+# pipe utilisation of k_batch from ncu (sm__inst_executed_pipe_*, issue active) on a 300-request launch
+K_BATCH_PIPES = {"fp64": 0.518, "integer_alu": 0.511, "issue_active": 0.611}
 
 
 def kernel_work(kernel: str, seeds8: bool, ns: int, np_: int, ntables: int) -> tuple[float, str, str] | None:
@@ -381,8 +392,12 @@ def run_gb300(args, rank, world, local_rank):
                 out["roofline"] = {"kernel": top, "bound": None, "achieved": None, "peak": None, "unit": None,
                                    "frac": None, "traffic": None}
         if not args.skip_extras:
-            out["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_sample_s)
-        print(json.dumps(out), flush=True)
+            dev_step(sh)
+            torch.cuda.synchronize(dev)
+            out["cpu_baseline"], out["parity"] = cpu_baseline(args.workload, args.cpu_sample_s, d_out.cpu().numpy())
+            if args.workload == "grid256":
+                out["parity_quart_form"] = quart_form_parity(mg, gen, dev)
+    return out
 
 
 def run_batch(args, rank, world, local_rank, mg, ge):
@@ -526,19 +541,16 @@ def run_batch(args, rank, world, local_rank, mg, ge):
             out["roofline"] = {"kernel": "k_batch", "bound": "fp64", "achieved": round(achieved, 1),
                                "peak": peaks["fp64_add"], "unit": "Gop/s", "frac": round(achieved / peaks["fp64_add"], 4),
                                "traffic": round(DRAM_BYTES_PER_UNIT["k_batch"] * samples),
-                               "traffic_note": "DRAM bytes per sample from the ncu capture of a 300-request launch "
-                                               "(profiles/k_batch_uneven_batch.md) x samples; a lower bound at full "
-                                               "size, where the output no longer fits L2",
+                               "traffic_note": K_BATCH_TRAFFIC_NOTE,
                                "work": f"{ops:.4g} FP64 ops per launch (per-sample model of the screened evaluation)",
                                "peak_source": "measured in-run (FP64 add pipe microbenchmark)",
-                               "binding_pipes": {"fp64": 0.518, "integer_alu": 0.511, "issue_active": 0.611,
-                                                 "source": "ncu sm__inst_executed_pipe_* of a 300-request launch "
-                                                           "(profiles/k_batch_uneven_batch.md)"}}
+                               "binding_pipes": K_BATCH_PIPES}
         if args.split_classes:
             out["classes"] = batch_classes(reqs, worlds, mg, dev, stream)
         if not args.skip_extras:
-            out["cpu_baseline"] = cpu_baseline_batch(reqs, args.cpu_sample_s)
-        print(json.dumps(out), flush=True)
+            got = d_out.cpu().numpy()
+            out["cpu_baseline"], out["parity"] = cpu_baseline_batch(reqs, offs, got, args.cpu_sample_s)
+    return out
 
 
 # code-path classes of the uneven batch (--split-classes): the double branch (26.1/26.2) and the float
@@ -579,27 +591,67 @@ def batch_classes(reqs, worlds, mg, dev, stream) -> dict:
     return out
 
 
-def cpu_baseline_batch(reqs, budget_s: float) -> dict:
-    """The reference algorithm on the host's cores over a prefix of the same requests (rows over threads)."""
+def class_of(v: str, d: str) -> str:
+    for name, f in BATCH_CLASSES.items():
+        if f(v, d):
+            return name
+    raise ValueError((v, d))
+
+
+def cpu_baseline_batch(reqs, offs, got, budget_s: float, stride: int = 10) -> tuple[dict, dict]:
+    """The reference algorithm (oracle port) on the host's cores over a stride sample of the requests (every
+    `stride`-th request of each code-path class, until the class's share of the time budget is used), and
+    the same outputs as the parity check of the GPU's timed output `got` (requests at offsets `offs`).
+    The rate is weighted by the whole batch's samples per class: total samples / sum over classes of the
+    class's samples / its CPU rate, so a sample's class mix does not bias it.  Returns (cpu_baseline, parity)."""
     import __graft_entry__ as ge
     from oracle import oracle as O
 
     cores = os.cpu_count() or 1
     worlds = {}
-    done = cells = 0
-    t0 = time.perf_counter()
+    total = {}
     for v, d, s, qx0, qz0, n, qy in reqs:
-        key = (v, d)
-        if key not in worlds:
-            worlds[key] = O.World(ge.data_root(), v, d.split(":")[1])
-        worlds[key].quart_grid(s, qx0, qz0, n, n, qy, O.TIE_ENGINE, threads=cores)
-        done += 1
-        cells += n * n
-        if time.perf_counter() - t0 > budget_s:
-            break
-    dt = time.perf_counter() - t0
-    return {"value": cells / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"first {done} of {len(reqs)} requests ({cells} samples, {dt:.1f} s), rows over threads"}
+        c = class_of(v, d)
+        total[c] = total.get(c, 0) + n * n
+    all_samples = sum(total.values())
+    rate, detail = {}, {}
+    compared = mismatches = nreq = 0
+    bad = []
+    for c in BATCH_CLASSES:
+        idx = [i for i, r in enumerate(reqs) if class_of(r[0], r[1]) == c][::stride]
+        if not idx:
+            continue
+        share = budget_s * total[c] / all_samples
+        t_cls, cells, done = 0.0, 0, 0
+        for i in idx:
+            v, d, s, qx0, qz0, n, qy = reqs[i]
+            if (v, d) not in worlds:
+                worlds[(v, d)] = O.World(ge.data_root(), v, d.split(":")[1])
+            t0 = time.perf_counter()
+            exp = worlds[(v, d)].quart_grid(s, qx0, qz0, n, n, qy, O.TIE_ENGINE, threads=cores)
+            t_cls += time.perf_counter() - t0
+            m = int(np.count_nonzero(got[offs[i]:offs[i] + n * n] != exp.ravel()))
+            mismatches += m
+            if m and len(bad) < 8:
+                bad.append(i)
+            compared += n * n
+            cells += n * n
+            done += 1
+            if t_cls > share and done >= 4:
+                break
+        rate[c] = cells / t_cls
+        nreq += done
+        detail[c] = {"requests": done, "samples": cells, "s": round(t_cls, 2), "samples_per_s": round(rate[c])}
+    value = all_samples / sum(total[c] / rate[c] for c in total)
+    base = {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"every {stride}th request of each code-path class until its share of a {budget_s:.0f} s "
+                      f"budget ({nreq} requests, {compared} samples), rows over threads; rate weighted by the full "
+                      "batch's samples per class", "classes": detail}
+    parity = {"against": "oracle (the reference engine's CPU algorithm restated, pinned to the reference's golden "
+                         "vectors)", "requests": nreq, "compared_samples": compared, "mismatches": mismatches,
+              "classes": sorted(detail), "sample": f"every {stride}th request per class (the CPU baseline's outputs) "
+                                                  "against the timed run's output", "first_bad_requests": bad}
+    return base, parity
 
 
 def zipf_table(n: int = 50000, s: float = 1.1) -> np.ndarray:
@@ -633,13 +685,16 @@ def config5_stream(rate: float, duration: float, state: int = 4, nseeds: int = 5
     return out
 
 
-def serve_run(mg, worlds, stream, budget: int, max_inflight: int = 2):
-    """Replay an arrival stream against a server: a submitter keeps the schedule, a collector waits."""
+def serve_run(mg, worlds, stream, budget: int, max_inflight: int = 2, keep_every: int = 0):
+    """Replay an arrival stream against a server: a submitter keeps the schedule, a collector waits.
+    Latency is counted from each request's scheduled arrival (open loop: a submitter that falls behind the
+    schedule adds to the latency instead of hiding it); the server's own submit-to-completion figure is
+    reported beside it.  keep_every > 0 keeps every keep_every-th request's ids for a parity check."""
     import threading
 
     srv = mg.Server(hbm_budget_bytes=budget, max_inflight=max_inflight)
-    tickets = []
-    lat = []
+    tickets = []  # (ticket, scheduled arrival, submit time) in perf_counter seconds
+    lat, lat_sub, kept = [], [], []
     samples = 0
     done = threading.Event()
 
@@ -650,31 +705,68 @@ def serve_run(mg, worlds, stream, budget: int, max_inflight: int = 2):
                 if done.is_set() and i >= len(tickets):
                     return
                 time.sleep(0.0002)
-            ids, ms = srv.wait(tickets[i])
-            lat.append(ms)
+            t, sched, sub = tickets[i]
+            ids, ms = srv.wait(t)  # ms: submit to completion, measured by the server
+            lat.append((sub - sched) * 1e3 + ms)
+            lat_sub.append(ms)
+            if keep_every and i % keep_every == 0:
+                kept.append((i, ids.copy()))
             i += 1
 
     col = threading.Thread(target=collector)
     col.start()
     t0 = time.perf_counter()
+    lag = 0.0
     for at, (v, d, s, qx0, qz0, n, qy) in stream:
         now = time.perf_counter() - t0
         if at > now:
             time.sleep(at - now)
-        tickets.append(srv.submit(worlds[(v, d)], s, qx0, qz0, n, n, qy))
+        sub = time.perf_counter()
+        lag = max(lag, sub - t0 - at)
+        tickets.append((srv.submit(worlds[(v, d)], s, qx0, qz0, n, n, qy), t0 + at, sub))
         samples += n * n
     done.set()
     col.join()
     elapsed = time.perf_counter() - t0
     st = srv.stats()
     srv.close()
-    lat_a = np.array(lat)
+    lat_a, lat_s = np.array(lat), np.array(lat_sub)
     looks = st["cache_hits"] + st["cache_misses"]
-    return {"requests": len(stream), "elapsed_s": round(elapsed, 3), "achieved_rps": round(len(stream) / elapsed, 1),
-            "samples_per_s": samples / elapsed, "p50_ms": round(float(np.percentile(lat_a, 50)), 3),
-            "p99_ms": round(float(np.percentile(lat_a, 99)), 3), "max_ms": round(float(lat_a.max()), 3),
-            "cache_hit_rate": round(st["cache_hits"] / max(1, looks), 4), "cache_evictions": st["cache_evictions"],
-            "batches": st["batches"], "mean_batch": round(st["requests_admitted"] / max(1, st["batches"]), 2)}
+    res = {"requests": len(stream), "elapsed_s": round(elapsed, 3), "achieved_rps": round(len(stream) / elapsed, 1),
+           "samples_per_s": samples / elapsed, "p50_ms": round(float(np.percentile(lat_a, 50)), 3),
+           "p99_ms": round(float(np.percentile(lat_a, 99)), 3), "max_ms": round(float(lat_a.max()), 3),
+           "latency_from": "scheduled arrival",
+           "p50_from_submit_ms": round(float(np.percentile(lat_s, 50)), 3),
+           "p99_from_submit_ms": round(float(np.percentile(lat_s, 99)), 3),
+           "max_submit_lag_ms": round(lag * 1e3, 3),
+           "cache_hit_rate": round(st["cache_hits"] / max(1, looks), 4), "cache_evictions": st["cache_evictions"],
+           "batches": st["batches"], "mean_batch": round(st["requests_admitted"] / max(1, st["batches"]), 2)}
+    return (res, kept) if keep_every else res
+
+
+def serve_parity(stream, kept) -> tuple[dict, dict]:
+    """The reference algorithm (oracle port) on all host cores over the kept served requests, timed (the CPU
+    baseline of the stream) and compared with the ids the server returned (parity)."""
+    import __graft_entry__ as ge
+    from oracle import oracle as O
+
+    cores = os.cpu_count() or 1
+    wl, mism, cmp_, dt = {}, 0, 0, 0.0
+    for i, ids in kept:
+        v, d, s, qx0, qz0, n, qy = stream[i][1]
+        if (v, d) not in wl:
+            wl[(v, d)] = O.World(ge.data_root(), v, d.split(":")[1])
+        t0 = time.perf_counter()
+        exp = wl[(v, d)].quart_grid(s, qx0, qz0, n, n, qy, O.TIE_ENGINE, threads=cores)
+        dt += time.perf_counter() - t0
+        mism += int(np.count_nonzero(ids != exp))
+        cmp_ += n * n
+    base = {"value": cmp_ / max(dt, 1e-9), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{len(kept)} requests at a fixed stride of the stream ({cmp_} samples, {dt:.1f} s), rows over "
+                      "threads"}
+    parity = {"against": ORACLE_NOTE, "requests": len(kept), "compared_samples": cmp_, "mismatches": mism,
+              "sample": "a fixed stride of the served requests, their ids as the server returned them"}
+    return base, parity
 
 
 SEARCH_SEED = 8675309
@@ -759,7 +851,7 @@ def run_search(args, rank, world, local_rank, mg, ge):
     if rank == 0:
         if not args.skip_extras:
             out["cpu_baseline"] = cpu_baseline_search(mg, ge, args.cpu_sample_s)
-        print(json.dumps(out), flush=True)
+    return out
 
 
 def cpu_baseline_search(mg, ge, budget_s: float) -> dict:
@@ -837,7 +929,7 @@ def run_map(args, rank, world, local_rank, mg, ge):
     if rank == 0:
         if not args.skip_extras:
             out["cpu_baseline"] = cpu_baseline_map(args.cpu_sample_s)
-        print(json.dumps(out), flush=True)
+    return out
 
 
 def cpu_baseline_map(budget_s: float) -> dict:
@@ -873,6 +965,7 @@ def run_dims(args, rank, world, local_rank, mg, ge):
     res = {}
     total_samples, total_ms, kern = 0, 0.0, {}
     total_e2e_s, total_h2d = 0.0, 0
+    outs = {}
     with ClockSampler(local_rank) as clk:
         for dim in ("minecraft:the_nether", "minecraft:the_end"):
             w = gen.world(dim, "normal", 0)
@@ -889,6 +982,7 @@ def run_dims(args, rank, world, local_rank, mg, ge):
             ev1.record(stream)
             torch.cuda.synchronize(dev)
             ms = ev0.elapsed_time(ev1) / args.steps
+            outs[dim.split(":")[1]] = d_out.cpu().numpy().reshape(len(seeds), 64, 64)  # request i at offset 4096 i
             mg.profile(True)
             plan.run_dev(d_out.data_ptr(), sh, graph=False)
             torch.cuda.synchronize(dev)
@@ -932,12 +1026,14 @@ def run_dims(args, rank, world, local_rank, mg, ge):
         out["clocks"] = clocks
     if rank == 0:
         if not args.skip_extras:
-            out["cpu_baseline"] = cpu_baseline_dims(args.cpu_sample_s)
-        print(json.dumps(out), flush=True)
+            out["cpu_baseline"], out["parity"] = cpu_baseline_dims(args.cpu_sample_s, outs)
+    return out
 
 
-def cpu_baseline_dims(budget_s: float) -> dict:
-    """The reference algorithm (oracle port) on all host cores over the first seeds of the same workload."""
+def cpu_baseline_dims(budget_s: float, got: dict, stride: int = 16) -> tuple[dict, dict]:
+    """The reference algorithm (oracle port) on all host cores over every `stride`-th seed of the workload
+    (until the time budget is used), and the same outputs as the parity check of the GPU's grids.
+    Returns (cpu_baseline, parity)."""
     import __graft_entry__ as ge
     from oracle import oracle as O
 
@@ -945,79 +1041,133 @@ def cpu_baseline_dims(budget_s: float) -> dict:
     seeds, origins = config3_inputs()
     wn = O.World(ge.data_root(), "26.3", "the_nether")
     we = O.World(ge.data_root(), "26.3", "the_end")
-    done, t0 = 0, time.perf_counter()
-    for sd, (qx, qz) in zip(seeds, origins):
-        wn.quart_grid(int(sd), int(qx), int(qz), 64, 64, 16, O.TIE_ENGINE, threads=cores)
-        we.quart_grid(int(sd), int(qx), int(qz), 64, 64, 16, O.TIE_ENGINE, threads=cores)
+    done, mism, t0 = 0, 0, time.perf_counter()
+    for i in range(0, len(seeds), stride):
+        sd, (qx, qz) = int(seeds[i]), origins[i]
+        en = wn.quart_grid(sd, int(qx), int(qz), 64, 64, 16, O.TIE_ENGINE, threads=cores)
+        ee = we.quart_grid(sd, int(qx), int(qz), 64, 64, 16, O.TIE_ENGINE, threads=cores)
+        mism += int(np.count_nonzero(got["the_nether"][i] != en)) + int(np.count_nonzero(got["the_end"][i] != ee))
         done += 1
         if time.perf_counter() - t0 > budget_s:
             break
     dt = time.perf_counter() - t0
-    return {"value": done * 2 * 64 * 64 / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"first {done} of the 4096 seeds, Nether and End ({dt:.1f} s), rows over threads"}
+    return ({"value": done * 2 * 64 * 64 / dt, "unit": UNIT, "cores": cores, "kind": "port",
+             "sample": f"every {stride}th of the 4096 seeds ({done} seeds), Nether and End ({dt:.1f} s), rows over "
+                       "threads"},
+            {"against": ORACLE_NOTE, "compared_samples": done * 2 * 64 * 64, "mismatches": mism,
+             "sample": f"every {stride}th seed's Nether and End grids (the CPU baseline's outputs)"})
 
 
 def run_serve(args, rank, world, local_rank, mg, ge):
-    """Serving: open-loop Poisson streams at several rates, continuous batching, 8 GB noise-state cache."""
+    """Serving: open-loop Poisson streams at each rate of --rates for --duration s, continuous batching,
+    8 GB noise-state cache; latency from each request's scheduled arrival.  With small_budget, one more run at
+    the middle rate with a 2 MB cache forces LRU evictions."""
     import torch
 
     torch.cuda.set_device(local_rank)
     gens = {v: mg.Generator.open(ge.data_root(), v) for v in C4_VERSIONS}
     worlds = {(v, d): gens[v].world(d, "normal", 0) for v in C4_VERSIONS for d in set(C4_DIMS)}
     warm = config5_stream(200.0, 1.0, state=99)
-    serve_run(mg, worlds, warm, 8 << 30)
+    serve_run(mg, worlds, warm, 8 << 30, args.inflight)
     rates = [float(x) for x in args.rates.split(",")]
     runs = {}
     with ClockSampler(local_rank) as clk:
-        for rate in rates:
-            runs[str(int(rate))] = serve_run(mg, worlds, config5_stream(rate, args.duration), 8 << 30)
-        small = serve_run(mg, worlds, config5_stream(rates[len(rates) // 2], args.duration / 2), 2 << 20)
+        for k, rate in enumerate(rates):
+            stream = config5_stream(rate, args.duration)
+            if k == len(rates) - 1 and not args.skip_extras:
+                runs[str(int(rate))], kept = serve_run(mg, worlds, stream, 8 << 30, args.inflight,
+                                                       keep_every=max(1, len(stream) // 200))
+                top_stream = stream
+            else:
+                runs[str(int(rate))] = serve_run(mg, worlds, stream, 8 << 30, args.inflight)
+        small = (serve_run(mg, worlds, config5_stream(rates[len(rates) // 2], args.duration / 2), 2 << 20, args.inflight)
+                 if getattr(args, "small_budget", True) else None)
     top = runs[str(int(rates[-1]))]
+    under = [r for r in rates if runs[str(int(r))]["p99_ms"] < 20.0]
     out = {"metric": METRIC + " (served)", "value": top["samples_per_s"], "unit": UNIT, "n_gpus": world,
            "steps": len(rates), "warmup": 1, "ms_per_step": top["elapsed_s"] * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64+int64",
            "data": "synthetic (SplitMix64(4) Poisson stream, Zipf(1.1) over 50,000 seeds)",
            "config": {"workload": f"served: open-loop Poisson arrivals at {args.rates} req/s for {args.duration} s each, "
                                   "requests from the uneven-batch distribution, seeds Zipf(1.1) over 50,000; "
-                                  "continuous batching on 2 streams, 8 GB noise-state cache (LRU)",
+                                  f"continuous batching on {args.inflight} streams, 8 GB noise-state cache (LRU); "
+                                  "latency from scheduled arrival",
                       "rates": rates, "duration_s": args.duration,
                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
-           "served": runs, "small_budget_2MB": small,
-           "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
+           "served": runs, "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"],
+           "highest_rate_p99_under_20ms": max(under) if under else None,
            "e2e": {"value": top["samples_per_s"], "unit": UNIT, "h2d_bytes_per_step": 0,
-                   "d2h_bytes_per_step": int(top["samples_per_s"] * top["elapsed_s"])}}
+                   "d2h_bytes_per_step": int(top["samples_per_s"] * top["elapsed_s"]),
+                   "call": "mcgen_gb300_server_submit (host output buffer) + server_wait per request"}}
+    if small is not None:
+        out["small_budget_2MB"] = small
     clocks = clk.summary()
     if clocks:
         out["clocks"] = clocks
-    if rank == 0:
-        print(json.dumps(out), flush=True)
+    if not args.skip_extras:
+        out["cpu_baseline"], out["parity"] = serve_parity(top_stream, kept)
+    return out
 
 
-def cpu_baseline(workload: str, budget_s: float) -> dict:
-    """The reference algorithm on this host's cores (CPU oracle, OpenMP over seeds or rows)."""
+ORACLE_NOTE = "oracle (the reference engine's CPU algorithm restated, pinned to the reference's golden vectors)"
+
+
+def cpu_baseline(workload: str, budget_s: float, got: np.ndarray) -> tuple[dict, dict]:
+    """The reference algorithm on this host's cores (CPU oracle, OpenMP over seeds or rows) over a sample of
+    the workload, and the same outputs as the parity check of the GPU's output `got`.
+    Returns (cpu_baseline, parity)."""
     import __graft_entry__ as ge
     from oracle import oracle as O
 
     cores = os.cpu_count() or 1
     w = O.World(ge.data_root(), "26.3", "overworld")
     if workload == "seeds8":
-        seeds, pts = config2_inputs()
-        n = 256
-        while True:  # grow the sample until it takes a meaningful share of the budget
+        seeds, pts = config2_inputs(got.size // 8)
+        got = got.reshape(seeds.size, len(pts))
+        stride = 256
+        while True:  # a stride sample of the seeds, grown until it takes a meaningful share of the budget
             t0 = time.perf_counter()
-            w.points(seeds[:n], pts, threads=cores)
+            exp = w.points(seeds[::stride], pts, threads=cores)
             dt = time.perf_counter() - t0
-            if dt > budget_s / 4 or n >= seeds.size:
+            if dt > budget_s / 4 or stride == 1:
                 break
-            n = min(seeds.size, n * 4)
-        return {"value": n * len(pts) / dt, "unit": UNIT, "cores": cores, "kind": "port",
-                "sample": f"first {n} of the 65536 seeds x 8 points ({dt:.2f} s)"}
+            stride = max(1, stride // 4)
+        n = exp.shape[0]
+        mism = int(np.count_nonzero(got[::stride] != exp))
+        return ({"value": n * len(pts) / dt, "unit": UNIT, "cores": cores, "kind": "port",
+                 "sample": f"every {stride}th of the {seeds.size} seeds x 8 points ({n} seeds, {dt:.2f} s)"},
+                {"against": ORACLE_NOTE, "compared_samples": int(exp.size), "mismatches": mism,
+                 "sample": f"every {stride}th seed x 8 points (the CPU baseline's outputs)"})
     t0 = time.perf_counter()
-    rows = 64
-    w.biome_grid(12345, -512, -512, 256, rows, 4, 64, threads=cores)
+    exp = w.biome_grid(12345, -512, -512, 256, 256, 4, 64, threads=cores)
     dt = time.perf_counter() - t0
-    return {"value": 256 * rows / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{rows} of the 256 grid rows ({dt:.2f} s), rows over threads"}
+    mism = int(np.count_nonzero(got.reshape(256, 256) != exp))
+    return ({"value": 256 * 256 / dt, "unit": UNIT, "cores": cores, "kind": "port",
+             "sample": f"the whole 256 x 256 grid ({dt:.2f} s), rows over threads"},
+            {"against": ORACLE_NOTE, "compared_samples": 256 * 256, "mismatches": mism,
+             "sample": "the whole drop-in grid (zoom + chunk-cell ties)"})
+
+
+# FNV-1a64 digest of the reference's golden 1024 x 1024 quart grid (GRID_CHAIN ties) of Overworld 26.3,
+# seed 12345, qx, qz in [-512, 512), qy = 16 (tests/vectors/26.3/biome_grid_hashes.tsv, mode "point")
+C1_GOLDEN_DIGEST = "a79bc97b2afa0ecd"
+
+
+def quart_form_parity(mg, gen, dev) -> dict:
+    """C1's quart form: the 256 x 256 quart grid qx, qz in [-128, 128) at qy = 16 (ENGINE ties) through
+    mcgen_gb300_quart_grid against the oracle, and its 1024 x 1024 superset under GRID_CHAIN against the
+    reference's golden digest."""
+    import __graft_entry__ as ge
+    from oracle import oracle as O
+
+    w = gen.world("minecraft:overworld", "normal", 12345)
+    got = w.quart_grid(-128, -128, 256, 256, 16, mg.TIE_ENGINE)
+    exp = O.World(ge.data_root(), "26.3", "overworld").quart_grid(12345, -128, -128, 256, 256, 16, O.TIE_ENGINE)
+    big = w.quart_grid(-512, -512, 1024, 1024, 16, mg.TIE_GRID_CHAIN)
+    digest = O.fnv1a64_names(big)
+    return {"against": ORACLE_NOTE + "; the golden digest", "compared_samples": 256 * 256,
+            "mismatches": int(np.count_nonzero(got != exp)), "golden_digest_1024": digest,
+            "golden_digest_match": digest == C1_GOLDEN_DIGEST}
 
 
 def run_reference(args, rank, world):
@@ -1038,18 +1188,34 @@ def run_reference(args, rank, world):
                   "version": "26.3", "dimension": "overworld"}
     elif args.workload in ("batch10k", "serve"):
         reqs = config4_requests(args.requests)
-        nfirst = 256
         wl = {}
-        for v, d, *_ in reqs[:nfirst]:
-            if (v, d) not in wl:
-                wl[(v, d)] = O.World(ge.data_root(), v, d.split(":")[1])
+        classes = {c: [i for i, r in enumerate(reqs) if class_of(r[0], r[1]) == c] for c in BATCH_CLASSES}
+        total = {c: sum(reqs[i][5] ** 2 for i in idx) for c, idx in classes.items() if idx}
+        stride = 40
+        step_no = [0]
+        acc = {c: [0, 0.0] for c in total}  # per class: samples, seconds
 
         def per_step():
-            for v, d, s, qx0, qz0, n, qy in reqs[:nfirst]:
-                wl[(v, d)].quart_grid(s, qx0, qz0, n, n, qy, O.TIE_ENGINE, threads=cores)
+            k = step_no[0] % stride
+            step_no[0] += 1
+            for c in total:
+                t0, cells = time.perf_counter(), 0
+                for i in classes[c][k::stride]:
+                    v, d, s, qx0, qz0, n, qy = reqs[i]
+                    if (v, d) not in wl:
+                        wl[(v, d)] = O.World(ge.data_root(), v, d.split(":")[1])
+                    wl[(v, d)].quart_grid(s, qx0, qz0, n, n, qy, O.TIE_ENGINE, threads=cores)
+                    cells += n * n
+                acc[c][0] += cells
+                acc[c][1] += time.perf_counter() - t0
 
-        samples = sum(n * n for *_, n, qy in reqs[:nfirst])
-        sample = f"first {nfirst} of the {len(reqs)} uneven-batch requests ({samples} samples) per step, rows over threads"
+        def weighted():  # the whole batch's samples over the time the per-class rates give it
+            return sum(total.values()) / sum(total[c] / (acc[c][0] / acc[c][1]) for c in total)
+
+        samples = sum(total.values())
+        sample = (f"per step every {stride}th request of each code-path class (a different offset each step), rows "
+                  "over threads; rate = the whole batch's samples / the sum of its per-class samples over the "
+                  "per-class rates")
         config = {"workload": f"uneven mixed batch: {len(reqs)} SplitMix64(3) requests, versions 26.1/26.2/26.3, "
                               "Overworld:Nether:End 6:2:2, square side log-uniform in [16,512) quart cells, origin "
                               "uniform in [-30000,30000] blocks, y=64, ENGINE tie rule", "requests": len(reqs)}
@@ -1087,18 +1253,54 @@ def run_reference(args, rank, world):
                     else (METRIC, UNIT))
     for _ in range(args.warmup):
         per_step()
+    if args.workload in ("batch10k", "serve"):
+        for c in acc:
+            acc[c] = [0, 0.0]
     t0 = time.perf_counter()
     for _ in range(args.steps):
         per_step()
     dt = time.perf_counter() - t0
     value = samples * args.steps / dt
+    full_batch_s = None
+    if args.workload in ("batch10k", "serve"):
+        value = weighted()
+        full_batch_s = samples / value  # the whole batch at the measured per-class rates
     out = {"impl": "reference", "metric": metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32+f64+int64", "data": "synthetic (SplitMix64 seeds and points)",
            "config": config,
            "cpu_baseline": {"value": value, "unit": unit, "cores": cores, "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if full_batch_s is not None:
+        out["full_batch_s"] = round(full_batch_s, 2)
     print(json.dumps(out), flush=True)
+
+
+# The configurations besides the headline (C4): the plain single-seed grid (C1, drop-in and quart forms),
+# many seeds x fixed points (C2), the other dimensions (C3) and the served stream at 2,000 requests/s for
+# 60 s (C5), each with its device value, end-to-end value, CPU baseline and parity check.
+CONFIGS = (("C1_grid256", "grid256", {}), ("C2_seeds8", "seeds8", {}), ("C3_dims4096", "dims4096", {}),
+           ("C5_serve_2000rps_60s", "serve", {"rates": "2000", "duration": 60.0, "small_budget": False}))
+CONFIG_KEYS = ("metric", "value", "unit", "ms_per_step", "steps", "config", "e2e", "cpu_baseline", "parity",
+               "parity_quart_form", "roofline", "kernels", "gpu_launches", "served", "p50_ms", "p99_ms",
+               "highest_rate_p99_under_20ms", "clocks")
+
+
+def run_configs(args, rank, world, local_rank) -> dict:
+    import copy
+
+    res = {}
+    for name, workload, extra in CONFIGS:
+        sub = copy.copy(args)
+        sub.workload = workload
+        sub.split_classes = False
+        sub.cpu_sample_s = min(args.cpu_sample_s, 6.0)
+        sub.seeds = 65536
+        for k, v in extra.items():
+            setattr(sub, k, v)
+        line = run_gb300(sub, rank, world, local_rank)
+        res[name] = {k: line[k] for k in CONFIG_KEYS if k in line}
+    return res
 
 
 def main():
@@ -1111,7 +1313,10 @@ def main():
                     default="batch10k")
     ap.add_argument("--search-candidates", type=int, default=1 << 26, help="search: candidates per step")
     ap.add_argument("--rates", default="500,1000,2000", help="serve: arrival rates (requests/s)")
-    ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds per rate (60 = the configuration)")
+    ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds per rate (60 = the configuration)")
+    ap.add_argument("--inflight", type=int, default=2, help="serve: batches in flight (server streams)")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="batch10k: the headline only, without the other configurations")
     ap.add_argument("--requests", type=int, default=10000, help="batch10k: number of requests")
     ap.add_argument("--split-classes", action="store_true",
                     help="batch10k: also time each code-path class's requests as a plan of their own")
@@ -1129,7 +1334,11 @@ def main():
 
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     try:
-        run_gb300(args, rank, world, local_rank)
+        out = run_gb300(args, rank, world, local_rank)
+        if args.workload == "batch10k" and not (args.skip_extras or args.no_configs) and world == 1:
+            out["configs"] = run_configs(args, rank, world, local_rank)
+        if rank == 0 and out is not None:
+            print(json.dumps(out), flush=True)
     finally:
         if world > 1:
             import torch
