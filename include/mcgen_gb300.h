@@ -214,8 +214,10 @@ MCGEN_API int mcgen_gb300_check_climate(const McWorld *w, long long n, unsigned 
                                         long long *fallback);
 /* Device self-check of the R-tree searches of a world's tree (Overworld or Nether): the level-unrolled and
  * single-loop searches with 32-bit box distances, and the tie search, against the 64-bit stack searches on
- * n random targets (half of them beyond the 32-bit distances' clamp).  *bad_leaf counts differing leaves,
- * *bad_other differing fitness values or tie flags.  MCGEN_E_ARG for End worlds. */
+ * n random targets (half of them beyond the 32-bit distances' clamp); and the warp-shared search (one pruned
+ * walk per warp of neighbouring cells) on n more targets clustered per warp at several spreads, some lanes
+ * inactive, some warps with a lane beyond the packed range.  *bad_leaf counts differing leaves, *bad_other
+ * differing fitness values or tie flags.  MCGEN_E_ARG for End worlds. */
 MCGEN_API int mcgen_gb300_check_tree(const McWorld *w, long long n, unsigned long long seed, long long *bad_leaf,
                                      long long *bad_other);
 

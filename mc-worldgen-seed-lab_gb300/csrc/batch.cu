@@ -146,6 +146,7 @@ struct BatchSmem {
         BatchLat o;
         BatchEnd end;
     };
+    WarpTreeScratch wt[BNT / 32]; /* each warp's R-tree candidate list (Overworld, ENGINE rule) */
     double depth_g; /* the double-branch Overworld tile's depth gradient (depth_grad_d) */
     int tile, req, state;
 };
@@ -155,22 +156,31 @@ struct BatchSmem {
 template <bool FM, int DIM, int TILE_W>
 __device__ __forceinline__ void batch_cells(const MgWorldDesc &W, const MgSpline &S, const MgLattice *T,
                                             const MgTreeNode *tree, const MgBatchReq &R, int tx0, int tz0,
-                                            const ShiftTable<8, BNT / 8> *tab, double g, uint8_t *out) {
+                                            const ShiftTable<8, BNT / 8> *tab, double g, WarpTreeScratch *wt,
+                                            uint8_t *out) {
     const int col = threadIdx.x % TILE_W, row = threadIdx.x / TILE_W;
     const int ix = tx0 + col, iz = tz0 + row;
-    if (ix >= R.nx || iz >= R.nz) return;
+    const bool in = ix < R.nx && iz < R.nz;
     const int qx = R.qx0 + ix, qz = R.qz0 + iz;
-    uint8_t b;
-    if (R.tie == MG_TIE_CHUNK_CELL) {
-        b = (uint8_t)cell_chunk<FM, DIM>(W, S, T, tree, qx, R.qy, qz);
-    } else {
-        int32_t tg[6];
+    if (R.tie == MG_TIE_CHUNK_CELL) { /* the request's rule: the same for the whole CTA */
+        if (in) out[R.out_off + (size_t)iz * R.nx + ix] = (uint8_t)cell_chunk<FM, DIM>(W, S, T, tree, qx, R.qy, qz);
+        return;
+    }
+    int32_t tg[6] = {0, 0, 0, 0, 0, 0};
+    if (in) {
         if (!FM && DIM == MG_OVERWORLD && TILE_W == 8 && tab) climate_ow_d_tab(W, S, T, *tab, col, row, qx, R.qy, qz, g, tg);
         else cell_target<FM, DIM>(W, S, T, qx, R.qy, qz, tg);
-        uint64_t d;
-        b = tree[tree_search(tree, tg, -1, d)].biome;
     }
-    out[R.out_off + (size_t)iz * R.nx + ix] = b;
+    int leaf;
+    /* one pruned walk of the tree per warp of 8 x 4 cells for wide trees (built only into the float branch's
+     * code: the double branch's versions, 26.1 and 26.2, have 6 children per node) */
+    if (FM && DIM == MG_OVERWORLD && W.tree_fanout >= MG_WARP_TREE_FANOUT) {
+        leaf = tree_search_warp(tree, tg, in, wt[threadIdx.x >> 5]);
+    } else {
+        uint64_t d;
+        leaf = in ? tree_search(tree, tg, -1, d) : -1;
+    }
+    if (in) out[R.out_off + (size_t)iz * R.nx + ix] = tree[leaf].biome;
 }
 
 /* End tile: chunks [cx0, cx0 + END_TC) x [cz0, cz0 + END_TC) counted from the chunk of the request's
@@ -259,8 +269,8 @@ __global__ void __launch_bounds__(BNT, MINB) k_batch(const MgWorldDesc *__restri
         const int tx0 = (tile % tw) * TILE_W, tz0 = (tile / tw) * TILE_H;
         const MgTreeNode *tree = trees[R.world];
         if (W.fmode) {
-            if (W.dim == MG_OVERWORLD) batch_cells<true, MG_OVERWORLD, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, 0.0, out);
-            else batch_cells<true, MG_NETHER, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, 0.0, out);
+            if (W.dim == MG_OVERWORLD) batch_cells<true, MG_OVERWORLD, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, 0.0, sm.wt, out);
+            else batch_cells<true, MG_NETHER, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, 0.0, sm.wt, out);
         } else if (W.dim == MG_OVERWORLD) {
             /* the tile's shift splits, computed once per column and row (ENGINE rule) */
             const bool tab = TILE_W == 8 && R.tie != MG_TIE_CHUNK_CELL && shift_table_ok(W);
@@ -270,9 +280,9 @@ __global__ void __launch_bounds__(BNT, MINB) k_batch(const MgWorldDesc *__restri
                 __syncthreads();
             }
             batch_cells<false, MG_OVERWORLD, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, tab ? &sm.o.shift : nullptr,
-                                                     tab ? sm.depth_g : 0.0, out);
+                                                     tab ? sm.depth_g : 0.0, sm.wt, out);
         } else {
-            batch_cells<false, MG_NETHER, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, 0.0, out);
+            batch_cells<false, MG_NETHER, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, 0.0, sm.wt, out);
         }
     }
 }

@@ -986,6 +986,165 @@ __device__ __forceinline__ int tree_search_tie(const MgTreeNode *__restrict__ T,
     return tree_search_tie_stack(T, t, best, tied);
 }
 
+/* ------------------------------------------------------------------ warp-shared R-tree candidates
+ * The search's result is the first leaf in depth-first order at the minimum distance (a child is entered
+ * iff its box is closer than the best leaf so far, a leaf replaces it iff strictly closer; every ancestor of
+ * the first minimal leaf is at most as far, so the walk reaches it, and nothing after it is strictly closer).
+ * So any list of leaves, in depth-first order, that holds every leaf able to be at the minimum for a target
+ * gives the same leaf when scanned for the first strict minimum.  A warp's 32 cells are neighbours (an 8 x 4
+ * block of a tile) with close targets: for the box B spanning them, a leaf whose distance to B (lower bound
+ * over B) exceeds U, the least over leaves of their largest distance to a point of B, is farther than some
+ * leaf for every target in B.  One walk per warp (the lanes take a node's children, up to 32 at once) lists
+ * the leaves with lower bound <= U in depth-first order, U shrinking as leaves are met and starting from the
+ * leaf a greedy descent reaches; each lane then scans only that list.  Both bounds use the packed 16-bit
+ * distances with B's corners in place of the target (max(lo - Bhi, Blo - hi, 0) and max(lo - Blo, Bhi - hi,
+ * 0) per dimension): a clamped lower bound is still a lower bound, and an upper bound is used only when
+ * below MG_RT_CLAMP^2, where no dimension was clamped.  A list or stack that would overflow gives up (-1)
+ * and the lanes search alone. */
+#define MG_WC_CAND 128
+#define MG_WC_STACK 128
+/* the shared walk pays when a node's children fill most of a warp's lanes: trees built with 19 children per
+ * node (26.3 on) take it; with 6 per node (26.1, 26.2) each step would use 6 of 32 lanes, and the lanes'
+ * own level-unrolled searches measured faster */
+#define MG_WARP_TREE_FANOUT 12
+struct WarpTreeScratch {
+    uint16_t cand[MG_WC_CAND];
+    uint16_t stack[MG_WC_STACK];
+};
+__device__ __forceinline__ uint32_t rt_ub_or_inf(const uint4 &a, const uint4 &b, const RtTarget &ubq) {
+    const uint32_t u = rt_dist(a, b, ubq);
+    return u < (uint32_t)MG_RT_CLAMP * MG_RT_CLAMP ? u : 0xFFFFFFFFu;
+}
+/* all 32 lanes call it with the same box; returns the number of candidates in ws.cand, or -1 */
+__device__ __forceinline__ int warp_tree_candidates(const MgTreeNode *__restrict__ T, const RtTarget &lbq,
+                                                    const RtTarget &ubq, WarpTreeScratch &ws) {
+    const unsigned FULL = 0xFFFFFFFFu;
+    const int lane = threadIdx.x & 31;
+    const uint32_t rw = reinterpret_cast<const uint4 *>(T)[1].w;
+    /* greedy descent to a leaf (the child nearest to B at each level) for the first bound */
+    uint32_t U = 0xFFFFFFFFu;
+    {
+        int first = (int)(rw & 0xFFFFu), count = (int)((rw >> 16) & 0xFFu);
+        for (int depth = 0; depth < MG_RT_STACK; depth++) {
+            if (count > 32) return -1; /* one lane per child */
+            uint32_t lb = 0xFFFFFFFFu, w = 0;
+            if (lane < count) {
+                const uint4 a = *reinterpret_cast<const uint4 *>(T + first + lane);
+                const uint4 b = *(reinterpret_cast<const uint4 *>(T + first + lane) + 1);
+                lb = rt_dist(a, b, lbq);
+                w = b.w;
+            }
+            const uint32_t m = __reduce_min_sync(FULL, lb);
+            const int pick = __ffs(__ballot_sync(FULL, lb == m)) - 1;
+            const uint32_t pw = __shfl_sync(FULL, w, pick);
+            if (((pw >> 16) & 0xFFu) == 0) {
+                const uint4 a = *reinterpret_cast<const uint4 *>(T + first + pick);
+                const uint4 b = *(reinterpret_cast<const uint4 *>(T + first + pick) + 1);
+                U = rt_ub_or_inf(a, b, ubq);
+                break;
+            }
+            first = (int)(pw & 0xFFFFu);
+            count = (int)((pw >> 16) & 0xFFu);
+        }
+    }
+    /* depth-first walk; the stack holds pending nodes with the earliest in depth-first order on top */
+    int sp = 1, nc = 0;
+    if (lane == 0) ws.stack[0] = 0;
+    __syncwarp();
+    while (sp > 0) {
+        const int node = ws.stack[--sp];
+        const uint32_t nw = reinterpret_cast<const uint4 *>(T + node)[1].w;
+        __syncwarp(); /* every lane has read the top before it is overwritten */
+        const int count = (int)((nw >> 16) & 0xFFu);
+        if (count == 0) { /* a leaf queued behind an internal sibling: it is next in depth-first order */
+            if (nc >= MG_WC_CAND) return -1;
+            if (lane == 0) ws.cand[nc] = (uint16_t)node;
+            nc++;
+            __syncwarp();
+            continue;
+        }
+        if (count > 32) return -1;
+        const int ci = (int)(nw & 0xFFFFu) + lane;
+        bool keep = false, leaf = false;
+        uint32_t ub = 0xFFFFFFFFu;
+        if (lane < count) {
+            const uint4 a = *reinterpret_cast<const uint4 *>(T + ci);
+            const uint4 b = *(reinterpret_cast<const uint4 *>(T + ci) + 1);
+            keep = rt_dist(a, b, lbq) <= U;
+            leaf = ((b.w >> 16) & 0xFFu) == 0;
+            if (keep && leaf) ub = rt_ub_or_inf(a, b, ubq);
+        }
+        U = min(U, __reduce_min_sync(FULL, ub));
+        const unsigned km = __ballot_sync(FULL, keep);
+        const unsigned im = __ballot_sync(FULL, keep && !leaf);
+        /* leaves before the first internal survivor come next in depth-first order: listed now; the first
+         * internal survivor and everything after it are pushed, the first on top */
+        const unsigned em = im ? km & ((1u << (__ffs(im) - 1)) - 1u) : km;
+        const unsigned pm = km & ~em;
+        const unsigned lt = (1u << lane) - 1u;
+        const int ne = __popc(em), np = __popc(pm);
+        if (nc + ne > MG_WC_CAND || sp + np > MG_WC_STACK) return -1;
+        if ((em >> lane) & 1u) ws.cand[nc + __popc(em & lt)] = (uint16_t)ci;
+        if ((pm >> lane) & 1u) ws.stack[sp + np - 1 - __popc(pm & lt)] = (uint16_t)ci;
+        nc += ne;
+        sp += np;
+        __syncwarp();
+    }
+    return nc;
+}
+/* first strict minimum of the packed distance over the listed leaves (the same for every lane's loop) */
+__device__ __forceinline__ RtState rt_scan(const MgTreeNode *__restrict__ T, const uint16_t *cand, int n,
+                                           const RtTarget &q) {
+    RtState s{0xFFFFFFFFu, -1, 0};
+    for (int k = 0; k < n; k++) {
+        const int ci = cand[k];
+        const uint4 a = *reinterpret_cast<const uint4 *>(T + ci);
+        const uint4 b = *(reinterpret_cast<const uint4 *>(T + ci) + 1);
+        const uint32_t d = rt_dist(a, b, q);
+        if (d < s.best) { s.best = d; s.res = ci; }
+    }
+    return s;
+}
+/* tree_search (no candidate) for the 32 cells of a warp, called by all 32 lanes; lanes with active == false
+ * take part in the walk and get -1.  Falls back to each lane's own search when the tree or a target is
+ * outside the packed range or the list overflows, and to the 64-bit search when a lane's distance was
+ * clamped. */
+__device__ __forceinline__ int tree_search_warp(const MgTreeNode *__restrict__ T, const int32_t *t, bool active,
+                                                WarpTreeScratch &ws) {
+    const unsigned FULL = 0xFFFFFFFFu;
+    RtTarget q{};
+    const bool ok = !active || rt_target(t, q);
+    const unsigned act = __ballot_sync(FULL, active);
+    if (!act) return -1;
+    int n = -1;
+    if (rt_packed(T) && __all_sync(FULL, ok)) {
+        int32_t lo[6], hi[6];
+        for (int k = 0; k < 6; k++) {
+            lo[k] = __reduce_min_sync(FULL, active ? t[k] : 0x7FFFFFFF);
+            hi[k] = __reduce_max_sync(FULL, active ? t[k] : (int32_t)0x80000000);
+        }
+        RtTarget lbq, ubq;
+        for (int k = 0; k < 3; k++) {
+            lbq.p[k] = pack16(lo[2 * k], lo[2 * k + 1]);
+            lbq.n[k] = pack16(-hi[2 * k], -hi[2 * k + 1]);
+            ubq.p[k] = pack16(hi[2 * k], hi[2 * k + 1]);
+            ubq.n[k] = pack16(-lo[2 * k], -lo[2 * k + 1]);
+        }
+        n = warp_tree_candidates(T, lbq, ubq, ws);
+    }
+    if (n >= 0) {
+        const RtState s = rt_scan(T, ws.cand, n, q);
+        __syncwarp(); /* the list is read by every lane before the warp's next walk */
+        if (!active) return -1;
+        if (s.res >= 0 && s.best < (uint32_t)MG_RT_CLAMP * MG_RT_CLAMP) return s.res;
+        uint64_t d;
+        return tree_search_stack(T, t, -1, d);
+    }
+    if (!active) return -1;
+    uint64_t d;
+    return tree_search(T, t, -1, d);
+}
+
 /* (long)(v * 10000f) */
 __device__ __forceinline__ int32_t quantize(float v) { return (int32_t)(int64_t)(v * 10000.0f); }
 

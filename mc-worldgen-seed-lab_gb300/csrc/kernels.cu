@@ -219,8 +219,20 @@ __global__ void __launch_bounds__(128) k_grid(const __grid_constant__ MgWorldDes
     }
     __syncthreads();
     const int ix = tx0 + col, iz = tz0 + row;
-    if (ix >= nx || iz >= nz) return;
+    const bool in = ix < nx && iz < nz;
     const long long g = (long long)iz * nx + ix;
+    if (FM && !CHAIN && DIM == MG_OVERWORLD && W.tree_fanout >= MG_WARP_TREE_FANOUT) { /* one pruned walk per warp */
+        __shared__ WarpTreeScratch wt[4];
+        int32_t tg[6] = {0, 0, 0, 0, 0, 0};
+        if (in) {
+            if (!FM && tab) climate_ow_d_tab(W, *S, T, *tab, col, row, qx0 + ix, qy, qz0 + iz, depth_g, tg);
+            else cell_target<FM, DIM>(W, *S, T, qx0 + ix, qy, qz0 + iz, tg);
+        }
+        const int leaf = tree_search_warp(tree, tg, in, wt[threadIdx.x >> 5]);
+        if (in) out[g] = tree[leaf].biome;
+        return;
+    }
+    if (!in) return;
     int32_t tg[6];
     if (!FM && DIM == MG_OVERWORLD && tab) climate_ow_d_tab(W, *S, T, *tab, col, row, qx0 + ix, qy, qz0 + iz, depth_g, tg);
     else cell_target<FM, DIM>(W, *S, T, qx0 + ix, qy, qz0 + iz, tg);

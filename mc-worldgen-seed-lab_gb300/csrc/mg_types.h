@@ -94,6 +94,7 @@ typedef struct {
     int32_t end_ids[5];            /* the_end, end_highlands, end_midlands, small_end_islands, end_barrens */
     double end_f2, end_g2;         /* 2-D simplex skew 0.5*(sqrt(3)-1) and unskew (3-sqrt(3))/6 */
     int32_t tree_root, tree_nodes, tree_leaves;
+    int32_t tree_fanout;           /* most children of a node (the build's children per node: 6 or 19) */
     MgSpline spline;
 } MgWorldDesc;
 

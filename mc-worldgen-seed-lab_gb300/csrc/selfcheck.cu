@@ -258,6 +258,39 @@ __global__ void k_check_tree(const MgTreeNode *__restrict__ T, long long n, uint
     atomicAdd(&out[1], bad_other);
 }
 
+/* The warp-shared search (tree_search_warp) against the 64-bit stack search on targets of the kind a warp of
+ * neighbouring cells has: per warp a centre in the tables' range and per lane a spread of 50, 400, 2,000 or
+ * 6,000 around it; about one lane in eight inactive; in one warp in sixteen one lane far outside the packed
+ * range (the warp's fallback).  Case i is lane i % 32 of warp case i / 32.  out[0]: differing leaves. */
+__global__ void __launch_bounds__(128) k_check_tree_warp(const MgTreeNode *__restrict__ T, long long n, uint64_t seed,
+                                                         unsigned long long *out) {
+    __shared__ WarpTreeScratch ws[4];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    unsigned long long bad = 0;
+    const long long nw = (n + 31) / 32, step = (long long)gridDim.x * 4;
+    for (long long wc = (long long)blockIdx.x * 4 + wib; wc < nw; wc += step) {
+        uint64_t r = mix64(seed ^ mix64(0x5157ULL ^ (uint64_t)wc));
+        const int spreads[4] = {50, 400, 2000, 6000};
+        const int spread = spreads[r & 3];
+        const bool far_lane = ((r >> 2) & 15) == 0 && lane == 7;
+        uint64_t q = mix64(r ^ (uint64_t)(lane + 1) * 0x9E3779B97F4A7C15ULL);
+        const bool active = wc * 32 + lane < n && (q & 7) != 0;
+        int32_t t[6];
+        for (int k = 0; k < 6; k++) {
+            r = mix64(r);
+            q = mix64(q);
+            const int32_t c = (int32_t)(r % 24001) - 12000;
+            t[k] = far_lane ? (int32_t)(q % 80001) - 40000 : c + (int32_t)(q % (uint64_t)(2 * spread + 1)) - spread;
+        }
+        const int lw = tree_search_warp(T, t, active, ws[wib]);
+        if (active) {
+            uint64_t d;
+            bad += lw != tree_search_stack(T, t, -1, d);
+        }
+    }
+    atomicAdd(&out[0], bad);
+}
+
 }  // namespace
 
 extern "C" MCGEN_API int mcgen_gb300_check_tree(const McWorld *w, long long n, unsigned long long seed, long long *bad_leaf,
@@ -272,6 +305,7 @@ extern "C" MCGEN_API int mcgen_gb300_check_tree(const McWorld *w, long long n, u
     if (cudaMalloc(&d, 2 * sizeof(unsigned long long)) != cudaSuccess) return MCGEN_E_NOMEM;
     cudaMemset(d, 0, 2 * sizeof(unsigned long long));
     k_check_tree<<<152 * 4, 128>>>(w->d_tree, n, seed, d);
+    k_check_tree_warp<<<152 * 4, 128>>>(w->d_tree, n, seed ^ 0xA5A5A5A5ULL, d);
     unsigned long long h[2] = {0, 0};
     cudaError_t e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
     cudaFree(d);

@@ -667,6 +667,8 @@ int build_world(const char *root, int version, int dim, const char *preset, MgWo
     D->tree_root = 0;
     D->tree_nodes = (int)tree->size();
     D->tree_leaves = nleaf;
+    D->tree_fanout = 0;
+    for (const MgTreeNode &n : *tree) D->tree_fanout = std::max(D->tree_fanout, (int32_t)n.count);
     return MCGEN_OK;
 }
 
