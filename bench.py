@@ -566,7 +566,8 @@ BATCH_CLASSES = {
 
 def batch_classes(reqs, worlds, mg, dev, stream) -> dict:
     """Each class's requests as a plan of their own (autotuned), mean of 3 graph runs: where a step's time
-    goes."""
+    goes; and each class at every tile shape (register budget: 0 = 56 registers / 9 CTAs per SM, 1 = 72 / 7,
+    2 = 80 / 6, 3 = 64 / 8), the table behind one shape for the whole batch."""
     import torch
 
     out = {}
@@ -577,16 +578,24 @@ def batch_classes(reqs, worlds, mg, dev, stream) -> dict:
         plan = mg.Plan([(worlds[(v, d)], s, qx0, qz0, n, n, qy) for v, d, s, qx0, qz0, n, qy in sub])
         d_out = torch.empty(plan.output_bytes, dtype=torch.uint8, device=dev)
         plan.autotune(d_out.data_ptr(), reps=1)
-        plan.run_dev(d_out.data_ptr(), stream.cuda_stream)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(3):
+        tuned = plan.shape
+
+        def timed(shape):
+            plan.shape = shape
             plan.run_dev(d_out.data_ptr(), stream.cuda_stream)
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
-        ms = e0.elapsed_time(e1) / 3
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(3):
+                plan.run_dev(d_out.data_ptr(), stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            return e0.elapsed_time(e1) / 3
+
+        per_shape = {str(k): round(timed(k), 3) for k in range(4)}  # every register budget, for the table
+        ms = timed(tuned)
         out[name] = {"requests": len(sub), "samples": plan.output_bytes, "ms": round(ms, 3),
-                     "ns_per_sample": round(ms * 1e6 / plan.output_bytes, 4), "tile_shape": plan.shape}
+                     "ns_per_sample": round(ms * 1e6 / plan.output_bytes, 4), "tile_shape": tuned,
+                     "ms_per_shape": per_shape}
         plan.close()
     return out
 
