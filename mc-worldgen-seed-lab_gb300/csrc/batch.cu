@@ -147,6 +147,7 @@ struct BatchSmem {
         BatchEnd end;
     };
     WarpTreeScratch wt[BNT / 32]; /* each warp's R-tree candidate list (Overworld, ENGINE rule) */
+    PendSink sink;  /* where double-branch Overworld cells left to the exact evaluation are recorded */
     double depth_g; /* the double-branch Overworld tile's depth gradient (depth_grad_d) */
     int tile, req, state;
 };
@@ -157,7 +158,7 @@ template <bool FM, int DIM, int TILE_W>
 __device__ __forceinline__ void batch_cells(const MgWorldDesc &W, const MgSpline &S, const MgLattice *T,
                                             const MgTreeNode *tree, const MgBatchReq &R, int tx0, int tz0,
                                             const ShiftTable<8, BNT / 8> *tab, double g, WarpTreeScratch *wt,
-                                            uint8_t *out) {
+                                            const PendSink *sink, uint8_t *out) {
     const int col = threadIdx.x % TILE_W, row = threadIdx.x / TILE_W;
     const int ix = tx0 + col, iz = tz0 + row;
     const bool in = ix < R.nx && iz < R.nz;
@@ -167,9 +168,13 @@ __device__ __forceinline__ void batch_cells(const MgWorldDesc &W, const MgSpline
         return;
     }
     int32_t tg[6] = {0, 0, 0, 0, 0, 0};
-    if (in) {
-        if (!FM && DIM == MG_OVERWORLD && TILE_W == 8 && tab) climate_ow_d_tab(W, S, T, *tab, col, row, qx, R.qy, qz, g, tg);
-        else cell_target<FM, DIM>(W, S, T, qx, R.qy, qz, tg);
+    const int64_t o = R.out_off + (int64_t)iz * R.nx + ix;
+    if (!FM && DIM == MG_OVERWORLD && TILE_W == 8 && tab) {
+        /* a cell whose screen left a value to the exact evaluation is recorded for the second launch (the
+         * double branch's tree search is per lane, so the lane may leave here) */
+        if (in && !climate_ow_d_tab_defer(W, S, T, *tab, col, row, qx, R.qy, qz, g, tg, sink, o)) return;
+    } else if (in) {
+        cell_target<FM, DIM>(W, S, T, qx, R.qy, qz, tg);
     }
     int leaf;
     /* one pruned walk of the tree per warp of 8 x 4 cells for wide trees (built only into the float branch's
@@ -180,7 +185,7 @@ __device__ __forceinline__ void batch_cells(const MgWorldDesc &W, const MgSpline
         uint64_t d;
         leaf = in ? tree_search(tree, tg, -1, d) : -1;
     }
-    if (in) out[R.out_off + (size_t)iz * R.nx + ix] = tree[leaf].biome;
+    if (in) out[o] = tree[leaf].biome;
 }
 
 /* End tile: chunks [cx0, cx0 + END_TC) x [cz0, cz0 + END_TC) counted from the chunk of the request's
@@ -221,10 +226,16 @@ template <int TILE_W, int MINB>
 __global__ void __launch_bounds__(BNT, MINB) k_batch(const MgWorldDesc *__restrict__ worlds, const MgTreeNode *const *__restrict__ trees,
                                                const MgBatchReq *__restrict__ reqs, int nreq, long long ntiles,
                                                const MgLattice *__restrict__ pool, unsigned long long *__restrict__ counter,
+                                               MgPending *__restrict__ pend, long long pend_cap,
                                                uint8_t *__restrict__ out) {
     extern __shared__ uint4 smem_raw[];
     BatchSmem &sm = *reinterpret_cast<BatchSmem *>(smem_raw);
-    if (threadIdx.x == 0) sm.state = -1;
+    if (threadIdx.x == 0) {
+        sm.state = -1;
+        sm.sink.rec = pend;
+        sm.sink.count = counter + 1;
+        sm.sink.cap = pend ? pend_cap : 0;
+    }
     for (;;) {
         __syncthreads();
         if (threadIdx.x < 32) { /* warp 0 takes the next tile and finds its request */
@@ -235,6 +246,10 @@ __global__ void __launch_bounds__(BNT, MINB) k_batch(const MgWorldDesc *__restri
             if (threadIdx.x == 0) {
                 sm.tile = (int)(r >= 0 ? tile - reqs[r].tile0 : -1);
                 sm.req = r;
+                if (r >= 0) {
+                    sm.sink.world = reqs[r].world;
+                    sm.sink.state = reqs[r].state;
+                }
             }
         }
         __syncthreads();
@@ -269,8 +284,8 @@ __global__ void __launch_bounds__(BNT, MINB) k_batch(const MgWorldDesc *__restri
         const int tx0 = (tile % tw) * TILE_W, tz0 = (tile / tw) * TILE_H;
         const MgTreeNode *tree = trees[R.world];
         if (W.fmode) {
-            if (W.dim == MG_OVERWORLD) batch_cells<true, MG_OVERWORLD, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, 0.0, sm.wt, out);
-            else batch_cells<true, MG_NETHER, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, 0.0, sm.wt, out);
+            if (W.dim == MG_OVERWORLD) batch_cells<true, MG_OVERWORLD, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, 0.0, sm.wt, &sm.sink, out);
+            else batch_cells<true, MG_NETHER, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, 0.0, sm.wt, &sm.sink, out);
         } else if (W.dim == MG_OVERWORLD) {
             /* the tile's shift splits, computed once per column and row (ENGINE rule) */
             const bool tab = TILE_W == 8 && R.tie != MG_TIE_CHUNK_CELL && shift_table_ok(W);
@@ -280,14 +295,36 @@ __global__ void __launch_bounds__(BNT, MINB) k_batch(const MgWorldDesc *__restri
                 __syncthreads();
             }
             batch_cells<false, MG_OVERWORLD, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, tab ? &sm.o.shift : nullptr,
-                                                     tab ? sm.depth_g : 0.0, sm.wt, out);
+                                                     tab ? sm.depth_g : 0.0, sm.wt, &sm.sink, out);
         } else {
-            batch_cells<false, MG_NETHER, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, 0.0, sm.wt, out);
+            batch_cells<false, MG_NETHER, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, 0.0, sm.wt, &sm.sink, out);
         }
     }
 }
 
+/* The recorded cells (MgPending): one thread each, the exact evaluation of the values the screen left, the
+ * climate finish and the R-tree search (the lanes' targets are unrelated), then the cell's output byte. */
+__global__ void __launch_bounds__(128) k_batch_exact(const MgWorldDesc *__restrict__ worlds,
+                                                     const MgTreeNode *const *__restrict__ trees,
+                                                     const MgLattice *__restrict__ pool,
+                                                     const MgPending *__restrict__ pend,
+                                                     const unsigned long long *__restrict__ npend, long long cap,
+                                                     uint8_t *__restrict__ out) {
+    const long long n = min((long long)*npend, cap);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const MgPending P = pend[i];
+        const MgWorldDesc &W = worlds[P.world];
+        int32_t tg[6];
+        pending_targets(W, pool + P.state, P, tg);
+        const MgTreeNode *tree = trees[P.world];
+        uint64_t d;
+        out[P.out] = tree[tree_search_scattered(tree, tg, -1, d)].biome;
+    }
+}
+
 /* ---------------------------------------------------------------- host side */
+long long batch_pending_cap(long long cells) { return cells > 0 ? cells / 256 + 1024 : 0; }
+
 /* tile shapes the autotuner chooses from: tile width, and the register budget (resident CTAs per SM: 9, 7,
  * 6, 8) in k_batch's second template argument */
 const int kBatchTileWidths[BATCH_SHAPES] = {8, 8, 8, 8};
@@ -348,24 +385,33 @@ int batch_prepare(int *ctas_per_sm) {
 
 /* ctas: upper bound on the persistent grid (0: every resident CTA of the shape) */
 int launch_batch(const MgWorldDesc *d_worlds, const MgTreeNode *const *d_trees, const MgBatchReq *d_reqs, int nreq,
-                 long long ntiles, const MgLattice *d_pool, unsigned long long *d_counter, uint8_t *d_out, int ctas,
-                 int shape, cudaStream_t st) {
+                 long long ntiles, const MgLattice *d_pool, unsigned long long *d_counter, MgPending *d_pend,
+                 long long pend_cap, uint8_t *d_out, int ctas, int shape, cudaStream_t st) {
     if (ntiles <= 0) return 0;
     if (shape < 0 || shape >= BATCH_SHAPES || g_resident[shape] <= 0) return (int)cudaErrorInvalidValue;
-    cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st);
+    if (!d_pend) pend_cap = 0;
+    cudaError_t e = cudaMemsetAsync(d_counter, 0, 2 * sizeof(unsigned long long), st);
     if (e) return (int)e;
     int grid = g_resident[shape];
     if (ctas > 0 && ctas < grid) grid = ctas;
     if ((long long)grid > ntiles) grid = (int)ntiles;
-    ProfScope ps_(K_BATCH, st);
     const size_t sm = sizeof(BatchSmem);
-    switch (shape) {
-    case 1: k_batch<8, 7><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
-    case 2: k_batch<8, 6><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
-    case 3: k_batch<8, 8><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
-    default: k_batch<8, 9><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_out); break;
+    {
+        ProfScope ps_(K_BATCH, st);
+        switch (shape) {
+        case 1: k_batch<8, 7><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_pend, pend_cap, d_out); break;
+        case 2: k_batch<8, 6><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_pend, pend_cap, d_out); break;
+        case 3: k_batch<8, 8><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_pend, pend_cap, d_out); break;
+        default: k_batch<8, 9><<<grid, BNT, sm, st>>>(d_worlds, d_trees, d_reqs, nreq, ntiles, d_pool, d_counter, d_pend, pend_cap, d_out); break;
+        }
     }
     count_launch_external();
+    if ((e = cudaGetLastError())) return (int)e;
+    if (pend_cap > 0) { /* the recorded cells; the grid covers the usual count, larger counts loop */
+        ProfScope ps_(K_BATCH_EXACT, st);
+        k_batch_exact<<<2 * 152, 128, 0, st>>>(d_worlds, d_trees, d_pool, d_pend, d_counter + 1, pend_cap, d_out);
+        count_launch_external();
+    }
     return (int)cudaGetLastError();
 }
 

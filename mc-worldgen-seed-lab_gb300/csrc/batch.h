@@ -25,8 +25,11 @@ typedef struct {
 
 #define BATCH_SHAPES 4
 namespace mg {
+/* records to provide for a batch with `cells` double-branch Overworld cells (a bound far above the
+ * measured 1.5-3.5e-4 share of unsettled values; cells beyond it take the exact path in place) */
+long long batch_pending_cap(long long cells);
 /* tile widths of the four Overworld/Nether tile shapes (128 cells each; the shapes also differ in the
- * register budget: 8, 4, 6 and 8 resident CTAs per SM) */
+ * register budget: 9, 7, 6 and 8 resident CTAs per SM) */
 extern const int kBatchTileWidths[BATCH_SHAPES];
 /* tiles of a request: 128 quart cells of shape `shape` (Overworld, Nether) or 8 x 8 chunks (End) */
 long long batch_tiles(int dim, int qx0, int qz0, int nx, int nz, int shape);
@@ -35,9 +38,11 @@ int launch_setup_list(const MgWorldDesc *d_worlds, int dim, const MgSetupEntry *
                       long long total_lattices, MgLattice *d_pool, cudaStream_t st);
 /* kernel attributes and resident grid sizes; call before any stream capture */
 int batch_prepare(int *ctas_per_sm);
-/* ctas: upper bound on the persistent grid, 0 = every resident CTA of the shape */
+/* ctas: upper bound on the persistent grid, 0 = every resident CTA of the shape.  d_counter holds two
+ * counters (tiles taken, cells recorded); with d_pend (pend_cap records) the double-branch Overworld cells
+ * left to the exact evaluation are recorded and finished by a second launch, without it in place. */
 int launch_batch(const MgWorldDesc *d_worlds, const MgTreeNode *const *d_trees, const MgBatchReq *d_reqs, int nreq,
-                 long long ntiles, const MgLattice *d_pool, unsigned long long *d_counter, uint8_t *d_out, int ctas,
-                 int shape, cudaStream_t st);
+                 long long ntiles, const MgLattice *d_pool, unsigned long long *d_counter, MgPending *d_pend,
+                 long long pend_cap, uint8_t *d_out, int ctas, int shape, cudaStream_t st);
 }  // namespace mg
 #endif

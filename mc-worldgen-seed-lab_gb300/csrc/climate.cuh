@@ -105,6 +105,80 @@ static __device__ __noinline__ void climate_ow_d_rest(const MgWorldDesc &W, cons
     ridge_float(W, T, x, z, xc, zc, rvf, rff);
     climate_finish_df(W, S, tf, hf, cf, ef, rvf, rff, g, tg);
 }
+/* Where a batch records the cells whose screened climate left a value to the exact evaluation (MgPending):
+ * the record array, its counter and capacity, and the request's world and lattices. */
+struct PendSink {
+    MgPending *rec;
+    unsigned long long *count;
+    long long cap;
+    int32_t world, state;
+};
+/* climate_ow_d_rest for a batch: the same values, but a cell with a value the screen does not settle is
+ * recorded in the sink (output byte `out`) and false returned, without the exact evaluation; when the sink
+ * is full (or absent) the exact evaluation runs here and the targets are returned as climate_ow_d_rest gives
+ * them. */
+static __device__ __noinline__ bool climate_ow_d_rest_defer(const MgWorldDesc &W, const MgSpline &S,
+                                                            const MgLattice *__restrict__ T, double x, double z,
+                                                            double g, int32_t *tg, const PendSink *sink, int64_t out) {
+    const double xc = x * MG_SECOND_STACK, zc = z * MG_SECOND_STACK;
+    float fv[6];
+    uint32_t pend = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const MgNoise &N = W.noise[1 + k];
+        const int64_t q = N.fix_eq >= 0 ? nn_q<false>(N, T, x, z, xc, zc) : MG_QFAIL;
+        if (q == MG_QFAIL || !cast_settled_q(q, N.fix_eq, fv[k])) pend |= 1u << k;
+    }
+    {
+        const MgNoise &N = W.noise[5];
+        const int64_t q = W.rf_eq >= 0 ? nn_q<false>(N, T, x, z, xc, zc) : MG_QFAIL;
+        if (q == MG_QFAIL || !cast_settled_q(q, N.fix_eq, fv[4]) || !ridges_folded_settled(W, q, fv[5])) pend |= 16u;
+    }
+    if (pend) {
+        const unsigned long long k = sink->cap > 0 ? atomicAdd(sink->count, 1ULL) : ~0ULL;
+        if (k < (unsigned long long)sink->cap) {
+            MgPending &P = sink->rec[k];
+            P.x = x;
+            P.z = z;
+            P.g = g;
+            P.out = out;
+            for (int j = 0; j < 4; j++) P.f[j] = fv[j];
+            P.rv = fv[4];
+            P.rf = fv[5];
+            P.world = sink->world;
+            P.state = sink->state;
+            P.pend = pend;
+            return false;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            if (pend & (1u << j)) fv[j] = (float)nn_d_y0(W.noise[1 + j], T, x, z, xc, zc);
+        if (pend & 16u) {
+            const double rv = nn_d_y0(W.noise[5], T, x, z, xc, zc);
+            fv[4] = (float)rv;
+            fv[5] = (float)ridges_folded_d(W, rv);
+        }
+    }
+    climate_finish_df(W, S, fv[0], fv[1], fv[2], fv[3], fv[4], fv[5], g, tg);
+    return true;
+}
+/* a recorded cell's targets: its settled floats and the exact evaluation of the rest (the values
+ * climate_ow_d_rest computes) */
+__device__ __forceinline__ void pending_targets(const MgWorldDesc &W, const MgLattice *__restrict__ T, const MgPending &P,
+                                                int32_t *tg) {
+    const double xc = P.x * MG_SECOND_STACK, zc = P.z * MG_SECOND_STACK;
+    float fv[6] = {P.f[0], P.f[1], P.f[2], P.f[3], P.rv, P.rf};
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+        if (P.pend & (1u << j)) fv[j] = (float)nn_d_y0(W.noise[1 + j], T, P.x, P.z, xc, zc);
+    if (P.pend & 16u) {
+        const double rv = nn_d_y0(W.noise[5], T, P.x, P.z, xc, zc);
+        fv[4] = (float)rv;
+        fv[5] = (float)ridges_folded_d(W, rv);
+    }
+    climate_finish_df(W, W.spline, fv[0], fv[1], fv[2], fv[3], fv[4], fv[5], P.g, tg);
+}
+
 /* double branch of the Overworld climate, out of line (the kernels reach the climate from two sites each:
  * the cell itself and the tie chain).  The shift noises stay exact in double: their value moves the climate
  * noises' input coordinates, and the kernels' integer pipes (which carry the screened climate noises) are
@@ -203,6 +277,21 @@ __device__ __forceinline__ void climate_ow_d_tab(const MgWorldDesc &W, const MgS
         return;
     }
     climate_ow_d_rest(W, S, T, X + sp.a * 4.0, Z + sp.b * 4.0, g, tg);
+}
+
+/* climate_ow_d_tab with the deferral of climate_ow_d_rest_defer */
+template <int TW, int TH>
+__device__ __forceinline__ bool climate_ow_d_tab_defer(const MgWorldDesc &W, const MgSpline &S,
+                                                       const MgLattice *__restrict__ T, const ShiftTable<TW, TH> &tab,
+                                                       int col, int row, int qx, int qy, int qz, double g, int32_t *tg,
+                                                       const PendSink *sink, int64_t out) {
+    const ShiftPair sp = shift_from_table(W.noise[0], T, tab, col, row);
+    const double X = (double)qx, Z = (double)qz;
+    if (!sp.ok) {
+        climate_ow_d(W, S, T, X, Z, X * MG_SECOND_STACK, Z * MG_SECOND_STACK, qy * 4, tg);
+        return true;
+    }
+    return climate_ow_d_rest_defer(W, S, T, X + sp.a * 4.0, Z + sp.b * 4.0, g, tg, sink, out);
 }
 
 /* Overworld climate of quart cell (qx, qy, qz) -> 6 quantised targets (engine/mc_climate.h:113-170). */

@@ -123,6 +123,22 @@ typedef struct __attribute__((aligned(16))) {
     uint8_t p[256];
 } MgLattice;
 
+/* A double-branch Overworld cell whose screened climate left a value to the exact double evaluation
+ * (about one cell in a thousand): the batch kernel records it here instead of running that evaluation inside
+ * a warp whose other lanes would wait for it, and a second kernel finishes the recorded cells densely, one per
+ * thread.  72 bytes. */
+typedef struct {
+    double x, z;      /* the climate noises' input: the cell's shifted coordinates */
+    double g;         /* depth gradient at the cell's y */
+    int64_t out;      /* output byte of the cell */
+    float f[4];       /* temperature, vegetation, continentalness, erosion: the settled floats */
+    float rv, rf;     /* ridge and ridges_folded floats, when settled */
+    int32_t world;    /* index into the batch's world table */
+    int32_t state;    /* first lattice of its seed in the state pool */
+    uint32_t pend;    /* bit k < 4: climate noise k + 1 unsettled; bit 4: the ridge (with ridges_folded) */
+    int32_t pad;
+} MgPending;
+
 /* One seed-search observation (the reference's McgObs, engine/cuda/mc_gpu.cuh:47-54): a quart cell, or a
  * block resolved through BiomeManager's zoom when flags has MG_OBS_BLOCK; flags' low byte is the End window
  * half-width; the biomes that satisfy it as a 128-bit mask.  32 bytes. */

@@ -39,7 +39,9 @@ struct McGb300Plan {
     int *d_first = nullptr; /* Overworld: first lattice of each entry, relative to the Overworld list */
     long long ow_lattices = 0;
     MgLattice *d_pool = nullptr;
-    unsigned long long *d_counter = nullptr;
+    unsigned long long *d_counter = nullptr; /* tiles taken, cells recorded for the exact pass */
+    MgPending *d_pend = nullptr;             /* records of double-branch Overworld cells left to the exact pass */
+    long long pend_cap = 0;
     /* graph of one run */
     cudaStream_t cap = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -93,7 +95,7 @@ int enqueue(McGb300Plan *p, uint8_t *d_out, int shape, cudaStream_t st) {
         if (rc) return rc;
     }
     return mg::launch_batch(p->d_worlds, p->d_trees, p->d_reqs[shape], p->nreq, p->ntiles[shape], p->d_pool,
-                            p->d_counter, d_out, p->ctas, shape, st);
+                            p->d_counter, p->d_pend, p->pend_cap, d_out, p->ctas, shape, st);
 }
 
 /* Order a run on `st` after the plan's previous run (on any stream); caller holds the ABI lock. */
@@ -192,6 +194,12 @@ MCGEN_API int mcgen_gb300_plan_new(const McGb300Request *reqs, int n, int tie_ru
         off += p->cells[(size_t)i];
     }
     p->out_bytes = off;
+    long long dcells = 0; /* double-branch Overworld cells: the ones the exact pass may take */
+    for (int i = 0; i < n; i++) {
+        const MgWorldDesc &W = worlds[(size_t)wof[(size_t)i]]->desc;
+        if (W.dim == MG_OVERWORLD && !W.fmode) dcells += p->cells[(size_t)i];
+    }
+    p->pend_cap = tie_rule == MCGEN_TIE_ENGINE ? mg::batch_pending_cap(dcells) : 0;
     /* processing order: requests grouped by world, heaviest code path first (Overworld double branch, then
      * float, Nether, End), so that the CTAs resident at any time run the same code (the kernel holds every
      * dimension and branch; mixing them thrashes the instruction cache) and the light tiles come last */
@@ -247,10 +255,12 @@ MCGEN_API int mcgen_gb300_plan_new(const McGb300Request *reqs, int n, int tie_ru
     for (const Part &q : parts) memcpy(host.data() + q.off, q.src, q.bytes);
     const size_t pool_off = (at + 255) & ~(size_t)255;
     const size_t counter_off = pool_off + sizeof(MgLattice) * (size_t)pool;
+    const size_t pend_off = counter_off + 2 * sizeof(unsigned long long);
+    const size_t arena_bytes = pend_off + sizeof(MgPending) * (size_t)p->pend_cap;
     cudaMemPool_t mp = nullptr;
     cudaStream_t ast = mg::abi_stream();
     cudaError_t e = plan_pool(&mp);
-    if (!e) e = cudaMallocFromPoolAsync(&p->d_arena, counter_off + sizeof(unsigned long long), mp, ast);
+    if (!e) e = cudaMallocFromPoolAsync(&p->d_arena, arena_bytes, mp, ast);
     if (!e && staged) e = cudaMemcpyAsync(p->d_arena, host.data(), staged, cudaMemcpyHostToDevice, ast);
     if (!e) e = cudaStreamSynchronize(ast); /* the arena is ready for any stream */
     if (!e) {
@@ -258,6 +268,7 @@ MCGEN_API int mcgen_gb300_plan_new(const McGb300Request *reqs, int n, int tie_ru
         for (const Part &q : parts) *q.dst = base + q.off;
         if (pool) p->d_pool = (MgLattice *)(base + pool_off);
         p->d_counter = (unsigned long long *)(base + counter_off);
+        if (p->pend_cap) p->d_pend = (MgPending *)(base + pend_off);
         p->h2d_bytes = (long long)staged;
     }
     if (!e) e = (cudaError_t)mg::batch_prepare(nullptr);

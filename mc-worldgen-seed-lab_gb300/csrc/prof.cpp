@@ -23,7 +23,7 @@ const char *kernel_name(int kid) {
     static const char *const n[K_NUM_KERNELS] = {"k_setup_xo", "k_setup_legacy", "k_setup_end", "k_points", "k_grid",
                                                  "k_chain_resolve", "k_blockgrid", "k_end_chunks", "k_end_lookup",
                                                  "k_ow_seed_climate", "k_ow_finish_tree", "k_batch", "k_search_cells",
-                                                 "k_ow_search_first", "k_search_rest", "k_density"};
+                                                 "k_ow_search_first", "k_search_rest", "k_density", "k_batch_exact"};
     return (kid >= 0 && kid < K_NUM_KERNELS) ? n[kid] : "?";
 }
 

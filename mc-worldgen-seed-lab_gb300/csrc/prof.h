@@ -12,7 +12,7 @@ namespace mg {
 enum {
     K_SETUP_XO = 0, K_SETUP_LEGACY, K_SETUP_END, K_POINTS, K_GRID, K_CHAIN_RESOLVE, K_BLOCKGRID, K_END_CHUNKS,
     K_END_LOOKUP, K_OW_SEED_CLIMATE, K_OW_FINISH_TREE, K_BATCH, K_SEARCH_CELLS, K_SEARCH_FIRST, K_SEARCH_REST,
-    K_DENSITY, K_NUM_KERNELS
+    K_DENSITY, K_BATCH_EXACT, K_NUM_KERNELS
 };
 const char *kernel_name(int kid);
 void prof_mark(int kid, cudaStream_t st, bool end);

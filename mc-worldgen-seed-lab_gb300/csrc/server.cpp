@@ -78,7 +78,8 @@ struct Batch {
     const MgTreeNode **d_trees = nullptr;
     uint8_t *d_out = nullptr; size_t cap_out = 0;
     uint8_t *h_out = nullptr; size_t cap_hout = 0;
-    unsigned long long *d_counter = nullptr;
+    unsigned long long *d_counter = nullptr; /* tiles taken, cells recorded for the exact pass */
+    MgPending *d_pend = nullptr; size_t cap_pend = 0;
     std::vector<long long> out_off;
 };
 
@@ -277,7 +278,14 @@ int launch_batch(McGb300Server *s, Batch &b) {
         e = cudaMallocHost((void **)&b.h_out, c);
         b.cap_hout = e ? 0 : c;
     }
-    if (!e && !b.d_counter) e = cudaMalloc(&b.d_counter, sizeof(unsigned long long));
+    if (!e && !b.d_counter) e = cudaMalloc(&b.d_counter, 2 * sizeof(unsigned long long));
+    long long dcells = 0; /* double-branch Overworld cells: the ones the exact pass may take */
+    for (const auto &r : reqs) {
+        const MgWorldDesc &W = worlds[(size_t)r.world]->desc;
+        if (W.dim == MG_OVERWORLD && !W.fmode) dcells += (long long)r.nx * r.nz;
+    }
+    const long long pend_cap = mg::batch_pending_cap(dcells);
+    if (!e && pend_cap > 0) e = grow_dev(&b.d_pend, &b.cap_pend, (size_t)pend_cap);
     if (e) return crc(e);
     if (s->fail_next) { /* injected failure of this step (tests of the failure path) */
         const int f = s->fail_next;
@@ -309,7 +317,7 @@ int launch_batch(McGb300Server *s, Batch &b) {
     for (int k : wait_on)
         if ((e = cudaStreamWaitEvent(st, s->batches[(size_t)k].setup_done, 0))) return crc(e);
     int rc = mg::launch_batch(b.d_worlds, b.d_trees, b.d_reqs, (int)reqs.size(), tiles, s->pool[0].base, b.d_counter,
-                              b.d_out, 0, kServeShape, st);
+                              pend_cap > 0 ? b.d_pend : nullptr, pend_cap, b.d_out, 0, kServeShape, st);
     if (rc) return MCGEN_E_INTERNAL;
     if ((e = cudaMemcpyAsync(b.h_out, b.d_out, (size_t)out, cudaMemcpyDeviceToHost, st))) return crc(e);
     if ((e = cudaEventRecord(b.done, st))) return crc(e);
@@ -484,6 +492,7 @@ MCGEN_API void mcgen_gb300_server_free(McGb300Server *s) {
         cudaFree(b.d_out);
         cudaFreeHost(b.h_out);
         cudaFree(b.d_counter);
+        cudaFree(b.d_pend);
     }
     cudaFree(s->pool[0].base);
     delete s;
