@@ -510,8 +510,8 @@ def run_batch(args, rank, world, local_rank, mg, ge):
            "vs_baseline": None, "dtype": "f32+f64+int64", "data": "synthetic (SplitMix64(3) requests)",
            "config": {"workload": f"uneven mixed batch: {len(reqs)} SplitMix64(3) requests, versions 26.1/26.2/26.3, "
                                   "Overworld:Nether:End 6:2:2, square side log-uniform in [16,512) quart cells, origin "
-                                  "uniform in [-30000,30000] blocks, y=64, ENGINE tie rule; one persistent launch "
-                                  "(CUDA graph) vs one plain launch pair per request",
+                                  "uniform in [-30000,30000] blocks, y=64, ENGINE tie rule",
+                      "form": "one persistent launch (CUDA graph) vs one plain launch pair per request",
                       "requests": len(reqs), "samples_per_step": samples, "tile_shape": plan.shape,
                       "autotune_ms": round(tuned_ms, 3), "l2": f"output {samples/1e6:.0f} MB per step > L2",
                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
@@ -668,89 +668,68 @@ def zipf_table(n: int = 50000, s: float = 1.1) -> np.ndarray:
     return np.cumsum(w) / w.sum()
 
 
-def config5_stream(rate: float, duration: float, state: int = 4, nseeds: int = 50000):
+def config5_stream(rate: float, duration: float, state: int = 4, nseeds: int = 50000) -> dict:
     """Open-loop Poisson arrivals at `rate` per second for `duration` s (SplitMix64(state), seven draws per
     request: exponential gap, Zipf(1.1) rank over nseeds seeds (drawn from SplitMix64(state + 100)), then
-    version, dimension, side, x, z as in the uneven batch).  Returns (arrival time, request) pairs."""
+    version, dimension, side, x, z as in the uneven batch).  Returns arrays: t (arrival, s), seed, version
+    and dimension (indices into C4_VERSIONS and C4_DIMS), side, qx0, qz0 (quart cells), qy."""
     seeds = splitmix64(state + 100, nseeds).view(np.int64)
     cdf = zipf_table(nseeds)
     est = int(rate * duration * 1.2) + 64
     r = splitmix64(state, 7 * est).reshape(est, 7)
-    t = 0.0
-    out = []
-    for i in range(est):
-        u = float(r[i, 0] >> np.uint64(11)) * 2.0 ** -53
-        t += -np.log1p(-u) / rate
-        if t >= duration:
-            break
-        rank = int(np.searchsorted(cdf, float(r[i, 1] >> np.uint64(11)) * 2.0 ** -53, side="right"))
-        seed = int(seeds[min(rank, nseeds - 1)])
-        version = C4_VERSIONS[int(r[i, 2] % np.uint64(3))]
-        dim = C4_DIMS[int(r[i, 3] % np.uint64(10))]
-        side = int(16.0 * 32.0 ** (float(r[i, 4] >> np.uint64(11)) * 2.0 ** -53))
-        x = -30000 + int(r[i, 5] % np.uint64(60001))
-        z = -30000 + int(r[i, 6] % np.uint64(60001))
-        out.append((t, (version, dim, seed, x >> 2, z >> 2, side, 16)))
-    return out
+    unit = lambda c: (r[:, c] >> np.uint64(11)).astype(np.float64) * 2.0 ** -53  # noqa: E731
+    t = np.cumsum(-np.log1p(-unit(0)) / rate)
+    n = int(np.searchsorted(t, duration, side="left"))
+    rank = np.minimum(np.searchsorted(cdf, unit(1), side="right"), nseeds - 1)
+    side = np.floor(16.0 * np.power(32.0, unit(4))).astype(np.int64)
+    x = -30000 + (r[:, 5] % np.uint64(60001)).astype(np.int64)
+    z = -30000 + (r[:, 6] % np.uint64(60001)).astype(np.int64)
+    return {"t": t[:n], "seed": seeds[rank[:n]], "version": (r[:n, 2] % np.uint64(3)).astype(np.int64),
+            "dim": (r[:n, 3] % np.uint64(10)).astype(np.int64), "side": side[:n], "qx0": x[:n] >> 2,
+            "qz0": z[:n] >> 2, "qy": 16}
+
+
+def stream_request(stream: dict, i: int):
+    """Request i of a stream as (version, dimension, seed, qx0, qz0, side, qy)."""
+    return (C4_VERSIONS[stream["version"][i]], C4_DIMS[stream["dim"][i]], int(stream["seed"][i]),
+            int(stream["qx0"][i]), int(stream["qz0"][i]), int(stream["side"][i]), stream["qy"])
 
 
 def serve_run(mg, worlds, stream, budget: int, max_inflight: int = 2, keep_every: int = 0):
-    """Replay an arrival stream against a server: a submitter keeps the schedule, a collector waits.
-    Latency is counted from each request's scheduled arrival (open loop: a submitter that falls behind the
-    schedule adds to the latency instead of hiding it); the server's own submit-to-completion figure is
-    reported beside it.  keep_every > 0 keeps every keep_every-th request's ids for a parity check."""
-    import threading
-
+    """Replay an arrival stream against a server with the library's native open-loop load generator
+    (mcgen_gb300_server_replay: a native submitter thread keeps the schedule, latency runs from each request's
+    scheduled arrival).  Ids go to a ring of output slots; with keep_every > 0 every keep_every-th request
+    gets a slot of its own and its ids are returned for a parity check."""
+    n = len(stream["t"])
+    keys = [(v, d) for v in C4_VERSIONS for d in C4_DIMS]
+    uniq = sorted(set(keys))
+    wlist = [worlds[k] for k in uniq]
+    kidx = np.array([uniq.index((C4_VERSIONS[v], C4_DIMS[d])) for v in range(3) for d in range(10)], np.int64)
+    widx = kidx[stream["version"] * 10 + stream["dim"]]
+    side = stream["side"]
+    reqs = mg.RequestArray.from_index(wlist, widx, stream["seed"], stream["qx0"], stream["qz0"], side, side,
+                                      stream["qy"])
+    slot, ring = 512 * 512, 2048
+    kept_idx = np.arange(0, n, keep_every) if keep_every else np.zeros(0, np.int64)
+    off = (np.arange(n) % ring) * slot
+    off[kept_idx] = (ring + np.arange(kept_idx.size)) * slot
+    out = np.empty((ring + kept_idx.size) * slot, np.uint8)
     srv = mg.Server(hbm_budget_bytes=budget, max_inflight=max_inflight)
-    tickets = []  # (ticket, scheduled arrival, submit time) in perf_counter seconds
-    lat, lat_sub, kept = [], [], []
-    samples = 0
-    done = threading.Event()
-
-    def collector():
-        i = 0
-        while True:
-            while i >= len(tickets):
-                if done.is_set() and i >= len(tickets):
-                    return
-                time.sleep(0.0002)
-            t, sched, sub = tickets[i]
-            ids, ms = srv.wait(t)  # ms: submit to completion, measured by the server
-            lat.append((sub - sched) * 1e3 + ms)
-            lat_sub.append(ms)
-            if keep_every and i % keep_every == 0:
-                kept.append((i, ids.copy()))
-            i += 1
-
-    col = threading.Thread(target=collector)
-    col.start()
-    t0 = time.perf_counter()
-    lag = 0.0
-    for at, (v, d, s, qx0, qz0, n, qy) in stream:
-        now = time.perf_counter() - t0
-        if at > now:
-            time.sleep(at - now)
-        sub = time.perf_counter()
-        lag = max(lag, sub - t0 - at)
-        tickets.append((srv.submit(worlds[(v, d)], s, qx0, qz0, n, n, qy), t0 + at, sub))
-        samples += n * n
-    done.set()
-    col.join()
-    elapsed = time.perf_counter() - t0
+    lat, elapsed = srv.replay(reqs, stream["t"], out, off)
     st = srv.stats()
     srv.close()
-    lat_a, lat_s = np.array(lat), np.array(lat_sub)
+    samples = int((side * side).sum())
     looks = st["cache_hits"] + st["cache_misses"]
-    res = {"requests": len(stream), "elapsed_s": round(elapsed, 3), "achieved_rps": round(len(stream) / elapsed, 1),
-           "samples_per_s": samples / elapsed, "p50_ms": round(float(np.percentile(lat_a, 50)), 3),
-           "p99_ms": round(float(np.percentile(lat_a, 99)), 3), "max_ms": round(float(lat_a.max()), 3),
-           "latency_from": "scheduled arrival",
-           "p50_from_submit_ms": round(float(np.percentile(lat_s, 50)), 3),
-           "p99_from_submit_ms": round(float(np.percentile(lat_s, 99)), 3),
-           "max_submit_lag_ms": round(lag * 1e3, 3),
+    res = {"requests": n, "elapsed_s": round(elapsed, 3), "achieved_rps": round(n / elapsed, 1),
+           "samples_per_s": samples / elapsed, "p50_ms": round(float(np.percentile(lat, 50)), 3),
+           "p99_ms": round(float(np.percentile(lat, 99)), 3), "max_ms": round(float(lat.max()), 3),
+           "latency_from": "scheduled arrival (native open-loop submitter)",
            "cache_hit_rate": round(st["cache_hits"] / max(1, looks), 4), "cache_evictions": st["cache_evictions"],
            "batches": st["batches"], "mean_batch": round(st["requests_admitted"] / max(1, st["batches"]), 2)}
-    return (res, kept) if keep_every else res
+    if not keep_every:
+        return res
+    kept = [(int(i), out[off[i]:off[i] + side[i] * side[i]].reshape(side[i], side[i]).copy()) for i in kept_idx]
+    return res, kept
 
 
 def serve_parity(stream, kept) -> tuple[dict, dict]:
@@ -762,7 +741,7 @@ def serve_parity(stream, kept) -> tuple[dict, dict]:
     cores = os.cpu_count() or 1
     wl, mism, cmp_, dt = {}, 0, 0, 0.0
     for i, ids in kept:
-        v, d, s, qx0, qz0, n, qy = stream[i][1]
+        v, d, s, qx0, qz0, n, qy = stream_request(stream, i)
         if (v, d) not in wl:
             wl[(v, d)] = O.World(ge.data_root(), v, d.split(":")[1])
         t0 = time.perf_counter()
@@ -1085,7 +1064,7 @@ def run_serve(args, rank, world, local_rank, mg, ge):
             stream = config5_stream(rate, args.duration)
             if k == len(rates) - 1 and not args.skip_extras:
                 runs[str(int(rate))], kept = serve_run(mg, worlds, stream, 8 << 30, args.inflight,
-                                                       keep_every=max(1, len(stream) // 200))
+                                                       keep_every=max(1, len(stream["t"]) // 200))
                 top_stream = stream
             else:
                 runs[str(int(rate))] = serve_run(mg, worlds, stream, 8 << 30, args.inflight)

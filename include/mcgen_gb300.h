@@ -129,6 +129,12 @@ MCGEN_API int mcgen_gb300_server_submit(McGb300Server *s, const McGb300Request *
  * request keeps its world alive until it completes (mcgen_world_free meanwhile only marks the world). */
 MCGEN_API int mcgen_gb300_server_wait(McGb300Server *s, long long ticket, int timeout_ms, double *latency_ms);
 MCGEN_API int mcgen_gb300_server_stats(McGb300Server *s, McGb300ServerStats *out);
+/* Measurement hook (a load generator for the served form): replay an open-loop arrival schedule -- request i
+ * submitted by a native thread at arrival_s[i] seconds after the call starts, its ids into out + out_off[i]
+ * -- and wait for every ticket; latency_ms[i] runs from the scheduled arrival to completion (a submitter
+ * behind schedule adds to it).  *elapsed_s: the whole replay.  The first error is returned. */
+MCGEN_API int mcgen_gb300_server_replay(McGb300Server *s, const McGb300Request *reqs, const double *arrival_s, int n,
+                                        uint8_t *out, const long long *out_off, double *latency_ms, double *elapsed_s);
 /* Testing aid: the next batch the server forms fails at its device-allocation step with `code` (> 0), as if
  * that allocation had failed; host-side only, no device fault. */
 MCGEN_API int mcgen_gb300_server_fail_next(McGb300Server *s, int code);

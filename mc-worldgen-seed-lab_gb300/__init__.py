@@ -126,6 +126,7 @@ _PROTOS.update({
     "mcgen_gb300_server_wait": (C.c_int, [_P, C.c_longlong, C.c_int, C.POINTER(C.c_double)]),
     "mcgen_gb300_server_stats": (C.c_int, [_P, _P]),
     "mcgen_gb300_server_fail_next": (C.c_int, [_P, C.c_int]),
+    "mcgen_gb300_server_replay": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, _P, _P]),
     "mcgen_gb300_density_values": (C.c_int, [_P, C.c_int64, C.c_int, _P, _P]),
     "mcgen_gb300_seed_points_noalloc": (C.c_int, [_P, _P, C.c_int, _P, C.c_int, _P, _P, _P]),
 })
@@ -514,6 +515,15 @@ class RequestArray:
     def __len__(self):
         return len(self.records)
 
+    @classmethod
+    def from_index(cls, worlds, world_index, seeds, qx0, qz0, nx, nz, qy=16) -> "RequestArray":
+        """Requests whose world is worlds[world_index[i]] (a few worlds, many requests)."""
+        handles = np.array([_handle_int(w) for w in worlds], np.uint64)
+        ra = cls(worlds[0], seeds, qx0, qz0, nx, nz, qy)
+        ra.worlds = list(worlds)
+        ra.records["world"] = handles[np.asarray(world_index, np.int64)]
+        return ra
+
 
 def _handle_int(w) -> int:
     """A world's McWorld* as an integer (0 for a closed world, which the library rejects with E_ARG)."""
@@ -649,6 +659,21 @@ class Server:
         lat = C.c_double()
         _check(load().mcgen_gb300_server_wait(self._h, ticket, timeout_ms, C.byref(lat)), "mcgen_gb300_server_wait")
         return self._keep.pop(ticket), lat.value
+
+    def replay(self, requests: "RequestArray", arrival_s, out: np.ndarray, out_off) -> tuple[np.ndarray, float]:
+        """Open-loop replay of an arrival schedule from a native submitter thread: (latency from each
+        request's scheduled arrival in ms, elapsed seconds).  Request i's ids go to out[out_off[i]:]."""
+        arr = np.ascontiguousarray(arrival_s, np.float64)
+        off = np.ascontiguousarray(out_off, np.int64)
+        n = len(requests)
+        if arr.size != n or off.size != n:
+            raise ValueError("one arrival time and one output offset per request")
+        lat = np.zeros(n, np.float64)
+        el = C.c_double()
+        rec = requests.records
+        _check(load().mcgen_gb300_server_replay(self._h, rec.ctypes.data_as(_P), _ptr(arr), n, _ptr(out), _ptr(off),
+                                                _ptr(lat), C.byref(el)), "mcgen_gb300_server_replay")
+        return lat, el.value
 
     def fail_next(self, code: int) -> None:
         """Testing aid: the next batch fails at its allocation step with `code` (host-side injection)."""

@@ -27,12 +27,15 @@
 
 namespace mg {
 
-#define FNT 192 /* threads per CTA: 4 seeds x 46 lattices */
+/* threads per CTA: 4 seeds x 46 lattices, no idle thread, so that the float branch's shared memory (55.8 KB:
+ * 4 x 46 permutations of 256 B, the chunk's octave values and offset headers) fits 4 CTAs per SM; the
+ * double branch's (62.3 KB, values in double) fits 3 */
+#define FNT 184
 #define FNPC 8  /* points per chunk */
 #define FMAXT 48 /* lattices per seed this kernel supports */
 
 #define FMAXS 4  /* seeds per CTA at 46 lattices per seed */
-#define FMAXOFF 32 /* offset-noise lattices per CTA (6 per seed) */
+#define FMAXOFF 24 /* offset-noise lattices per CTA (6 per seed) */
 
 /* header of an offset-noise lattice, shared so that any thread can sample it */
 struct OffHdr {
@@ -306,6 +309,8 @@ static int search_first_t(const MgWorldDesc &W, const MgTreeNode *tree, const in
     typedef typename std::conditional<FM, float, double>::type V;
     const size_t sm = sizeof(FusedSmem<V>);
     cudaError_t e = cudaFuncSetAttribute(k_ow_seed_climate<FM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (!e) e = cudaFuncSetAttribute(k_ow_seed_climate<FM>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxShared); /* room for 4 CTAs per SM */
     if (e) return (int)e;
     const int spc = FNT / W.ntables;
     V *clim = (V *)scratch;
@@ -347,6 +352,8 @@ static int fused_t(const MgWorldDesc &W, const MgTreeNode *tree, const int64_t *
     typedef typename std::conditional<FM, float, double>::type V;
     const size_t sm = sizeof(FusedSmem<V>);
     cudaError_t e = cudaFuncSetAttribute(k_ow_seed_climate<FM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (!e) e = cudaFuncSetAttribute(k_ow_seed_climate<FM>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxShared); /* room for 4 CTAs per SM */
     if (e) return (int)e;
     const int spc = FNT / W.ntables;
     V *clim = (V *)scratch;

@@ -23,6 +23,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -541,6 +542,56 @@ MCGEN_API int mcgen_gb300_server_wait(McGb300Server *s, long long ticket, int ti
     const int err = T.state == 3 ? (T.err ? T.err : MCGEN_E_INTERNAL) : MCGEN_OK;
     s->tickets.erase(it);
     return err;
+}
+
+/* Open-loop replay of an arrival schedule (a load generator for measuring the served form): a native thread
+ * submits request i at t0 + arrival_s[i] (sleeping until shortly before, then spinning), the calling thread
+ * waits for the tickets in order; latency_ms[i] runs from the scheduled arrival to the completion the server
+ * records, so a submitter behind schedule adds to the latency instead of hiding it. */
+MCGEN_API int mcgen_gb300_server_replay(McGb300Server *s, const McGb300Request *reqs, const double *arrival_s, int n,
+                                        uint8_t *out, const long long *out_off, double *latency_ms, double *elapsed_s) {
+    if (!s || n < 0 || (n > 0 && (!reqs || !arrival_s || !out || !out_off || !latency_ms))) return MCGEN_E_ARG;
+    std::vector<long long> tk((size_t)n, -1);
+    std::vector<Clock::time_point> sub((size_t)n);
+    std::atomic<int> submitted{0};
+    std::atomic<bool> done{false};
+    std::atomic<int> sub_err{0};
+    const auto t0 = Clock::now();
+    auto due_of = [&](int i) {
+        return t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(arrival_s[i]));
+    };
+    std::thread submitter([&] {
+        for (int i = 0; i < n; i++) {
+            const auto due = due_of(i);
+            const auto early = due - std::chrono::microseconds(80);
+            if (Clock::now() < early) std::this_thread::sleep_until(early);
+            while (Clock::now() < due) {
+            }
+            sub[(size_t)i] = Clock::now();
+            long long t = -1;
+            const int rc = mcgen_gb300_server_submit(s, &reqs[i], out + out_off[i], &t);
+            tk[(size_t)i] = rc ? -1 : t;
+            submitted.store(i + 1, std::memory_order_release);
+            if (rc) {
+                sub_err = rc;
+                break;
+            }
+        }
+        done.store(true, std::memory_order_release);
+    });
+    int rc_all = 0;
+    for (int i = 0; i < n; i++) {
+        while (submitted.load(std::memory_order_acquire) <= i && !done.load(std::memory_order_acquire))
+            std::this_thread::yield();
+        if (submitted.load(std::memory_order_acquire) <= i || tk[(size_t)i] < 0) break; /* the submitter stopped */
+        double ms = 0.0;
+        const int rc = mcgen_gb300_server_wait(s, tk[(size_t)i], -1, &ms);
+        if (rc && !rc_all) rc_all = rc;
+        latency_ms[i] = std::chrono::duration<double, std::milli>(sub[(size_t)i] - due_of(i)).count() + ms;
+    }
+    submitter.join();
+    if (elapsed_s) *elapsed_s = std::chrono::duration<double>(Clock::now() - t0).count();
+    return sub_err ? sub_err.load() : rc_all;
 }
 
 MCGEN_API int mcgen_gb300_server_fail_next(McGb300Server *s, int code) {

@@ -176,3 +176,29 @@ def test_world_freed_while_served(env):
         ids, _ = srv.wait(srv.submit(w2, 77 + i, 100, -50, 40, 40, 16))
         assert np.array_equal(ids, lb.quart_grid(77 + i, 100, -50, 40, 40, 16, O.TIE_ENGINE))
     srv.close()
+
+
+def test_native_replay(env):
+    """mcgen_gb300_server_replay: an open-loop schedule replayed by the library's native submitter; every
+    request's ids equal the oracle's, latencies (from each scheduled arrival) are positive."""
+    mg, gens, worlds = env
+    rng = np.random.default_rng(17)
+    n = 60
+    keys = sorted(worlds)
+    wi = rng.integers(0, len(keys), n)
+    seeds = rng.integers(-2**62, 2**62, n)
+    side = rng.integers(4, 40, n)
+    qx0, qz0 = rng.integers(-3000, 3000, n), rng.integers(-3000, 3000, n)
+    arrival = np.cumsum(rng.exponential(1 / 3000.0, n))
+    reqs = mg.RequestArray.from_index([worlds[k] for k in keys], wi, seeds, qx0, qz0, side, side, 16)
+    off = np.concatenate([[0], np.cumsum(side * side)[:-1]])
+    out = np.zeros(int((side * side).sum()), np.uint8)
+    srv = mg.Server(hbm_budget_bytes=64 << 20, max_inflight=2)
+    lat, elapsed = srv.replay(reqs, arrival, out, off)
+    srv.close()
+    assert lat.shape == (n,) and (lat > 0).all() and elapsed >= arrival[-1]
+    for i in range(n):
+        v, d = keys[wi[i]]
+        exp = O.World(ge.data_root(), v, d.split(":")[1]).quart_grid(int(seeds[i]), int(qx0[i]), int(qz0[i]),
+                                                                     int(side[i]), int(side[i]), 16, O.TIE_ENGINE)
+        assert np.array_equal(out[off[i]:off[i] + side[i] ** 2].reshape(side[i], side[i]), exp), i
