@@ -407,6 +407,8 @@ def run_batch(args, rank, world, local_rank, mg, ge):
 
     dev = torch.device("cuda", local_rank)
     reqs = config4_requests(args.requests)
+    if args.batch_class:  # profiling one code path: only that class's requests
+        reqs = [r for r in reqs if class_of(r[0], r[1]) == args.batch_class]
     gens = {v: mg.Generator.open(ge.data_root(), v) for v in C4_VERSIONS}
     worlds = {(v, d): gens[v].world(d, "normal", 0) for v in C4_VERSIONS for d in set(C4_DIMS)}
     plan = mg.Plan([(worlds[(v, d)], s, qx0, qz0, n, n, qy) for v, d, s, qx0, qz0, n, qy in reqs])
@@ -512,6 +514,7 @@ def run_batch(args, rank, world, local_rank, mg, ge):
                                   "Overworld:Nether:End 6:2:2, square side log-uniform in [16,512) quart cells, origin "
                                   "uniform in [-30000,30000] blocks, y=64, ENGINE tie rule",
                       "form": "one persistent launch (CUDA graph) vs one plain launch pair per request",
+                      **({"class_only": args.batch_class} if args.batch_class else {}),
                       "requests": len(reqs), "samples_per_step": samples, "tile_shape": plan.shape,
                       "autotune_ms": round(tuned_ms, 3), "l2": f"output {samples/1e6:.0f} MB per step > L2",
                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
@@ -1306,6 +1309,9 @@ def main():
     ap.add_argument("--no-configs", action="store_true",
                     help="batch10k: the headline only, without the other configurations")
     ap.add_argument("--requests", type=int, default=10000, help="batch10k: number of requests")
+    ap.add_argument("--class", dest="batch_class", choices=["overworld_double", "overworld_float", "nether_double",
+                                                            "nether_float", "end"], default=None,
+                    help="batch10k: only the requests of one code-path class (profiling)")
     ap.add_argument("--split-classes", action="store_true",
                     help="batch10k: also time each code-path class's requests as a plan of their own")
     ap.add_argument("--cpu-sample-s", type=float, default=12.0)

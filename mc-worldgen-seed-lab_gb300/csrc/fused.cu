@@ -27,31 +27,47 @@
 
 namespace mg {
 
-/* threads per CTA: 4 seeds x 46 lattices, no idle thread, so that the float branch's shared memory (55.8 KB:
- * 4 x 46 permutations of 256 B, the chunk's octave values and offset headers) fits 4 CTAs per SM; the
- * double branch's (62.3 KB, values in double) fits 3 */
+/* threads per CTA: 4 seeds x 46 lattices, no idle thread, so that the float branch's shared memory (55.9 KB:
+ * 64 permutation rows of FPS words, the chunk's octave values, offset headers) fits 4 CTAs per SM; the
+ * double branch's (63.3 KB, values in double) fits 3 */
 #define FNT 184
+/* words per permutation row: byte i of thread t's permutation is in word [i >> 2][t]; a row of a multiple of
+ * 32 words puts every thread's bytes in bank t % 32 whatever the row, so the shuffle's random swaps never
+ * conflict (with 184 words a swap's bank would depend on its row) */
+#define FPS 192
 #define FNPC 8  /* points per chunk */
 #define FMAXT 48 /* lattices per seed this kernel supports */
 
 #define FMAXS 4  /* seeds per CTA at 46 lattices per seed */
 #define FMAXOFF 24 /* offset-noise lattices per CTA (6 per seed) */
 
-/* header of an offset-noise lattice, shared so that any thread can sample it */
+/* header of an offset-noise lattice, shared so that any thread can sample it: all of it for the double
+ * branch, the fields the float branch's octaves read (offsets, floors, zero-coordinate split) for the float */
 struct OffHdr {
     double ox, oy, oz, fyd, fzd, uyd, uzd;
     int64_t Fy, Fz;
     int iy, iz;
     MgLatZero z0;
 };
+struct OffHdrF {
+    double ox, oy, oz;
+    int iy, iz;
+    MgLatZero z0;
+    __device__ OffHdrF &operator=(const OffHdr &h) {
+        ox = h.ox; oy = h.oy; oz = h.oz; iy = h.iy; iz = h.iz; z0 = h.z0;
+        return *this;
+    }
+};
 
 template <typename V>
 struct FusedSmem {
-    uint32_t perm[64][FNT];
+    uint32_t perm[64][FPS];
     V val[FNT][FNPC];               /* octave value of lattice (owner thread) t at point p of the chunk */
-    V valb[FMAXOFF][FNPC];          /* ShiftB octave of the offset lattices */
-    OffHdr hdr[FMAXOFF];
-    double coord[FMAXS][FNPC][4];   /* per (seed, point): x, z, x*c, z*c */
+    union {                         /* valb until phase C has read it, then coord (phase C syncs between) */
+        V valb[FMAXOFF][FNPC];      /* ShiftB octave of the offset lattices */
+        double coord[FMAXS][FNPC][4]; /* per (seed, point): x, z, x*c, z*c */
+    };
+    typename std::conditional<std::is_same<V, float>::value, OffHdrF, OffHdr>::type hdr[FMAXOFF];
 };
 
 /* Threads are lattice-major: thread t owns lattice j = t / spc of local seed t % spc, so the offset-noise
@@ -94,14 +110,14 @@ __global__ void __launch_bounds__(FNT) k_ow_seed_climate(const __grid_constant__
         oy = xo_double(x) * 256.0;
         oz = xo_double(x) * 256.0;
         for (int w = 0; w < 64; w++) sm.perm[w][t] = 0x03020100u + 0x04040404u * (uint32_t)w;
-        uint8_t *mine = reinterpret_cast<uint8_t *>(&sm.perm[0][t]); /* byte i at mine + (i>>2)*4*FNT + (i&3) */
+        uint8_t *mine = reinterpret_cast<uint8_t *>(&sm.perm[0][t]); /* byte i at mine + (i>>2)*4*FPS + (i&3) */
         for (int qw = 0; qw < 64; qw++) {
 #pragma unroll
             for (int r4 = 0; r4 < 4; r4++) {
                 const int q = 4 * qw + r4;
                 const int k = q + xo_int(x, 256u - (uint32_t)q);
-                uint8_t *pa = mine + qw * (4 * FNT) + r4;
-                uint8_t *pb = mine + (k >> 2) * (4 * FNT) + (k & 3);
+                uint8_t *pa = mine + qw * (4 * FPS) + r4;
+                uint8_t *pb = mine + (k >> 2) * (4 * FPS) + (k & 3);
                 uint8_t va = *pa, vb = *pb;
                 *pa = vb;
                 *pb = va;
@@ -127,14 +143,14 @@ __global__ void __launch_bounds__(FNT) k_ow_seed_climate(const __grid_constant__
             const int oj = o / spc;
             const int ost = oj >= O.nlev, olev = oj - ost * O.nlev;
             if (s0 + o % spc >= ns) continue;
-            const OffHdr &oh = sm.hdr[o];
-            const IlvPerm<FNT> perm{pbase, o};
+            const auto &oh = sm.hdr[o];
+            const IlvPerm<FPS> perm{pbase, o};
             const int32_t *pp = pts + (size_t)(s0 + o % spc) * pstride + 3 * (p0 + p);
             double X = (double)pp[0], Z = (double)pp[2];
             if (ost) { X = X * MG_SECOND_STACK; Z = Z * MG_SECOND_STACK; }
             const double of = O.freq[olev];
             const int ok = O.fexp[olev];
-            if (FM) {
+            if constexpr (FM) {
                 int ix, izz, iyy;
                 float fx, fzz, fyy;
                 split_fk(X, of, ok, oh.ox, ix, fx);
@@ -157,6 +173,8 @@ __global__ void __launch_bounds__(FNT) k_ow_seed_climate(const __grid_constant__
         }
         __syncthreads();
         /* ---- phase C: shift sums and shifted coordinates, one thread per (seed, point) */
+        double cx = 0.0, cz = 0.0;
+        bool cw = false;
         if (t < spc * FNPC) {
             const int cs = t / FNPC, p = t % FNPC;
             if (p < npc && s0 + cs < ns) {
@@ -184,16 +202,23 @@ __global__ void __launch_bounds__(FNT) k_ow_seed_climate(const __grid_constant__
                     x = X + ((a1 + a2) * O.vfac) * 4.0;
                     z = Z + ((b1 + b2) * O.vfac) * 4.0;
                 }
-                sm.coord[cs][p][0] = x;
-                sm.coord[cs][p][1] = z;
-                sm.coord[cs][p][2] = x * MG_SECOND_STACK;
-                sm.coord[cs][p][3] = z * MG_SECOND_STACK;
+                cx = x;
+                cz = z;
+                cw = true;
             }
+        }
+        __syncthreads(); /* every valb read is done: coord may overwrite it */
+        if (cw) {
+            const int cs = t / FNPC, p = t % FNPC;
+            sm.coord[cs][p][0] = cx;
+            sm.coord[cs][p][1] = cz;
+            sm.coord[cs][p][2] = cx * MG_SECOND_STACK;
+            sm.coord[cs][p][3] = cz * MG_SECOND_STACK;
         }
         __syncthreads();
         /* ---- phase D: climate octaves at (x, 0, z), each thread on its own lattice */
         if (active && noise != 0) {
-            const IlvPerm<FNT> perm{pbase, t};
+            const IlvPerm<FPS> perm{pbase, t};
             for (int p = 0; p < npc; p++) {
                 const double x = sm.coord[ls][p][st ? 2 : 0], z = sm.coord[ls][p][st ? 3 : 1];
                 if (FM) {
