@@ -498,6 +498,50 @@ __device__ __forceinline__ void zoom_cell(int64_t zseed, int x, int y, int z, in
     cy = py + ((best >> 1) & 1);
     cz = pz + (best & 1);
 }
+/* The chain of cell_chunk, given the cell's own search (leaf, tied): when the cell is tied, walk back to the
+ * first untied cell of the chunk's fill order and replay the chain forward. */
+template <bool FM, int DIM>
+__device__ int cell_chunk_chain(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
+                                const MgTreeNode *__restrict__ tree, int qx, int qy, int qz, int leaf, bool tied) {
+    const int qmin = W.min_y >> 2, qh = W.height >> 2;
+    qy = qy < qmin ? qmin : (qy > qmin + qh - 1 ? qmin + qh - 1 : qy);
+    const int bx = qx & ~3, bz = qz & ~3, ly = qy - qmin;
+    const int idx0 = (ly >> 2) * 64 + (qx & 3) * 16 + (ly & 3) * 4 + (qz & 3);
+    if (idx0 == 0 || !tied) return tree[leaf].biome;
+    int32_t tg[6];
+    uint64_t d;
+    int idx = idx0 - 1;
+    for (;;) {
+        int sec = idx >> 6, r = idx & 63;
+        cell_target<FM, DIM>(W, S, T, bx + (r >> 4), qmin + sec * 4 + ((r >> 2) & 3), bz + (r & 3), tg);
+        leaf = tree_search_tie(tree, tg, d, tied);
+        if (idx == 0 || !tied) break;
+        idx--;
+    }
+    for (int k = idx + 1; k <= idx0; k++) { /* replay the chain forward */
+        int sec = k >> 6, r = k & 63;
+        cell_target<FM, DIM>(W, S, T, bx + (r >> 4), qmin + sec * 4 + ((r >> 2) & 3), bz + (r & 3), tg);
+        int l0 = tree_search(tree, tg, -1, d);
+        if (node_dist(tree[leaf], tg) != d) leaf = l0;
+    }
+    return tree[leaf].biome;
+}
+/* cell_chunk for the 32 neighbouring cells of a warp (all lanes call it, inactive lanes get -1): the cell's
+ * own search is the warp-shared walk; the chain (rare) runs per lane. */
+template <bool FM, int DIM>
+__device__ __forceinline__ int cell_chunk_warp(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
+                                               const MgTreeNode *__restrict__ tree, int qx, int qy, int qz, bool active,
+                                               WarpTreeScratch &ws) {
+    const int qmin = W.min_y >> 2, qh = W.height >> 2;
+    const int cy = qy < qmin ? qmin : (qy > qmin + qh - 1 ? qmin + qh - 1 : qy);
+    int32_t tg[6] = {0, 0, 0, 0, 0, 0};
+    if (active) cell_target<FM, DIM>(W, S, T, qx, cy, qz, tg);
+    uint64_t d = 0;
+    bool tied = false;
+    const int leaf = tree_search_tie_warp(tree, tg, active, ws, d, tied);
+    if (!active) return -1;
+    return cell_chunk_chain<FM, DIM>(W, S, T, tree, qx, qy, qz, leaf, tied);
+}
 /* world_biome_cell (libmcgen/src/biome.c:87-114): y clamped into the dimension; a tied cell walks back along
  * LevelChunkSection.fillBiomesFromNoise order (sections bottom-up, then x, y, z) to an untied cell or the
  * column's first cell, then replays the candidate chain forward.  The walk is bounded by the column. */

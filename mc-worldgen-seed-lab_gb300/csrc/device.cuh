@@ -1092,7 +1092,10 @@ __device__ __forceinline__ int warp_tree_candidates(const MgTreeNode *__restrict
     }
     return nc;
 }
-/* first strict minimum of the packed distance over the listed leaves (the same for every lane's loop) */
+/* first strict minimum of the packed distance over the listed leaves (the same for every lane's loop); with
+ * TIE, also the leaves at that minimum, capped at 2 (the list holds every leaf that can be at the minimum, so
+ * the count is the tree's) */
+template <bool TIE = false>
 __device__ __forceinline__ RtState rt_scan(const MgTreeNode *__restrict__ T, const uint16_t *cand, int n,
                                            const RtTarget &q) {
     RtState s{0xFFFFFFFFu, -1, 0};
@@ -1101,7 +1104,8 @@ __device__ __forceinline__ RtState rt_scan(const MgTreeNode *__restrict__ T, con
         const uint4 a = *reinterpret_cast<const uint4 *>(T + ci);
         const uint4 b = *(reinterpret_cast<const uint4 *>(T + ci) + 1);
         const uint32_t d = rt_dist(a, b, q);
-        if (d < s.best) { s.best = d; s.res = ci; }
+        if (d < s.best) { s.best = d; s.res = ci; s.cnt = 1; }
+        else if (TIE && d == s.best && s.cnt < 2) s.cnt++;
     }
     return s;
 }
@@ -1143,6 +1147,45 @@ __device__ __forceinline__ int tree_search_warp(const MgTreeNode *__restrict__ T
     if (!active) return -1;
     uint64_t d;
     return tree_search(T, t, -1, d);
+}
+/* tree_search_tie for the 32 neighbouring cells of a warp (all lanes call it; inactive lanes get -1): the
+ * first leaf at the minimum, its distance and whether a second leaf has the same distance */
+__device__ __forceinline__ int tree_search_tie_warp(const MgTreeNode *__restrict__ T, const int32_t *t, bool active,
+                                                    WarpTreeScratch &ws, uint64_t &best, bool &tied) {
+    const unsigned FULL = 0xFFFFFFFFu;
+    RtTarget q{};
+    const bool ok = !active || rt_target(t, q);
+    const unsigned act = __ballot_sync(FULL, active);
+    if (!act) return -1;
+    int n = -1;
+    if (rt_packed(T) && __all_sync(FULL, ok)) {
+        int32_t lo[6], hi[6];
+        for (int k = 0; k < 6; k++) {
+            lo[k] = __reduce_min_sync(FULL, active ? t[k] : 0x7FFFFFFF);
+            hi[k] = __reduce_max_sync(FULL, active ? t[k] : (int32_t)0x80000000);
+        }
+        RtTarget lbq, ubq;
+        for (int k = 0; k < 3; k++) {
+            lbq.p[k] = pack16(lo[2 * k], lo[2 * k + 1]);
+            lbq.n[k] = pack16(-hi[2 * k], -hi[2 * k + 1]);
+            ubq.p[k] = pack16(hi[2 * k], hi[2 * k + 1]);
+            ubq.n[k] = pack16(-lo[2 * k], -lo[2 * k + 1]);
+        }
+        n = warp_tree_candidates(T, lbq, ubq, ws);
+    }
+    if (n >= 0) {
+        const RtState s = rt_scan<true>(T, ws.cand, n, q);
+        __syncwarp();
+        if (!active) return -1;
+        if (s.res >= 0 && s.best < (uint32_t)MG_RT_CLAMP * MG_RT_CLAMP) {
+            best = s.best;
+            tied = s.cnt >= 2;
+            return s.res;
+        }
+        return tree_search_tie_stack(T, t, best, tied);
+    }
+    if (!active) return -1;
+    return tree_search_tie(T, t, best, tied);
 }
 
 /* (long)(v * 10000f) */

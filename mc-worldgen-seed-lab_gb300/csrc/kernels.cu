@@ -311,7 +311,19 @@ __global__ void __launch_bounds__(128, 6) k_blockgrid(const __grid_constant__ Mg
         __syncthreads();
     }
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= (long long)nx * nz) return;
+    const bool in = g < (long long)nx * nz;
+    /* grids of a wide tree: a warp's 32 samples are neighbours (one row of the grid), so the cells' own R-tree
+     * searches share one pruned walk (the chunk-cell chain, rare, stays per lane); not for scattered points or
+     * sparse grids, whose warps' targets are unrelated */
+    if (FM && DIM == MG_OVERWORLD && !xyz && step <= 16 && W.tree_fanout >= MG_WARP_TREE_FANOUT) {
+        __shared__ WarpTreeScratch wt[4];
+        int cx = 0, cy = 0, cz = 0;
+        if (in) zoom_cell(zseed, x0 + (int)(g % nx) * step, y, z0 + (int)(g / nx) * step, cx, cy, cz);
+        const int b = cell_chunk_warp<FM, DIM>(W, *S, T, tree, cx, cy, cz, in, wt[threadIdx.x >> 5]);
+        if (in) out[g] = (uint8_t)b;
+        return;
+    }
+    if (!in) return;
     int bxk, byk, bzk;
     if (xyz) { bxk = xyz[3 * g]; byk = xyz[3 * g + 1]; bzk = xyz[3 * g + 2]; }
     else { bxk = x0 + (int)(g % nx) * step; byk = y; bzk = z0 + (int)(g / nx) * step; }
