@@ -483,7 +483,11 @@ def run_batch(args, rank, world, local_rank, mg, ge):
     h_out = torch.empty(samples, dtype=torch.uint8).pin_memory()
     hv = h_out.numpy()
     shape = plan.shape
-    plan_args = [(worlds[(v, d)], s, qx0, qz0, n, n, qy) for v, d, s, qx0, qz0, n, qy in reqs]
+    # the request list as a caller keeps it for the library: one packed record array (McGb300Request[])
+    wkeys = sorted(worlds)
+    plan_args = mg.RequestArray.from_index([worlds[k] for k in wkeys], [wkeys.index((v, d)) for v, d, *_ in reqs],
+                                           [r[2] for r in reqs], [r[3] for r in reqs], [r[4] for r in reqs],
+                                           [r[5] for r in reqs], [r[5] for r in reqs], [r[6] for r in reqs])
 
     def e2e_step():
         p = mg.Plan(plan_args)
@@ -527,7 +531,8 @@ def run_batch(args, rank, world, local_rank, mg, ge):
                            "form": "per request: setup + grid launch into device memory, no synchronisation"},
            **ratios,
            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(samples),
-                   "steps": e2e_steps, "call": "Plan(requests) + plan_run(host buffer) + plan_free per step"},
+                   "steps": e2e_steps, "call": "mcgen_gb300_plan_new(request records) + plan_run(host buffer) + "
+                                               "plan_free per step"},
            "gpu_launches": int(graph_launches) + args.steps * per_step_launches}
     if rank == 0:
         out["kernels"] = {k: {"ms_total": round(v[0], 4), "launches": v[1], "avg_ms": round(v[0] / v[1], 5)}

@@ -572,7 +572,12 @@ class Plan:
                "mcgen_gb300_plan_new")
         self._h = h
         self.n = len(arr)
-        self.shapes = list(zip(arr["nx"].tolist(), arr["nz"].tolist()))
+        self._nx, self._nz = arr["nx"].copy(), arr["nz"].copy()
+
+    @property
+    def shapes(self):
+        """(nx, nz) of every request."""
+        return list(zip(self._nx.tolist(), self._nz.tolist()))
 
     def close(self):
         if self._h:
