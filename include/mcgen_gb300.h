@@ -227,6 +227,14 @@ MCGEN_API int mcgen_gb300_check_climate(const McWorld *w, long long n, unsigned 
 MCGEN_API int mcgen_gb300_check_tree(const McWorld *w, long long n, unsigned long long seed, long long *bad_leaf,
                                      long long *bad_other);
 
+/* Device self-check of the End's screened island test (the three simplex corner terms in float, decided when
+ * farther from the -0.9 threshold than the float evaluation's error bound, else the exact double value)
+ * against the reference's double simplex: n random (permutation, chunk cell) cases, both branches.  *bad
+ * counts different decisions, *screened_out the cases left to the exact value, *worst_ratio the largest
+ * |float evaluation - double value| over the bound. */
+MCGEN_API int mcgen_gb300_check_end(long long n, unsigned long long seed, long long *bad, long long *screened_out,
+                                    double *worst_ratio);
+
 /* Pipe microbenchmarks on the current device, in giga-operations per second:
  * 0 FP32 FMA, 1 FP64 FMA, 2 FP64 add, 3 int32 multiply-add, 4 double->int floor conversion,
  * 5 int->double conversion, 6 double->float conversion, 7 64-bit wide integer multiply-add. */

@@ -126,6 +126,7 @@ _PROTOS.update({
     "mcgen_gb300_server_wait": (C.c_int, [_P, C.c_longlong, C.c_int, C.POINTER(C.c_double)]),
     "mcgen_gb300_server_stats": (C.c_int, [_P, _P]),
     "mcgen_gb300_server_fail_next": (C.c_int, [_P, C.c_int]),
+    "mcgen_gb300_check_end": (C.c_int, [C.c_longlong, C.c_ulonglong, _P, _P, _P]),
     "mcgen_gb300_server_replay": (C.c_int, [_P, _P, _P, C.c_int, _P, _P, _P, _P]),
     "mcgen_gb300_density_values": (C.c_int, [_P, C.c_int64, C.c_int, _P, _P]),
     "mcgen_gb300_seed_points_noalloc": (C.c_int, [_P, _P, C.c_int, _P, C.c_int, _P, _P, _P]),
@@ -238,6 +239,14 @@ def check_zoom(n: int, seed: int = 1) -> tuple[int, int]:
     b, c = C.c_longlong(), C.c_longlong()
     _check(load().mcgen_gb300_check_zoom(n, seed, C.byref(b), C.byref(c)), "mcgen_gb300_check_zoom")
     return b.value, c.value
+
+
+def check_end(n: int, seed: int = 1) -> tuple[int, int, float]:
+    """(wrong decisions, cases left to the exact value, worst float error / bound) of the End's screened
+    island test against the reference's double simplex."""
+    b, c, r = C.c_longlong(), C.c_longlong(), C.c_double()
+    _check(load().mcgen_gb300_check_end(n, seed, C.byref(b), C.byref(c), C.byref(r)), "mcgen_gb300_check_end")
+    return b.value, c.value, r.value
 
 
 def check_noise(world: "World", n: int, seed: int = 1) -> tuple[int, int, float]:

@@ -369,6 +369,46 @@ __device__ __forceinline__ double simplex2(const uint8_t *__restrict__ p, double
     n = acc[0] + acc[1] + acc[2];
     return 70.0 * n;
 }
+/* End island test, screened: the reference decides an island cell by nv < -0.9f (double branch, the float
+ * constant widened) or (float)nv < -0.9f (float branch), nv = simplex2 in double (about 60 FP64-pipe
+ * operations).  Here the skew, the cell (i, j), the corner choice and the first corner's offsets x0, y0 are
+ * the reference's double arithmetic (exact same values), and the three corner terms are evaluated in float
+ * from those offsets: |float value - nv| <= END_ISLAND_E (a forward error bound: offsets within 5 u of the
+ * double ones, u = 2^-24; tt = 0.5 - x^2 - y^2 within 32 u; tt^4 within 18 u; the gradient dot within 12 u;
+ * each term tt^4 * dot within 26 u for |x|, |y| < 0.71 (tt > 0); three terms and their sums within 78 u; times
+ * 70: 5,500 u = 3.3e-4 plus the reference's own double roundings, taken as 5e-4).  A value farther than that
+ * from the threshold settles the test (with one more float ulp for the float branch's rounding); the rest
+ * (a few in 10^4) take the exact double evaluation.  mcgen_gb300_check_end checks the bound and the decisions
+ * on the device. */
+#define END_ISLAND_E 5e-4f
+__device__ __forceinline__ bool end_island(const uint8_t *__restrict__ p, double xin, double yin, double F2, double G2,
+                                           bool fm) {
+    const double s = (xin + yin) * F2;
+    const int i = ifloor(xin + s), j = ifloor(yin + s);
+    const double t = (double)(i + j) * G2;
+    const double x0 = xin - ((double)i - t), y0 = yin - ((double)j - t);
+    const int i1 = x0 > y0 ? 1 : 0, j1 = 1 - i1;
+    const float g2 = (float)G2, xf = (float)x0, yf = (float)y0;
+    const float xs[3] = {xf, xf - (float)i1 + g2, xf - 1.0f + 2.0f * g2};
+    const float ys[3] = {yf, yf - (float)j1 + g2, yf - 1.0f + 2.0f * g2};
+    const int ii = i & 255, jj = j & 255;
+    const int gs[3] = {p[(ii + p[jj]) & 255] % 12, p[(ii + i1 + p[(jj + j1) & 255]) & 255] % 12,
+                       p[(ii + 1 + p[(jj + 1) & 255]) & 255] % 12};
+    float n = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        float tt = 0.5f - xs[c] * xs[c] - ys[c] * ys[c];
+        if (tt > 0.0f) {
+            tt *= tt;
+            n += tt * tt * gdot<float>(gs[c], xs[c], ys[c], 0.0f);
+        }
+    }
+    n *= 70.0f;
+    if (n < -0.9f - (END_ISLAND_E + 1e-4f)) return true; /* nv < -0.9f - ulp: an island in both branches */
+    if (n >= -0.9f + (END_ISLAND_E + 1e-4f)) return false; /* nv > -0.9f: none */
+    const double nv = simplex2(p, xin, yin, F2, G2);
+    return fm ? ((float)nv < -0.9f) : (nv < (double)-0.9f);
+}
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return v < lo ? lo : (v < hi ? v : hi); }
 /* EndIslandDensityFunction.getHeightValue at (sx, sz) = (block / 8); rad: half-width of the island window in
  * chunk cells (12 in the game; the seed search may narrow it, engine/cuda/mc_gpu.cuh:600-626, 640-652) */
@@ -385,9 +425,7 @@ inline __device__ float end_height(const uint8_t *__restrict__ p, bool fm, int s
         for (int dz = -rad; dz <= rad; dz++) {
             long long tx = (long long)cx + dx, tz = (long long)cz + dz;
             if (tx * tx + tz * tz <= 4096LL) continue;
-            double nv = simplex2(p, (double)tx, (double)tz, F2, G2);
-            bool island = fm ? ((float)nv < -0.9f) : (nv < (double)-0.9f);
-            if (!island) continue;
+            if (!end_island(p, (double)tx, (double)tz, F2, G2, fm)) continue;
             float size = fmodf(fabsf((float)tx) * 3439.0f + fabsf((float)tz) * 147.0f, 13.0f) + 9.0f;
             float xd = (float)(ox - dx * 2), zd = (float)(oz - dz * 2);
             float h = clampf(100.0f - (float)sqrt((double)(xd * xd + zd * zd)) * size, -100.0f, 80.0f);

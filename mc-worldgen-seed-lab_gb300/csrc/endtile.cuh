@@ -34,8 +34,7 @@ __device__ __forceinline__ void end_tile_classes(const uint8_t *__restrict__ p, 
         bool isl = false;
         float size = 0.0f;
         if (tx * tx + tz * tz > 4096LL) {
-            const double nv = simplex2(p, (double)tx, (double)tz, F2, G2);
-            isl = FM ? ((float)nv < -0.9f) : (nv < (double)-0.9f);
+            isl = end_island(p, (double)tx, (double)tz, F2, G2, FM);
             if (isl) size = fmodf(fabsf((float)tx) * 3439.0f + fabsf((float)tz) * 147.0f, 13.0f) + 9.0f;
         }
         e.isize[i] = size;

@@ -183,9 +183,7 @@ __device__ __forceinline__ bool end_accept(const MgWorldDesc &W, const uint8_t *
         if (dx < -rad || dx > rad || dz < -rad || dz > rad) continue;
         const long long tx = (long long)ccx + dx, tz = (long long)ccz + dz;
         if (tx * tx + tz * tz <= 4096LL) continue;
-        const double nv = simplex2(p, (double)tx, (double)tz, W.end_f2, W.end_g2);
-        const bool island = FM ? ((float)nv < -0.9f) : (nv < (double)-0.9f);
-        if (!island) continue;
+        if (!end_island(p, (double)tx, (double)tz, W.end_f2, W.end_g2, FM)) continue;
         const float size = fmodf(fabsf((float)tx) * 3439.0f + fabsf((float)tz) * 147.0f, 13.0f) + 9.0f;
         const float xd = (float)(ox - dx * 2), zd = (float)(oz - dz * 2);
         const float h = clampf(100.0f - (float)sqrt((double)(xd * xd + zd * zd)) * size, -100.0f, 80.0f);

@@ -291,7 +291,93 @@ __global__ void __launch_bounds__(128) k_check_tree_warp(const MgTreeNode *__res
     atomicAdd(&out[0], bad);
 }
 
+/* The End's screened island test (end_island) against the reference's double simplex: each CTA shuffles a
+ * random permutation (java.util.Random style, thread 0), then its threads test cells at chunk-cell coordinates
+ * of magnitude up to 2^7, 2^11, 2^15 or 2^21, both branches.  out: wrong decisions, cases the screen left to
+ * the exact path, and the largest |float evaluation - double value| / END_ISLAND_E as double bits. */
+__global__ void __launch_bounds__(128) k_check_end(long long n, uint64_t seed, double F2, double G2,
+                                                   unsigned long long *out) {
+    __shared__ uint8_t perm[256];
+    unsigned long long bad = 0, left = 0;
+    double worst = 0.0;
+    const long long per_round = (long long)gridDim.x * blockDim.x * 64;
+    for (long long base = 0; base < n; base += per_round) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint64_t r = mix64(seed ^ mix64((uint64_t)(base / per_round) * 0x9E37ULL + blockIdx.x));
+            for (int k = 0; k < 256; k++) perm[k] = (uint8_t)k;
+            for (int k = 255; k > 0; k--) {
+                r = mix64(r);
+                const int m = (int)(r % (uint64_t)(k + 1));
+                const uint8_t a = perm[k];
+                perm[k] = perm[m];
+                perm[m] = a;
+            }
+        }
+        __syncthreads();
+        for (int q = 0; q < 64; q++) {
+            const long long i = base + ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 64 + q;
+            if (i >= n) break;
+            const uint64_t r = mix64(seed ^ mix64((uint64_t)i)), r2 = mix64(r);
+            const int lims[4] = {7, 11, 15, 21};
+            const int lim = 1 << lims[r & 3];
+            const double x = (double)((long long)((r >> 8) % (uint64_t)(2 * lim)) - lim);
+            const double z = (double)((long long)((r2 >> 8) % (uint64_t)(2 * lim)) - lim);
+            const bool fm = (r >> 4) & 1;
+            const double nv = mg::simplex2(perm, x, z, F2, G2);
+            const bool exact = fm ? ((float)nv < -0.9f) : (nv < (double)-0.9f);
+            bad += mg::end_island(perm, x, z, F2, G2, fm) != exact;
+            /* the float evaluation alone, as end_island forms it, for the bound */
+            const double s = (x + z) * F2;
+            const int ci = mgd::ifloor(x + s), cj = mgd::ifloor(z + s);
+            const double t = (double)(ci + cj) * G2;
+            const double x0 = x - ((double)ci - t), y0 = z - ((double)cj - t);
+            const int i1 = x0 > y0 ? 1 : 0, j1 = 1 - i1;
+            const float g2 = (float)G2, xf = (float)x0, yf = (float)y0;
+            const float xs[3] = {xf, xf - (float)i1 + g2, xf - 1.0f + 2.0f * g2};
+            const float ys[3] = {yf, yf - (float)j1 + g2, yf - 1.0f + 2.0f * g2};
+            const int ii = ci & 255, jj = cj & 255;
+            const int gs[3] = {perm[(ii + perm[jj]) & 255] % 12, perm[(ii + i1 + perm[(jj + j1) & 255]) & 255] % 12,
+                               perm[(ii + 1 + perm[(jj + 1) & 255]) & 255] % 12};
+            float nf = 0.0f;
+            for (int c = 0; c < 3; c++) {
+                float tt = 0.5f - xs[c] * xs[c] - ys[c] * ys[c];
+                if (tt > 0.0f) {
+                    tt *= tt;
+                    nf += tt * tt * mgd::gdot<float>(gs[c], xs[c], ys[c], 0.0f);
+                }
+            }
+            nf *= 70.0f;
+            worst = fmax(worst, fabs((double)nf - nv) / (double)END_ISLAND_E);
+            left += !(nf < -0.9f - (END_ISLAND_E + 1e-4f) || nf >= -0.9f + (END_ISLAND_E + 1e-4f));
+        }
+    }
+    atomicAdd(&out[0], bad);
+    atomicAdd(&out[1], left);
+    atomicMax(&out[2], (unsigned long long)__double_as_longlong(worst));
+}
+
 }  // namespace
+
+extern "C" MCGEN_API int mcgen_gb300_check_end(long long n, unsigned long long seed, long long *bad, long long *screened_out,
+                                               double *worst_ratio) {
+    if (n < 0 || !bad || !screened_out || !worst_ratio) return MCGEN_E_ARG;
+    std::lock_guard<std::mutex> lk(mg::abi_lock());
+    if (!mg::abi_device_ready()) return MCGEN_E_UNSUPPORTED;
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, 3 * sizeof(unsigned long long)) != cudaSuccess) return MCGEN_E_NOMEM;
+    cudaMemset(d, 0, 3 * sizeof(unsigned long long));
+    const double F2 = 0.5 * (sqrt(3.0) - 1.0), G2 = (3.0 - sqrt(3.0)) / 6.0; /* the 2-D simplex skew and unskew */
+    k_check_end<<<152 * 2, 128>>>(n, seed, F2, G2, d);
+    unsigned long long h[3] = {0, 0, 0};
+    cudaError_t e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return MCGEN_E_INTERNAL;
+    *bad = (long long)h[0];
+    *screened_out = (long long)h[1];
+    memcpy(worst_ratio, &h[2], sizeof(double));
+    return MCGEN_OK;
+}
 
 extern "C" MCGEN_API int mcgen_gb300_check_tree(const McWorld *w, long long n, unsigned long long seed, long long *bad_leaf,
                                                 long long *bad_other) {

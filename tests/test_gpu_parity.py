@@ -230,6 +230,16 @@ def test_fixed_point_octave(mg):
         assert mg.check_octave(1 << 24, seed) == 0
 
 
+def test_end_island_screen(mg):
+    """The End's screened island test (float corner terms, exact double only near the -0.9 threshold) on
+    2^26 random (permutation, chunk cell) cases of both branches: every decision equals the reference's double
+    simplex, the float evaluation stays within its bound, and only a small share needs the exact value."""
+    bad, left, worst = mg.check_end(1 << 26, 77)
+    assert bad == 0
+    assert worst < 1.0
+    assert left < (1 << 26) // 100
+
+
 def test_zoom_screen(mg):
     """BiomeManager's zoom choice, screened in single precision, equals the double-precision first minimum of
     the 8 candidates on 2^27 random (zoom seed, block) cases, and the double-precision fallback ran."""
