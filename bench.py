@@ -216,8 +216,8 @@ def batch_fp64_ops(reqs) -> float:
 # Algorithmic work per launch of each kernel, counted from the reference algorithm:
 # (work units per launch, unit name, pipe peak key).
 # DRAM bytes (read + write) per work unit of a launch, from one ncu capture each: k_batch per sample
-# (300-request prefix of the uneven batch), k_ow_seed_climate per seed (4,096 seeds x 8 points).
-DRAM_BYTES_PER_UNIT = {"k_batch": (70121472 + 947673600) / 147087943, "k_ow_seed_climate": 83200 / 4096}
+# (the first 4,000 requests of the uneven batch), k_ow_seed_climate per seed (4,096 seeds x 8 points).
+DRAM_BYTES_PER_UNIT = {"k_batch": (68409600 + 852130304) / 147087943, "k_ow_seed_climate": 83200 / 4096}
 K_BATCH_TRAFFIC_NOTE = ("DRAM bytes read + written per sample in an ncu capture of one k_batch<8, 8> launch over the "
                         "first 4,000 requests (147 M samples, an output larger than L2) x this launch's samples; "
                         "the writes are mostly local-memory write-back (register spills), the ids 1 B per sample")

@@ -152,6 +152,10 @@ struct BatchSmem {
     int tile, req, state;
 };
 
+/* a biome id to the output: written once and never read back by the kernel, so stored with the streaming
+ * (evict-first) policy, which keeps the streamed output from evicting the threads' local memory from L2 */
+__device__ __forceinline__ void put_id(uint8_t *p, int v) { __stcs(p, (unsigned char)v); }
+
 /* tab: the tile's shift table (double-branch Overworld, ENGINE rule) or null; g: with a table, the tile's
  * depth gradient */
 template <bool FM, int DIM, int TILE_W>
@@ -164,7 +168,7 @@ __device__ __forceinline__ void batch_cells(const MgWorldDesc &W, const MgSpline
     const bool in = ix < R.nx && iz < R.nz;
     const int qx = R.qx0 + ix, qz = R.qz0 + iz;
     if (R.tie == MG_TIE_CHUNK_CELL) { /* the request's rule: the same for the whole CTA */
-        if (in) out[R.out_off + (size_t)iz * R.nx + ix] = (uint8_t)cell_chunk<FM, DIM>(W, S, T, tree, qx, R.qy, qz);
+        if (in) put_id(out + R.out_off + (size_t)iz * R.nx + ix, cell_chunk<FM, DIM>(W, S, T, tree, qx, R.qy, qz));
         return;
     }
     int32_t tg[6] = {0, 0, 0, 0, 0, 0};
@@ -185,7 +189,7 @@ __device__ __forceinline__ void batch_cells(const MgWorldDesc &W, const MgSpline
         uint64_t d;
         leaf = in ? tree_search(tree, tg, -1, d) : -1;
     }
-    if (in) out[o] = tree[leaf].biome;
+    if (in) put_id(out + o, tree[leaf].biome);
 }
 
 /* End tile: chunks [cx0, cx0 + END_TC) x [cz0, cz0 + END_TC) counted from the chunk of the request's
@@ -199,7 +203,8 @@ __device__ __forceinline__ void batch_end(const MgWorldDesc &W, BatchSmem &sm, c
         const int qx = 4 * cx0 + i % (4 * END_TC), qz = 4 * cz0 + i / (4 * END_TC);
         const int ix = qx - R.qx0, iz = qz - R.qz0;
         if (ix < 0 || iz < 0 || ix >= R.nx || iz >= R.nz) continue;
-        out[R.out_off + (size_t)iz * R.nx + ix] = (uint8_t)W.end_ids[sm.end.tile.cls[(i / (16 * END_TC)) * END_TC + (i % (4 * END_TC)) / 4]];
+        put_id(out + R.out_off + (size_t)iz * R.nx + ix,
+               W.end_ids[sm.end.tile.cls[(i / (16 * END_TC)) * END_TC + (i % (4 * END_TC)) / 4]]);
     }
 }
 
@@ -318,7 +323,7 @@ __global__ void __launch_bounds__(128) k_batch_exact(const MgWorldDesc *__restri
         pending_targets(W, pool + P.state, P, tg);
         const MgTreeNode *tree = trees[P.world];
         uint64_t d;
-        out[P.out] = tree[tree_search_scattered(tree, tg, -1, d)].biome;
+        put_id(out + P.out, tree[tree_search_scattered(tree, tg, -1, d)].biome);
     }
 }
 
