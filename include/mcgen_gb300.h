@@ -211,6 +211,15 @@ MCGEN_API int mcgen_gb300_check_zoom(long long n, unsigned long long seed, long 
  * largest |fixed-point - exact| over the bound.  MCGEN_E_ARG for float-branch and End worlds. */
 MCGEN_API int mcgen_gb300_check_noise(const McWorld *w, long long n, unsigned long long seed, long long *bad,
                                       long long *screened_out, double *worst_ratio);
+/* Device self-check of the double branch's 32-bit screen of the noises whose value is only quantised (the
+ * kernels' form for the Nether's two noises; checked on the Overworld's temperature and vegetation as well,
+ * whose constants differ), on mcgen_gb300_check_noise's coordinates:
+ * *bad counts settled targets that differ from quantize((float)exact), *screened_out the values the screen
+ * leaves to the 59-bit screen, *worst_ratio the largest |value - exact| over the bound, *near_boundary the
+ * settled values whose exact value lies within twice the bound of a target boundary.  MCGEN_E_ARG for
+ * float-branch and End worlds. */
+MCGEN_API int mcgen_gb300_check_noise_quant(const McWorld *w, long long n, unsigned long long seed, long long *bad,
+                                            long long *screened_out, double *worst_ratio, long long *near_boundary);
 /* Device self-check of the double branch's whole Overworld climate as the kernels compute it (exact shift
  * noises, climate noises screened in fixed point) against the plain double evaluation of every noise: n
  * random quart cells (|qx|, |qz| up to 2^21).  *bad counts cells whose six quantised targets differ,

@@ -95,6 +95,9 @@ _PROTOS = {
                                          C.POINTER(C.c_longlong)]),
     "mcgen_gb300_check_noise": (C.c_int, [_P, C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong),
                                           C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
+    "mcgen_gb300_check_noise_quant": (C.c_int, [_P, C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong),
+                                                C.POINTER(C.c_longlong), C.POINTER(C.c_double),
+                                                C.POINTER(C.c_longlong)]),
     "mcgen_gb300_check_climate": (C.c_int, [_P, C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong),
                                             C.POINTER(C.c_longlong)]),
     "mcgen_gb300_check_tree": (C.c_int, [_P, C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong),
@@ -256,6 +259,16 @@ def check_noise(world: "World", n: int, seed: int = 1) -> tuple[int, int, float]
     _check(load().mcgen_gb300_check_noise(world.handle, n, seed, C.byref(b), C.byref(c), C.byref(r)),
            "mcgen_gb300_check_noise")
     return b.value, c.value, r.value
+
+
+def check_noise_quant(world: "World", n: int, seed: int = 1) -> tuple[int, int, float, int]:
+    """(target mismatches, values left to the 59-bit screen, worst error / bound, settled values near a target
+    boundary) of the 32-bit screen of the double branch's quantised-only noises (temperature, vegetation)
+    against the exact double evaluation, on the world's own seed lattices."""
+    b, c, r, m = C.c_longlong(), C.c_longlong(), C.c_double(), C.c_longlong()
+    _check(load().mcgen_gb300_check_noise_quant(world.handle, n, seed, C.byref(b), C.byref(c), C.byref(r),
+                                                C.byref(m)), "mcgen_gb300_check_noise_quant")
+    return b.value, c.value, r.value, m.value
 
 
 def check_climate(world: "World", n: int, seed: int = 1) -> tuple[int, int]:

@@ -62,6 +62,29 @@ __device__ __forceinline__ float nn_d_y0_float(const MgNoise &N, const MgLattice
     }
     return (float)nn_d_y0(N, T, x, z, xc, zc);
 }
+/* a value only quantised, from a fixed-point approximation q (units of 2^-59) within eq units of the
+ * reference's double value v: true when every real in [q - eq, q + eq] 2^-59 has the target of the two ends
+ * (the rounding to float, the product by 10000 and the truncation are each monotone, so the ends settle
+ * quantize((float)v)); f is then a float with that target (the lower end's) */
+__device__ __forceinline__ bool quant_settled_q(int64_t q, int64_t eq, float &f) {
+    const float lo = __ll2float_rn(q - eq) * 0x1.0p-59f, hi = __ll2float_rn(q + eq) * 0x1.0p-59f;
+    f = lo;
+    return quantize(lo) == quantize(hi);
+}
+/* a float with the target of a double-branch NormalNoise's value at (x, 0, z), for a noise whose float is
+ * only quantised (the Nether's two): the 32-bit screen's when it settles the target, else nn_d_y0_float's
+ * (the float itself).  The Overworld's temperature and vegetation are only quantised too, but there the
+ * second octave form measured slower: its code pushed the double branch's hot path out of the instruction
+ * cache. */
+__device__ __forceinline__ float nn_d_y0_qfloat(const MgNoise &N, const MgLattice *__restrict__ T, double x, double z,
+                                                double xc, double zc) {
+    float f;
+    if (N.fix_eq32 >= 0) {
+        const int64_t q = nn_q32(N, T, x, z, xc, zc);
+        if (q != MG_QFAIL && quant_settled_q(q, N.fix_eq32, f)) return f;
+    }
+    return nn_d_y0_float(N, T, x, z, xc, zc);
+}
 /* ridges_folded (|(|r| + c0)| + c1) * c2 of a ridge value (the exact path) */
 __device__ __forceinline__ double ridges_folded_d(const MgWorldDesc &W, double r) {
     return (fabs(fabs(r) + W.rf_d[0]) + W.rf_d[1]) * W.rf_d[2];
@@ -245,22 +268,28 @@ static __device__ __noinline__ ShiftPair shift_from_table(const MgNoise &N, cons
     const int64_t M52 = (1LL << 52) - 1;
     double sa[2] = {0.0, 0.0}, sb[2] = {0.0, 0.0};
     const MgLattice *A = T + N.base;
-    for (int q = 0; q < 2 * N.nlev; q++) {
-        const int k = q >> 1, st = q & 1, j = st * N.nlev + k;
+    /* one octave per step (ShiftA and ShiftB of each level and stack in turn; each sum keeps its order): one
+     * copy of the octave code, where two per step measured slower, the hot code no longer fitting the
+     * instruction cache */
+#pragma unroll 1
+    for (int e = 0; e < 4 * N.nlev; e++) {
+        const int q = e >> 1, isb = e & 1, k = q >> 1, st = q & 1, j = st * N.nlev + k;
         const MgLattice *L = A + j;
         const ShiftSplit ex = tab.e[j][col], ey = tab.e[j][TW + col], ez = tab.e[j][2 * TW + row],
                          ew = tab.e[j][2 * TW + TH + row];
         if ((ex.pk | ey.pk | ez.pk | ew.pk | L->Fy | L->Fz) < 0) return ShiftPair{0.0, 0.0, false};
         const PlainPerm p{L->p};
-        /* ShiftA (x, 0, z): x input X-side, z input Z-side, y from the header */
-        const double oa = octave_dfix_u(p, (int)(ex.pk >> 52), ex.pk & M52, ex.u, L->iy, L->Fy, L->uyd, (int)(ez.pk >> 52),
-                                        ez.pk & M52, ez.u);
-        /* ShiftB (z, x, 0): x input Z-side, y input X-side, z from the header */
-        const double ob = octave_dfix_u(p, (int)(ew.pk >> 52), ew.pk & M52, ew.u, (int)(ey.pk >> 52), ey.pk & M52, ey.u,
-                                        L->iz, L->Fz, L->uzd);
-        const double ta = N.amp_d[k] * oa * N.vf_d[k], tb = N.amp_d[k] * ob * N.vf_d[k];
-        if (st) { sa[1] += ta; sb[1] += tb; }
-        else { sa[0] += ta; sb[0] += tb; }
+        const ShiftSplit sx = isb ? ew : ex, sz = isb ? ey : ez;
+        const int ix = (int)(sx.pk >> 52), iy = isb ? (int)(sz.pk >> 52) : L->iy;
+        const int64_t FX = sx.pk & M52, FY = isb ? (sz.pk & M52) : L->Fy;
+        const double u = sx.u, v = isb ? sz.u : L->uyd;
+        const int iz = isb ? L->iz : (int)(sz.pk >> 52);
+        const int64_t FZ = isb ? L->Fz : (sz.pk & M52);
+        const double w = isb ? L->uzd : sz.u;
+        const double o = octave_dfix_u(p, ix, FX, u, iy, FY, v, iz, FZ, w);
+        const double t = N.amp_d[k] * o * N.vf_d[k];
+        if (isb) { if (st) sb[1] += t; else sb[0] += t; }
+        else { if (st) sa[1] += t; else sa[0] += t; }
     }
     return ShiftPair{(sa[0] + sa[1]) * N.vfac, (sb[0] + sb[1]) * N.vfac, true};
 }
@@ -327,8 +356,8 @@ __device__ __forceinline__ void climate_nether(const MgWorldDesc &W, const MgLat
         t = nn_f_legacy_y0(W.nether[0], T, X, Z, Xc, Zc);
         h = nn_f_legacy_y0(W.nether[1], T, X, Z, Xc, Zc);
     } else {
-        t = nn_d_y0_float(W.nether[0], T, X, Z, Xc, Zc);
-        h = nn_d_y0_float(W.nether[1], T, X, Z, Xc, Zc);
+        t = nn_d_y0_qfloat(W.nether[0], T, X, Z, Xc, Zc);
+        h = nn_d_y0_qfloat(W.nether[1], T, X, Z, Xc, Zc);
     }
     tg[0] = quantize(t);
     tg[1] = quantize(h);

@@ -603,12 +603,13 @@ static __device__ __noinline__ float nn_f(const MgNoise &N, const MgLattice *__r
                                           double ac, double bc, bool z0) {
     float acc = 0.0f;
     const MgLattice *A = T + N.base, *B = A + N.nlev;
-    /* two octaves per level in flight (the float path's code is small; its instruction cache is not the
-     * limit, unlike the double branch's) */
-    for (int k = 0; k < N.nlev; k++) {
-        double f = N.freq[k];
-        acc += N.amp_f[k] * oct_f(A + k, a, b, f, N.fexp[k], z0);
-        acc += N.amp_f[k] * oct_f(B + k, ac, bc, f, N.fexp[k], z0);
+    /* one octave per step, first and second stack of each level in turn (the reference's order): one copy of
+     * the octave code (the batch kernel runs every code path's tiles side by side, so all of their hot code
+     * shares the instruction cache) */
+#pragma unroll 1
+    for (int j = 0; j < 2 * N.nlev; j++) {
+        const int k = j >> 1, st = j & 1;
+        acc += N.amp_f[k] * oct_f((st ? B : A) + k, st ? ac : a, st ? bc : b, N.freq[k], N.fexp[k], z0);
     }
     return acc;
 }
@@ -684,6 +685,71 @@ static __device__ __noinline__ int64_t nn_q(const MgNoise &N, const MgLattice *_
         if (st) {
             const int64_t c = N.cq[k], m = mulq_us(c < 0 ? -c : c, lev);
             acc += c < 0 ? -m : m;
+            lev = 0;
+        }
+    }
+    return acc;
+}
+/* The 32-bit screened form of nn_q (input (a, 0, b)), for a noise whose value is only quantised (the double
+ * branch's Nether noises: their floats feed nothing but quantize, whose steps of 1e-4 need far less precision
+ * than a float's rounding): the octaves in 28-bit fixed point (values in units of 2^-28 in
+ * int32, below 8 in magnitude), the smoothstep weights in units of 2^-31, every lerp one 32 x 32-bit product
+ * where nn_q's 59-bit form takes a 64 x 64-bit one, and the levels' constants N.c31 (units of 2^-31) bring
+ * the sum to nn_q's units of 2^-59.  Within N.fix_eq32 units of the reference's double value (the host's
+ * bound); MG_QFAIL as nn_q. */
+/* smoothstep of a fraction t (units of 2^-32), in units of 2^-31: t^3 (6t^2 - 15t + 10) with t^3 truncated
+ * once from the exact t^2, the factor (in [1, 10]) from t^2 truncated, and their product truncated */
+__device__ __forceinline__ int32_t fade31(uint32_t t) {
+    const uint64_t t2w = (uint64_t)t * t;
+    const uint32_t t2 = (uint32_t)(t2w >> 32);
+    const uint32_t t3 = (uint32_t)(((uint64_t)t2 * t + (((uint64_t)(uint32_t)t2w * t) >> 32)) >> 32);
+    const int64_t p = (10LL << 32) + 6 * (int64_t)t2 - 15 * (int64_t)t; /* > 2^32 - 7: positive */
+    const uint32_t f = (uint32_t)(((uint64_t)t3 * (uint32_t)p) >> 32) + t3 * (uint32_t)(p >> 32);
+    return (int32_t)(f >> 1);
+}
+/* a + w (b - a) for a weight w in [0, 1) (units of 2^-31), floored */
+__device__ __forceinline__ int32_t lerp28(int32_t w, int32_t a, int32_t b) {
+    return a + (int32_t)(((int64_t)w * (int64_t)(b - a)) >> 31);
+}
+__device__ __forceinline__ int32_t gdot28(int h, int32_t x, int32_t y, int32_t z) {
+    const int4 g = __ldg(&kGradI[h & 15]);
+    return x * g.x + y * g.y + z * g.z;
+}
+/* fractions X, Y, Z (units of 2^-28) and weights U, V, W (of X, Y, Z; units of 2^-31) */
+template <typename P>
+__device__ __forceinline__ int32_t octave_q28(const P &p, int ix, int32_t X, int32_t U, int iy, int32_t Y, int32_t V,
+                                              int iz, int32_t Z, int32_t W) {
+    const int32_t ONE = 1 << 28;
+    const int a = p(ix), b = p(ix + 1);
+    const int aa = p(a + iy), ab = p(a + iy + 1);
+    const int ba = p(b + iy), bb = p(b + iy + 1);
+    const int32_t GX = X - ONE, GY = Y - ONE, GZ = Z - ONE;
+    const int32_t x00 = lerp28(U, gdot28(p(aa + iz), X, Y, Z), gdot28(p(ba + iz), GX, Y, Z));
+    const int32_t x10 = lerp28(U, gdot28(p(ab + iz), X, GY, Z), gdot28(p(bb + iz), GX, GY, Z));
+    const int32_t x01 = lerp28(U, gdot28(p(aa + iz + 1), X, Y, GZ), gdot28(p(ba + iz + 1), GX, Y, GZ));
+    const int32_t x11 = lerp28(U, gdot28(p(ab + iz + 1), X, GY, GZ), gdot28(p(bb + iz + 1), GX, GY, GZ));
+    return lerp28(W, lerp28(V, x00, x10), lerp28(V, x01, x11));
+}
+static __device__ __noinline__ int64_t nn_q32(const MgNoise &N, const MgLattice *__restrict__ T, double a, double b,
+                                              double ac, double bc) {
+    int64_t acc = 0;
+    int32_t lev = 0;
+    const MgLattice *A = T + N.base;
+    for (int j = 0; j < 2 * N.nlev; j++) {
+        const int k = j >> 1, st = j & 1;
+        const MgLattice *L = A + st * N.nlev + k;
+        const double f = N.freq[k];
+        int ia, ib;
+        double fa, fb;
+        int64_t FA, FB;
+        split_dk(st ? ac : a, f, N.fexp[k], L->ox, ia, fa, FA);
+        split_dk(st ? bc : b, f, N.fexp[k], L->oz, ib, fb, FB);
+        if ((FA | FB | L->Fy) < 0) return MG_QFAIL;
+        lev += octave_q28(PlainPerm{L->p}, ia, (int32_t)(FA >> 24), fade31((uint32_t)(FA >> 20)), L->iy,
+                          (int32_t)(L->Fy >> 24), (int32_t)(L->z0.q.uy >> 28), ib, (int32_t)(FB >> 24),
+                          fade31((uint32_t)(FB >> 20)));
+        if (st) {
+            acc += (int64_t)lev * N.c31[k];
             lev = 0;
         }
     }

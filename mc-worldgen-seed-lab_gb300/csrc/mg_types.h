@@ -41,6 +41,11 @@ typedef struct {
     int64_t cq[MG_MAX_OCT];
     double fix_err;
     int64_t fix_eq;
+    /* double branch, the 32-bit screen of a noise whose value is only quantised (the Nether's two noises):
+     * amp_d[k] * vf_d[k] * vfac times 2^31 rounded, and the bound on the difference between its value and the
+     * reference's double value in units of 2^-59 (rounded up; < 0: not screened this way) */
+    int64_t c31[MG_MAX_OCT];
+    int64_t fix_eq32;
 } MgNoise;
 
 /* Offset spline (CubicSpline over continents, erosion, ridges, ridges_folded), float.
@@ -131,7 +136,7 @@ typedef struct {
     double x, z;      /* the climate noises' input: the cell's shifted coordinates */
     double g;         /* depth gradient at the cell's y */
     int64_t out;      /* output byte of the cell */
-    float f[4];       /* temperature, vegetation, continentalness, erosion: the settled floats */
+    float f[4];       /* temperature, vegetation (a float with the settled target), continentalness, erosion */
     float rv, rf;     /* ridge and ridges_folded floats, when settled */
     int32_t world;    /* index into the batch's world table */
     int32_t state;    /* first lattice of its seed in the state pool */

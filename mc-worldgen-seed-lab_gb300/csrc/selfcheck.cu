@@ -188,6 +188,49 @@ __global__ void k_check_noise(const __grid_constant__ MgWorldDesc W, const MgLat
     atomicMax(&out[2], (unsigned long long)__double_as_longlong(worst)); /* non-negative: bits order as values */
 }
 
+/* 32-bit screen of the noises whose value is only quantised (the Nether kernels' form for their two noises;
+ * the Overworld's temperature and vegetation, with other constants, are checked too), on k_check_noise's
+ * coordinates: the screen's value against the exact double value.  out: targets
+ * that differ from quantize((float)exact) where the screen settles them, values it leaves to the 59-bit
+ * screen, the largest |value - exact| / bound as a double's bits, and the settled values whose exact value
+ * lies within twice the bound of a target boundary (the cases that try the screen's margin). */
+__global__ void k_check_noise_quant(const __grid_constant__ MgWorldDesc W, const MgLattice *__restrict__ T, long long n,
+                                    uint64_t seed, unsigned long long *out) {
+    unsigned long long bad = 0, left = 0, near = 0;
+    double worst = 0.0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const uint64_t r = mix64(seed ^ mix64((uint64_t)i)), r2 = mix64(r), r3 = mix64(r2), r4 = mix64(r3);
+        const int lim = 1 << ((r & 3) == 0 ? 10 : ((r & 3) == 1 ? 16 : ((r & 3) == 2 ? 21 : 25)));
+        const int X = (int)((r >> 8) % (uint64_t)(2 * lim)) - lim, Z = (int)((r2 >> 8) % (uint64_t)(2 * lim)) - lim;
+        const double sx = ((double)(r3 >> 11) * 0x1.0p-53 * 2.0 - 1.0) * 4.0;
+        const double sz = ((double)(r4 >> 11) * 0x1.0p-53 * 2.0 - 1.0) * 4.0;
+        const double x = (double)X + sx, z = (double)Z + sz;
+        const double xc = x * MG_SECOND_STACK, zc = z * MG_SECOND_STACK;
+        for (int j = 0; j < 2; j++) {
+            const MgNoise &N = W.dim == MG_OVERWORLD ? W.noise[1 + j] : W.nether[j];
+            if (N.fix_eq32 < 0) continue;
+            const double e = mgd::nn_d_y0(N, T, x, z, xc, zc);
+            const int64_t q = mgd::nn_q32(N, T, x, z, xc, zc);
+            if (q == MG_QFAIL) { left++; continue; }
+            const double bound = (double)N.fix_eq32 * 0x1.0p-59;
+            const double ratio = fabs((double)q * 0x1.0p-59 - e) / bound;
+            worst = ratio > worst ? ratio : worst;
+            float f;
+            if (!mg::quant_settled_q(q, N.fix_eq32, f)) { left++; continue; }
+            const int want = mgd::quantize((float)e);
+            bad += mgd::quantize(f) != want;
+            /* the exact value's distance to the nearest target boundary, in the float domain */
+            const int64_t e59 = (int64_t)(e * 0x1.0p59);
+            float g;
+            near += !mg::quant_settled_q(e59, 2 * N.fix_eq32, g);
+        }
+    }
+    atomicAdd(&out[0], bad);
+    atomicAdd(&out[1], left);
+    atomicMax(&out[2], (unsigned long long)__double_as_longlong(worst));
+    atomicAdd(&out[3], near);
+}
+
 /* Overworld climate of the double branch as the kernels compute it (climate_ow_d: exact shift noises, the
  * five climate noises screened in fixed point) against the plain double evaluation of every noise: random
  * quart cells (|qx|, |qz| below 2^8, 2^11, 2^13, 2^15, 2^18 or 2^21, qy in [-16, 80)).  out: cells whose
@@ -419,6 +462,30 @@ extern "C" MCGEN_API int mcgen_gb300_check_climate(const McWorld *w, long long n
     if (e != cudaSuccess) return MCGEN_E_INTERNAL;
     *bad = (long long)h[0];
     *fallback = (long long)h[1];
+    return MCGEN_OK;
+}
+
+extern "C" MCGEN_API int mcgen_gb300_check_noise_quant(const McWorld *w, long long n, unsigned long long seed,
+                                                       long long *bad, long long *screened_out, double *worst_ratio,
+                                                       long long *near_boundary) {
+    if (!w || n < 0 || !bad || !screened_out || !worst_ratio || !near_boundary) return MCGEN_E_ARG;
+    if (w->desc.dim == MG_END || w->desc.fmode) return MCGEN_E_ARG; /* the double branch's noises only */
+    std::lock_guard<std::mutex> lk(mg::abi_lock());
+    if (!mg::abi_device_ready()) return MCGEN_E_UNSUPPORTED;
+    int rc = mg::abi_world_device(const_cast<McWorld *>(w));
+    if (rc) return rc;
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, 4 * sizeof(unsigned long long)) != cudaSuccess) return MCGEN_E_NOMEM;
+    cudaMemset(d, 0, 4 * sizeof(unsigned long long));
+    k_check_noise_quant<<<152 * 4, 128>>>(w->desc, w->d_state, n, seed, d);
+    unsigned long long h[4] = {0, 0, 0, 0};
+    cudaError_t e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return MCGEN_E_INTERNAL;
+    *bad = (long long)h[0];
+    *screened_out = (long long)h[1];
+    memcpy(worst_ratio, &h[2], sizeof(double));
+    *near_boundary = (long long)h[3];
     return MCGEN_OK;
 }
 

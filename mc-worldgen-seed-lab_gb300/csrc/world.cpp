@@ -216,6 +216,38 @@ static double screen_bound(const MgNoise *s) {
                      (654.0 * c + 6.0 * s->nlev) * 0x1.0p-59;
     return 1.25 * e + 4.0 * u * vmax;
 }
+/* Bound on |value of the 32-bit screen (nn_q32) - the reference's double value| of one double-branch
+ * NormalNoise, in reals (units of 2^-32 written "w").  The octave runs in 28-bit fixed point (units
+ * u = 2^-28 = 16 w; every value below 8 in magnitude):
+ *  - the fractions are the exact fractions truncated to u (each within u below), so a gradient sum of two
+ *    of them is within 2u;
+ *  - the x and z smoothstep weights (fade31, units of 2^-31) are within 20 w of the exact smoothstep of the
+ *    exact fraction: t^3 truncated once (1 w), the factor 6t^2 - 15t + 10 <= 10 within 6 w (6 x t^2's
+ *    truncation), the product truncated (1 w), so 10 x 1 + 6 + 1 = 17 w at the 32-bit fraction, 1.875 w more
+ *    for that fraction's truncation (the smoothstep's slope is at most 1.875) and 1 w for the final halving;
+ *    the y weight (the lattice header's 59-bit smoothstep truncated to 2^-31) is within 2.01 w;
+ *  - a lerp a + floor(w (b - a)) against the exact a' + W (b' - a') is within max(e_a, e_b) + |b' - a'| e_W +
+ *    u, with |b' - a'| <= 4 (exact values lie in [-2, 2]);
+ *  so an octave is within 2u + (u + 4 x 20) + (u + 4 x 2.01) + (u + 4 x 20) w < 250 w of the exact octave.
+ * A level's two octaves (each within 250 w) times the constant c31 (within 2^-32 of amp vf vfac, on a sum of
+ * magnitude at most 4.01) add (|c| + 2^-32) 500 w + 4.01 w; the products and the sum are exact integers
+ * (units of 2^-59).  The reference's own roundings are screen_bound's: the same terms as there.  The bound is
+ * taken 25 % larger.  Negative: not screened (the levels' constants or the sum beyond the ranges above). */
+static double screen_bound32(const MgNoise *s) {
+    const double u = 0x1.0p-53, w = 0x1.0p-32;
+    double c = 0.0, e = 0.0;
+    for (int k = 0; k < s->nlev; k++) {
+        const double ck = fabs(s->amp_d[k] * s->vf_d[k] * s->vfac);
+        if (ck >= 4.0) return -1.0;
+        c += ck;
+        e += (ck + w) * 500.0 * w + 4.01 * w;
+    }
+    const double vmax = 2.1 * 2.0 * c;
+    if (vmax * 1.01 >= 15.0) return -1.0;
+    e += 2.0 * c * (640.0 * u + 4.2 * u) + (2.0 * s->nlev + 6.0) * u * vmax;
+    return 1.25 * e;
+}
+
 /* PerlinNoise/NormalNoise constants of 26.1/26.2 (engine/mc_noise.h:178-196) */
 static void noise_double(MgNoise *s, const NoiseParams &P, int legacy) {
     memset(s, 0, sizeof *s);
@@ -242,12 +274,16 @@ static void noise_double(MgNoise *s, const NoiseParams &P, int legacy) {
     for (int k = 0; k < s->nlev; k++) s->cq[k] = q59_product(s->amp_d[k], s->vf_d[k], s->vfac);
     s->fix_err = screen_bound(s);
     s->fix_eq = s->fix_err < 0.0 ? -1 : (int64_t)ceil(s->fix_err * 0x1.0p59);
+    for (int k = 0; k < s->nlev; k++) s->c31[k] = (int64_t)llround(s->amp_d[k] * s->vf_d[k] * s->vfac * 0x1.0p31);
+    const double e32 = screen_bound32(s);
+    s->fix_eq32 = e32 < 0.0 ? -1 : (int64_t)ceil(e32 * 0x1.0p59) + 1;
     octave_seeds(s);
 }
 
 /* NoiseStack layer constants of 26.3 (engine/mc_noise.h:198-252) */
 static void noise_float(MgNoise *s, const NoiseParams &P, int legacy) {
     memset(s, 0, sizeof *s);
+    s->fix_eq32 = -1;
     s->legacy = legacy;
     s->octs = P.n;
     s->first = P.first;

@@ -269,6 +269,26 @@ def test_noise_screen(gens, mg, version, dim):
 
 
 @pytest.mark.parametrize("version", ["26.1", "26.2"])
+@pytest.mark.parametrize("dim", ["minecraft:overworld", "minecraft:the_nether"])
+def test_noise_quant_screen(gens, mg, version, dim):
+    """The 32-bit screen of the double branch's noises whose value is only quantised (the Nether kernels'
+    form for their two noises; checked on the Overworld's temperature and vegetation too, whose constants
+    differ) gives quantize((float)exact) wherever it settles the target, on 2^22 random coordinates per seed; its error stays well inside the bound, it leaves under 2 % of the values to the 59-bit screen, and
+    values whose exact double lies within twice the bound of a target boundary occurred among the settled
+    ones (the cases that try the bound)."""
+    for seed in (12345, -(2**62) + 17):
+        w = gens[version].world(dim, "normal", seed)
+        bad, left, worst, near = mg.check_noise_quant(w, 1 << 22, seed & 0xFFFF)
+        n_values = (1 << 22) * 2
+        print(f"{version} {dim} seed {seed}: worst error / bound {worst:.4f}, left {left / n_values:.2e}, "
+              f"near a boundary {near}")
+        assert bad == 0
+        assert worst < 0.8
+        assert 0 < left < n_values // 50
+        assert near > 0
+
+
+@pytest.mark.parametrize("version", ["26.1", "26.2"])
 @pytest.mark.parametrize("preset", ["normal", "large_biomes", "amplified"])
 def test_climate_screen(gens, mg, version, preset):
     """The double branch's Overworld climate as the kernels compute it (exact shift noises, climate noises
