@@ -136,6 +136,44 @@ struct PendSink {
     long long cap;
     int32_t world, state;
 };
+/* the rare part of climate_ow_d_rest_defer (a value the screen left unsettled), out of line so that the hot
+ * path stays compact: the cell recorded in the sink (recorded true), or, the sink full or absent, the unsettled
+ * values evaluated exactly in place (fv updated) */
+struct F6 {
+    float v[6];
+};
+struct DeferOut {
+    F6 f;
+    bool recorded;
+};
+static __device__ __noinline__ DeferOut defer_or_exact(const MgWorldDesc &W, const MgLattice *__restrict__ T, double x,
+                                                      double z, double g, uint32_t pend, const PendSink *sink,
+                                                      int64_t out, F6 fv) {
+    const double xc = x * MG_SECOND_STACK, zc = z * MG_SECOND_STACK;
+    const unsigned long long k = sink->cap > 0 ? atomicAdd(sink->count, 1ULL) : ~0ULL;
+    if (k < (unsigned long long)sink->cap) {
+        MgPending &P = sink->rec[k];
+        P.x = x;
+        P.z = z;
+        P.g = g;
+        P.out = out;
+        for (int j = 0; j < 4; j++) P.f[j] = fv.v[j];
+        P.rv = fv.v[4];
+        P.rf = fv.v[5];
+        P.world = sink->world;
+        P.state = sink->state;
+        P.pend = pend;
+        return DeferOut{fv, true};
+    }
+    for (int j = 0; j < 4; j++)
+        if (pend & (1u << j)) fv.v[j] = (float)nn_d_y0(W.noise[1 + j], T, x, z, xc, zc);
+    if (pend & 16u) {
+        const double rv = nn_d_y0(W.noise[5], T, x, z, xc, zc);
+        fv.v[4] = (float)rv;
+        fv.v[5] = (float)ridges_folded_d(W, rv);
+    }
+    return DeferOut{fv, false};
+}
 /* climate_ow_d_rest for a batch: the same values, but a cell with a value the screen does not settle is
  * recorded in the sink (output byte `out`) and false returned, without the exact evaluation; when the sink
  * is full (or absent) the exact evaluation runs here and the targets are returned as climate_ow_d_rest gives
@@ -158,29 +196,9 @@ static __device__ __noinline__ bool climate_ow_d_rest_defer(const MgWorldDesc &W
         if (q == MG_QFAIL || !cast_settled_q(q, N.fix_eq, fv[4]) || !ridges_folded_settled(W, q, fv[5])) pend |= 16u;
     }
     if (pend) {
-        const unsigned long long k = sink->cap > 0 ? atomicAdd(sink->count, 1ULL) : ~0ULL;
-        if (k < (unsigned long long)sink->cap) {
-            MgPending &P = sink->rec[k];
-            P.x = x;
-            P.z = z;
-            P.g = g;
-            P.out = out;
-            for (int j = 0; j < 4; j++) P.f[j] = fv[j];
-            P.rv = fv[4];
-            P.rf = fv[5];
-            P.world = sink->world;
-            P.state = sink->state;
-            P.pend = pend;
-            return false;
-        }
-#pragma unroll
-        for (int j = 0; j < 4; j++)
-            if (pend & (1u << j)) fv[j] = (float)nn_d_y0(W.noise[1 + j], T, x, z, xc, zc);
-        if (pend & 16u) {
-            const double rv = nn_d_y0(W.noise[5], T, x, z, xc, zc);
-            fv[4] = (float)rv;
-            fv[5] = (float)ridges_folded_d(W, rv);
-        }
+        const DeferOut r = defer_or_exact(W, T, x, z, g, pend, sink, out, F6{{fv[0], fv[1], fv[2], fv[3], fv[4], fv[5]}});
+        if (r.recorded) return false;
+        for (int j = 0; j < 6; j++) fv[j] = r.f.v[j];
     }
     climate_finish_df(W, S, fv[0], fv[1], fv[2], fv[3], fv[4], fv[5], g, tg);
     return true;
@@ -611,9 +629,11 @@ __device__ __forceinline__ int cell_chunk_warp(const MgWorldDesc &W, const MgSpl
 }
 /* world_biome_cell (libmcgen/src/biome.c:87-114): y clamped into the dimension; a tied cell walks back along
  * LevelChunkSection.fillBiomesFromNoise order (sections bottom-up, then x, y, z) to an untied cell or the
- * column's first cell, then replays the candidate chain forward.  The walk is bounded by the column. */
+ * column's first cell, then replays the candidate chain forward.  The walk is bounded by the column.  Out of
+ * line: the batch kernel reaches it only for requests under this rule, and inlined its code and registers
+ * weighed on the other paths' hot code (spills and the instruction cache). */
 template <bool FM, int DIM>
-__device__ int cell_chunk(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
+__device__ __noinline__ int cell_chunk(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
                           const MgTreeNode *__restrict__ tree, int qx, int qy, int qz) {
     const int qmin = W.min_y >> 2, qh = W.height >> 2;
     qy = qy < qmin ? qmin : (qy > qmin + qh - 1 ? qmin + qh - 1 : qy);
