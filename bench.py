@@ -398,6 +398,7 @@ def run_gb300(args, rank, world, local_rank):
             out["cpu_baseline"], out["parity"] = cpu_baseline(args.workload, args.cpu_sample_s, d_out.cpu().numpy())
             if args.workload == "grid256":
                 out["parity_quart_form"] = quart_form_parity(mg, gen, dev)
+                out["quart_form"] = quart_form_rate(mg, gen, dev, args.steps, max(3, args.warmup))
     return out
 
 
@@ -1167,6 +1168,40 @@ def quart_form_parity(mg, gen, dev) -> dict:
             "golden_digest_match": digest == C1_GOLDEN_DIGEST}
 
 
+def quart_form_rate(mg, gen, dev, steps: int, warmup: int) -> dict:
+    """C1's quart form timed: the 256 x 256 quart grid qx, qz in [-128, 128) at qy = 16 (ENGINE ties) through
+    mcgen_gb300_quart_grid_dev (one world, its lattices resident), CUDA events per step with L2 flushed
+    between steps; and end to end through mcgen_gb300_quart_grid (host output buffer)."""
+    import torch
+
+    w = gen.world("minecraft:overworld", "normal", 12345)
+    n = 256 * 256
+    d_out = torch.empty(n, dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(warmup):
+        w.quart_grid_dev(-128, -128, 256, 256, 16, mg.TIE_ENGINE, d_out.data_ptr(), stream.cuda_stream)
+    torch.cuda.synchronize(dev)
+    ms = 0.0
+    for _ in range(steps):
+        flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        w.quart_grid_dev(-128, -128, 256, 256, 16, mg.TIE_ENGINE, d_out.data_ptr(), stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms += e0.elapsed_time(e1)
+    for _ in range(warmup):
+        w.quart_grid(-128, -128, 256, 256, 16, mg.TIE_ENGINE)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        w.quart_grid(-128, -128, 256, 256, 16, mg.TIE_ENGINE)
+    e2e_s = time.perf_counter() - t0
+    return {"value": n * steps / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / steps,
+            "e2e": {"value": n * steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": n},
+            "form": "mcgen_gb300_quart_grid: 256 x 256 quarts qx, qz in [-128, 128), qy = 16, ENGINE ties"}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -1279,7 +1314,7 @@ def run_reference(args, rank, world):
 CONFIGS = (("C1_grid256", "grid256", {}), ("C2_seeds8", "seeds8", {}), ("C3_dims4096", "dims4096", {}),
            ("C5_serve_2000rps_60s", "serve", {"rates": "2000", "duration": 60.0, "small_budget": False}))
 CONFIG_KEYS = ("metric", "value", "unit", "ms_per_step", "steps", "config", "e2e", "cpu_baseline", "parity",
-               "parity_quart_form", "roofline", "kernels", "gpu_launches", "served", "p50_ms", "p99_ms",
+               "parity_quart_form", "quart_form", "roofline", "kernels", "gpu_launches", "served", "p50_ms", "p99_ms",
                "highest_rate_p99_under_20ms", "clocks")
 
 

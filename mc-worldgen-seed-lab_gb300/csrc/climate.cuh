@@ -583,19 +583,22 @@ __device__ __forceinline__ void zoom_cell(int64_t zseed, int x, int y, int z, in
     cy = py + ((best >> 1) & 1);
     cz = pz + (best & 1);
 }
-/* The chain of cell_chunk, given the cell's own search (leaf, tied): when the cell is tied, walk back to the
- * first untied cell of the chunk's fill order and replay the chain forward. */
+/* The chain of cell_chunk, given the cell's own target tg0 and search (leaf0, the first leaf at the minimum
+ * distance d0, and whether another leaf ties it): when the cell is tied, walk back to the first untied cell of
+ * the chunk's fill order and replay the chain forward, the cell's own step from tg0, leaf0 and d0 (a tied
+ * lane pays one climate evaluation per cell walked back, not two; its warp waits for it). */
 template <bool FM, int DIM>
 __device__ int cell_chunk_chain(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
-                                const MgTreeNode *__restrict__ tree, int qx, int qy, int qz, int leaf, bool tied) {
+                                const MgTreeNode *__restrict__ tree, int qx, int qy, int qz, const int32_t *tg0,
+                                int leaf0, uint64_t d0, bool tied) {
     const int qmin = W.min_y >> 2, qh = W.height >> 2;
     qy = qy < qmin ? qmin : (qy > qmin + qh - 1 ? qmin + qh - 1 : qy);
     const int bx = qx & ~3, bz = qz & ~3, ly = qy - qmin;
     const int idx0 = (ly >> 2) * 64 + (qx & 3) * 16 + (ly & 3) * 4 + (qz & 3);
-    if (idx0 == 0 || !tied) return tree[leaf].biome;
+    if (idx0 == 0 || !tied) return tree[leaf0].biome;
     int32_t tg[6];
     uint64_t d;
-    int idx = idx0 - 1;
+    int idx = idx0 - 1, leaf;
     for (;;) {
         int sec = idx >> 6, r = idx & 63;
         cell_target<FM, DIM>(W, S, T, bx + (r >> 4), qmin + sec * 4 + ((r >> 2) & 3), bz + (r & 3), tg);
@@ -603,12 +606,13 @@ __device__ int cell_chunk_chain(const MgWorldDesc &W, const MgSpline &S, const M
         if (idx == 0 || !tied) break;
         idx--;
     }
-    for (int k = idx + 1; k <= idx0; k++) { /* replay the chain forward */
+    for (int k = idx + 1; k < idx0; k++) { /* replay the chain forward */
         int sec = k >> 6, r = k & 63;
         cell_target<FM, DIM>(W, S, T, bx + (r >> 4), qmin + sec * 4 + ((r >> 2) & 3), bz + (r & 3), tg);
         int l0 = tree_search(tree, tg, -1, d);
         if (node_dist(tree[leaf], tg) != d) leaf = l0;
     }
+    if (node_dist(tree[leaf], tg0) != d0) leaf = leaf0; /* the cell's own step */
     return tree[leaf].biome;
 }
 /* cell_chunk for the 32 neighbouring cells of a warp (all lanes call it, inactive lanes get -1): the cell's
@@ -625,7 +629,7 @@ __device__ __forceinline__ int cell_chunk_warp(const MgWorldDesc &W, const MgSpl
     bool tied = false;
     const int leaf = tree_search_tie_warp(tree, tg, active, ws, d, tied);
     if (!active) return -1;
-    return cell_chunk_chain<FM, DIM>(W, S, T, tree, qx, qy, qz, leaf, tied);
+    return cell_chunk_chain<FM, DIM>(W, S, T, tree, qx, qy, qz, tg, leaf, d, tied);
 }
 /* world_biome_cell (libmcgen/src/biome.c:87-114): y clamped into the dimension; a tied cell walks back along
  * LevelChunkSection.fillBiomesFromNoise order (sections bottom-up, then x, y, z) to an untied cell or the
@@ -634,29 +638,15 @@ __device__ __forceinline__ int cell_chunk_warp(const MgWorldDesc &W, const MgSpl
  * weighed on the other paths' hot code (spills and the instruction cache). */
 template <bool FM, int DIM>
 __device__ __noinline__ int cell_chunk(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
-                          const MgTreeNode *__restrict__ tree, int qx, int qy, int qz) {
+                                       const MgTreeNode *__restrict__ tree, int qx, int qy, int qz) {
     const int qmin = W.min_y >> 2, qh = W.height >> 2;
-    qy = qy < qmin ? qmin : (qy > qmin + qh - 1 ? qmin + qh - 1 : qy);
-    const int bx = qx & ~3, bz = qz & ~3, ly = qy - qmin;
-    const int idx0 = (ly >> 2) * 64 + (qx & 3) * 16 + (ly & 3) * 4 + (qz & 3);
+    const int cy = qy < qmin ? qmin : (qy > qmin + qh - 1 ? qmin + qh - 1 : qy);
     int32_t tg[6];
+    cell_target<FM, DIM>(W, S, T, qx, cy, qz, tg);
     uint64_t d;
-    int idx = idx0, leaf;
-    for (;;) {
-        int sec = idx >> 6, r = idx & 63;
-        cell_target<FM, DIM>(W, S, T, bx + (r >> 4), qmin + sec * 4 + ((r >> 2) & 3), bz + (r & 3), tg);
-        bool tied;
-        leaf = tree_search_tie(tree, tg, d, tied);
-        if (idx == 0 || !tied) break;
-        idx--;
-    }
-    for (int k = idx + 1; k <= idx0; k++) { /* replay the chain forward */
-        int sec = k >> 6, r = k & 63;
-        cell_target<FM, DIM>(W, S, T, bx + (r >> 4), qmin + sec * 4 + ((r >> 2) & 3), bz + (r & 3), tg);
-        int l0 = tree_search(tree, tg, -1, d);
-        if (node_dist(tree[leaf], tg) != d) leaf = l0;
-    }
-    return tree[leaf].biome;
+    bool tied;
+    const int leaf = tree_search_tie(tree, tg, d, tied);
+    return cell_chunk_chain<FM, DIM>(W, S, T, tree, qx, qy, qz, tg, leaf, d, tied);
 }
 
 }  // namespace mg
