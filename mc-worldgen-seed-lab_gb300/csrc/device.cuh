@@ -772,7 +772,7 @@ __device__ __forceinline__ bool cast_settled_q(int64_t q, int64_t eq, float &f) 
 __device__ __forceinline__ float spline_eval(const MgSpline &S, const float co[4]) {
     if (S.root < 0) return S.cval[~S.root];
     struct Frame { int node, i; float in, y1; int state; };
-    Frame st[12];
+    Frame st[MG_SPL_DEPTH];
     int sp = 0;
     float ret = 0.0f;
     st[0].node = S.root;

@@ -13,6 +13,8 @@
 #define MG_SPL_MP 128        /* offset-spline multipoint nodes (26.x: 53) */
 #define MG_SPL_PTS 512       /* offset-spline points (26.x: 253) */
 #define MG_SPL_CONST 512     /* offset-spline constant leaves (26.x: 201) */
+#define MG_SPL_DEPTH 6       /* multipoint levels an offset spline may nest (every 26.x table: 4); the device
+                              * evaluator keeps one stack frame per level */
 #define MG_TREE_DIMS 7
 
 enum { MG_OVERWORLD = 0, MG_NETHER = 1, MG_END = 2 };

@@ -396,7 +396,7 @@ struct SplineBuilder {
     }
 };
 
-/* nesting depth of multipoint nodes below reference c (the device evaluator keeps 12 frames) */
+/* nesting depth of multipoint nodes below reference c (the device evaluator keeps MG_SPL_DEPTH frames) */
 static int spline_depth(const MgSpline &S, int c) {
     if (c < 0) return 0;
     int d = 0;
@@ -638,7 +638,7 @@ int build_world(const char *root, int version, int dim, const char *preset, MgWo
             SplineBuilder sb{&D->spline, tok, 0};
             D->spline.root = sb.parse();
             if (!sb.ok) { *err = "malformed offset spline"; return MCGEN_E_DATA; }
-            if (spline_depth(D->spline, D->spline.root) > 11) { *err = "offset spline nests too deep"; return MCGEN_E_DATA; }
+            if (spline_depth(D->spline, D->spline.root) > MG_SPL_DEPTH) { *err = "offset spline nests too deep"; return MCGEN_E_DATA; }
             have_spline = true;
         } else if (t[0] == "ridges_folded" && t.size() >= 4) {
             for (int i = 0; i < 3; i++) {

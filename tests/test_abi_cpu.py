@@ -103,6 +103,34 @@ def test_world_new_errors(mg):
     assert (n.min_y, n.height, n.sea_level) == (0, 256, 32)
 
 
+def test_spline_nesting_limit(mg, tmp_path):
+    """An offset spline that nests deeper than the device evaluator's stack (six multipoint levels; every
+    shipped table nests four) is refused with MCGEN_E_DATA when the world is built, and six levels are
+    accepted."""
+    import shutil
+
+    def spline(levels: int) -> str:
+        s = "C 0.25"
+        for _ in range(levels):
+            s = f"S 0 1 0.0 0.0 {s}"
+        return s
+
+    for levels, ok in ((6, True), (7, False)):
+        root = tmp_path / f"root{levels}"
+        shutil.copytree(os.path.join(ge.data_root(), "data"), root / "data")
+        f = root / "data" / "climate-26.3.txt"
+        lines = [f"offset_spline overworld {spline(levels)}" if ln.startswith("offset_spline overworld ") else ln
+                 for ln in f.read_text().splitlines()]
+        f.write_text("\n".join(lines) + "\n")
+        g = mg.Generator.open(str(root), "26.3")
+        if ok:
+            g.world("minecraft:overworld", "normal", 1)
+        else:
+            with pytest.raises(mg.McError) as e:
+                g.world("minecraft:overworld", "normal", 1)
+            assert e.value.code == mg.MCGEN_E_DATA
+
+
 def test_world_info(mg):
     g = mg.Generator.open(ge.data_root(), "26.1")
     w = g.world("overworld", "normal", -42)
