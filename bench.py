@@ -217,12 +217,12 @@ def batch_fp64_ops(reqs) -> float:
 # (work units per launch, unit name, pipe peak key).
 # DRAM bytes (read + write) per work unit of a launch, from one ncu capture each: k_batch per sample
 # (the first 4,000 requests of the uneven batch), k_ow_seed_climate per seed (4,096 seeds x 8 points).
-DRAM_BYTES_PER_UNIT = {"k_batch": (67288576 + 587729664) / 147087943, "k_ow_seed_climate": 83200 / 4096}
+DRAM_BYTES_PER_UNIT = {"k_batch": (72375552 + 1504797696) / 147087943, "k_ow_seed_climate": 83200 / 4096}
 K_BATCH_TRAFFIC_NOTE = ("DRAM bytes read + written per sample in an ncu capture of one k_batch<8, 8> launch over the "
                         "first 4,000 requests (147 M samples, an output larger than L2) x this launch's samples; "
                         "the writes are mostly local-memory write-back (register spills), the ids 1 B per sample")
 # pipe utilisation of k_batch<8, 8> from ncu (sm__inst_executed_pipe_*, issue active) on a 300-request launch
-K_BATCH_PIPES = {"fp64": 0.546, "integer_alu": 0.542, "issue_active": 0.678}
+K_BATCH_PIPES = {"fp64": 0.547, "integer_alu": 0.546, "issue_active": 0.682}
 
 
 def kernel_work(kernel: str, seeds8: bool, ns: int, np_: int, ntables: int) -> tuple[float, str, str] | None:
