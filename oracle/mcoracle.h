@@ -1,7 +1,7 @@
 /* mcoracle.h -- CPU oracle for bit-exact multi-noise biome generation.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker: tests/, the smoke
- * entry point and bench.py's CPU-baseline leg may load it; the product library
+ * TEST INFRASTRUCTURE ONLY.  Parity tests compare the GPU path with this library: tests/, the
+ * smoke entry point and bench.py's CPU-baseline leg may load it; the product library
  * (libmcgen_gb300.so) never links, loads or calls it.
  *
  * It is a plain-C restatement of the reference engine's algorithm

@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (test infrastructure only).
 
-Loaded by tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg as the
-checker.  The product library never imports this module.
+Loaded by tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg, which compare the
+GPU path's outputs with it.  The product library never imports this module.
 """
 from __future__ import annotations
 

@@ -1,7 +1,7 @@
 """Shared test configuration.
 
 Markers: ``gpu`` -- needs a CUDA device (runs on the GPU host); everything else runs on CPU.
-The CPU oracle under oracle/ is the checker for every parity test.
+Every parity test compares the GPU path with the CPU oracle under oracle/.
 """
 import os
 import sys

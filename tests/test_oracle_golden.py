@@ -1,6 +1,6 @@
 """Pin the CPU oracle against the reference's golden vectors (CPU only).
 
-The oracle is the checker for every GPU parity test, so it is itself checked first against
+Every GPU parity test compares against the oracle, so the oracle is itself checked first against
 every fixture the reference holds for this path (tests/golden/, generated by make_fixtures.py).
 """
 import struct
