@@ -310,19 +310,24 @@ __global__ void __launch_bounds__(128, 6) k_blockgrid(const __grid_constant__ Mg
         stage(W, state, W.ntables, T, S, DIM == MG_OVERWORLD);
         __syncthreads();
     }
-    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool in = g < (long long)nx * nz;
-    /* grids of a wide tree: a warp's 32 samples are neighbours (one row of the grid), so the cells' own R-tree
-     * searches share one pruned walk (the chunk-cell chain, rare, stays per lane); not for scattered points or
-     * sparse grids, whose warps' targets are unrelated */
+    /* grids of a wide tree (the launcher sizes the grid in tiles for this form): the CTA takes a 16 x 8-cell tile
+     * and each warp an 8 x 4 block of it, neighbours whose targets are close, so the cells' own R-tree searches share one pruned walk (the
+     * chunk-cell chain, rare, stays per lane); not for scattered points or sparse grids, whose warps' targets
+     * are unrelated */
     if (FM && DIM == MG_OVERWORLD && !xyz && step <= 16 && W.tree_fanout >= MG_WARP_TREE_FANOUT) {
         __shared__ WarpTreeScratch wt[4];
+        const int tw = (nx + 15) / 16, w = threadIdx.x >> 5, l = threadIdx.x & 31;
+        const int ix = (int)(blockIdx.x % tw) * 16 + (w & 1) * 8 + (l & 7);
+        const int iz = (int)(blockIdx.x / tw) * 8 + (w >> 1) * 4 + (l >> 3);
+        const bool in = ix < nx && iz < nz;
         int cx = 0, cy = 0, cz = 0;
-        if (in) zoom_cell(zseed, x0 + (int)(g % nx) * step, y, z0 + (int)(g / nx) * step, cx, cy, cz);
-        const int b = cell_chunk_warp<FM, DIM>(W, *S, T, tree, cx, cy, cz, in, wt[threadIdx.x >> 5]);
-        if (in) out[g] = (uint8_t)b;
+        if (in) zoom_cell(zseed, x0 + ix * step, y, z0 + iz * step, cx, cy, cz);
+        const int b = cell_chunk_warp<FM, DIM>(W, *S, T, tree, cx, cy, cz, in, wt[w]);
+        if (in) out[(long long)iz * nx + ix] = (uint8_t)b;
         return;
     }
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = g < (long long)nx * nz;
     if (!in) return;
     int bxk, byk, bzk;
     if (xyz) { bxk = xyz[3 * g]; byk = xyz[3 * g + 1]; bzk = xyz[3 * g + 2]; }
@@ -533,8 +538,11 @@ static void blockgrid_t(const MgWorldDesc &W, const MgTreeNode *tree, const MgLa
     size_t sm = DIM == MG_END ? 0 : grid_smem(W);
     if (sm) cudaFuncSetAttribute(k_blockgrid<FM, DIM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     ProfScope ps_(K_BLOCKGRID, st);
-    k_blockgrid<FM, DIM><<<blocks_for((long long)nx * nz, 128), 128, sm, st>>>(W, tree, state, zseed, x0, z0, nx, nz, step,
-                                                                            y, xyz, out, cls, ecx0, ecz0, encx);
+    /* the kernel's warp-tile form (its own test of the same condition): one CTA per 16 x 8-cell tile */
+    const bool tiles = FM && DIM == MG_OVERWORLD && !xyz && step <= 16 && W.tree_fanout >= MG_WARP_TREE_FANOUT;
+    const unsigned nb = tiles ? (unsigned)(((long long)(nx + 15) / 16) * ((nz + 7) / 8)) : blocks_for((long long)nx * nz, 128);
+    k_blockgrid<FM, DIM><<<nb, 128, sm, st>>>(W, tree, state, zseed, x0, z0, nx, nz, step, y, xyz, out, cls, ecx0, ecz0,
+                                              encx);
 }
 /* Block-coordinate biomes: a grid (xyz == nullptr) or n = nx points (nz == 1) at xyz. For the End,
  * `scratch` holds the chunk classes of [ecx0, ecx0+encx) x [ecz0, ecz0+encz). */
