@@ -139,7 +139,10 @@ struct BatchEnd {
 /* the lattices of an Overworld/Nether request, and the shift table of a double-branch Overworld tile */
 struct BatchLat {
     MgLattice lat[MG_MAX_TABLES];
-    ShiftTable<8, BNT / 8> shift;
+    union {
+        ShiftTable<8, BNT / 8> shift;   /* double-branch Overworld tile */
+        ShiftTableF<8, BNT / 8> shiftf; /* float-branch Overworld tile */
+    };
 };
 struct BatchSmem {
     union {
@@ -163,8 +166,8 @@ __device__ __forceinline__ void put_id(uint8_t *p, int v) { __stcs(p, (unsigned 
 template <bool FM, int DIM, int TILE_W>
 __device__ __noinline__ void batch_cells(const MgWorldDesc &W, const MgSpline &S, const MgLattice *T,
                                             const MgTreeNode *tree, const MgBatchReq &R, int tx0, int tz0,
-                                            const ShiftTable<8, BNT / 8> *tab, double g, WarpTreeScratch *wt,
-                                            const PendSink *sink, uint8_t *out) {
+                                            const ShiftTable<8, BNT / 8> *tab, const ShiftTableF<8, BNT / 8> *tabf,
+                                            double g, WarpTreeScratch *wt, const PendSink *sink, uint8_t *out) {
     const int col = threadIdx.x % TILE_W, row = threadIdx.x / TILE_W;
     const int ix = tx0 + col, iz = tz0 + row;
     const bool in = ix < R.nx && iz < R.nz;
@@ -179,6 +182,8 @@ __device__ __noinline__ void batch_cells(const MgWorldDesc &W, const MgSpline &S
         /* a cell whose screen left a value to the exact evaluation is recorded for the second launch (the
          * double branch's tree search is per lane, so the lane may leave here) */
         if (in && !climate_ow_d_tab_defer(W, S, T, *tab, col, row, qx, R.qy, qz, g, tg, sink, o)) return;
+    } else if (FM && DIM == MG_OVERWORLD && TILE_W == 8 && tabf) {
+        if (in) climate_ow_f_tab(W, S, T, *tabf, col, row, qx, R.qy, qz, tg);
     } else if (in) {
         cell_target<FM, DIM>(W, S, T, qx, R.qy, qz, tg);
     }
@@ -291,8 +296,19 @@ __global__ void __launch_bounds__(BNT, MINB) k_batch(const MgWorldDesc *__restri
         const int tx0 = (tile % tw) * TILE_W, tz0 = (tile / tw) * TILE_H;
         const MgTreeNode *tree = trees[R.world];
         if (W.fmode) {
-            if (W.dim == MG_OVERWORLD) batch_cells<true, MG_OVERWORLD, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, 0.0, sm.wt, &sm.sink, out);
-            else batch_cells<true, MG_NETHER, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, 0.0, sm.wt, &sm.sink, out);
+            if (W.dim == MG_OVERWORLD) {
+                /* the tile's shift splits, computed once per column and row (ENGINE rule) */
+                const bool tab = TILE_W == 8 && R.tie != MG_TIE_CHUNK_CELL && shift_table_ok(W);
+                if (tab) {
+                    shift_table_fill_f<8, BNT / 8, BNT>(W.noise[0], sm.o.lat, R.qx0 + tx0, R.qz0 + tz0, sm.o.shiftf);
+                    __syncthreads();
+                }
+                batch_cells<true, MG_OVERWORLD, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr,
+                                                        tab ? &sm.o.shiftf : nullptr, 0.0, sm.wt, &sm.sink, out);
+            } else {
+                batch_cells<true, MG_NETHER, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, nullptr, 0.0, sm.wt,
+                                                     &sm.sink, out);
+            }
         } else if (W.dim == MG_OVERWORLD) {
             /* the tile's shift splits, computed once per column and row (ENGINE rule) */
             const bool tab = TILE_W == 8 && R.tie != MG_TIE_CHUNK_CELL && shift_table_ok(W);
@@ -302,9 +318,10 @@ __global__ void __launch_bounds__(BNT, MINB) k_batch(const MgWorldDesc *__restri
                 __syncthreads();
             }
             batch_cells<false, MG_OVERWORLD, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, tab ? &sm.o.shift : nullptr,
-                                                     tab ? sm.depth_g : 0.0, sm.wt, &sm.sink, out);
+                                                     nullptr, tab ? sm.depth_g : 0.0, sm.wt, &sm.sink, out);
         } else {
-            batch_cells<false, MG_NETHER, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, 0.0, sm.wt, &sm.sink, out);
+            batch_cells<false, MG_NETHER, TILE_W>(W, W.spline, sm.o.lat, tree, R, tx0, tz0, nullptr, nullptr, 0.0, sm.wt,
+                                                  &sm.sink, out);
         }
     }
 }

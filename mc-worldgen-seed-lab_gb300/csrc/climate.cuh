@@ -326,6 +326,85 @@ __device__ __forceinline__ void climate_ow_d_tab(const MgWorldDesc &W, const MgS
     climate_ow_d_rest(W, S, T, X + sp.a * 4.0, Z + sp.b * 4.0, g, tg);
 }
 
+/* The float branch's shift noises of a tile from a table, as the double branch's: the entries are the float
+ * splits (cell, fraction) and the fraction's smoothstep that oct_f computes per cell, on the same inputs (the
+ * same families of X- and Z-side coordinates), so each cell's octaves run on the same values and give the same
+ * bits; the sums keep nn_f's order. */
+struct ShiftSplitF {
+    int32_t i;  /* cell */
+    float f, u; /* fraction, its smoothstep */
+};
+template <int TW, int TH>
+struct ShiftTableF {
+    ShiftSplitF e[2 * SHIFT_MAXLEV][2 * TW + 2 * TH]; /* per lattice: X+ox, X+oy (TW each), Z+oz, Z+ox (TH each) */
+};
+template <int TW, int TH, int NT>
+__device__ __forceinline__ void shift_table_fill_f(const MgNoise &N, const MgLattice *__restrict__ T, int qx0, int qz0,
+                                                   ShiftTableF<TW, TH> &tab) {
+    const int per = 2 * TW + 2 * TH, nl = 2 * N.nlev;
+    const MgLattice *A = T + N.base;
+    for (int e = threadIdx.x; e < nl * per; e += NT) {
+        const int j = e / per, r = e % per;
+        const int fam = r < 2 * TW ? r / TW : 2 + (r - 2 * TW) / TH;
+        const int idx = r < 2 * TW ? r % TW : (r - 2 * TW) % TH;
+        const int st = j >= N.nlev, k = j - st * N.nlev;
+        const MgLattice *L = A + j;
+        double c = fam < 2 ? (double)(qx0 + idx) : (double)(qz0 + idx);
+        if (st) c = c * MG_SECOND_STACK;
+        const double off = fam == 0 ? L->ox : (fam == 1 ? L->oy : (fam == 2 ? L->oz : L->ox));
+        int i;
+        float fr;
+        split_fk(c, N.freq[k], N.fexp[k], off, i, fr);
+        ShiftSplitF &o = tab.e[j][r];
+        o.i = i;
+        o.f = fr;
+        o.u = fade<float>(fr);
+    }
+}
+/* ShiftA and ShiftB of the cell in column col and row row (nn_f's values: level by level, first stack then
+ * second, each sum in its own order), one octave per loop step */
+template <int TW, int TH>
+static __device__ __noinline__ float2 shift_from_table_f(const MgNoise &N, const MgLattice *__restrict__ T,
+                                                         const ShiftTableF<TW, TH> &tab, int col, int row) {
+    float sa = 0.0f, sb = 0.0f;
+    const MgLattice *A = T + N.base;
+#pragma unroll 1
+    for (int e = 0; e < 4 * N.nlev; e++) {
+        const int q = e >> 1, isb = e & 1, k = q >> 1, st = q & 1, j = st * N.nlev + k;
+        const MgLattice *L = A + j;
+        /* ShiftA (x, 0, z): x input X + ox, z input Z + oz, y from the header; ShiftB (z, x, 0): x input Z + ox,
+         * y input X + oy, z from the header */
+        const ShiftSplitF ex = isb ? tab.e[j][2 * TW + TH + row] : tab.e[j][col];
+        const ShiftSplitF eo = isb ? tab.e[j][TW + col] : tab.e[j][2 * TW + row];
+        const int iy = isb ? eo.i : L->iy, iz = isb ? L->iz : eo.i;
+        const float fy = isb ? eo.f : L->z0.f.fy, fz = isb ? L->z0.f.fz : eo.f;
+        const float v = isb ? eo.u : L->z0.f.uy, w = isb ? L->z0.f.uz : eo.u;
+        const float o = octave_q<float>(PlainPerm{L->p}, ex.i, ex.f, iy, fy, fy - 1.0f, v, iz, fz, fz - 1.0f, w);
+        const float t = N.amp_f[k] * o;
+        if (isb) sb += t;
+        else sa += t;
+    }
+    return make_float2(sa, sb);
+}
+/* the float branch's Overworld climate of a tile cell, the shifts from the tile's table (climate_ow<true>'s
+ * values) */
+template <int TW, int TH>
+__device__ __forceinline__ void climate_ow_f_tab(const MgWorldDesc &W, const MgSpline &S, const MgLattice *__restrict__ T,
+                                                 const ShiftTableF<TW, TH> &tab, int col, int row, int qx, int qy, int qz,
+                                                 int32_t tg[6]) {
+    const double X = (double)qx, Z = (double)qz;
+    const float2 sh = shift_from_table_f(W.noise[0], T, tab, col, row);
+    const float sx = sh.x * 4.0f, sz = sh.y * 4.0f;
+    const double x = X + (double)sx, z = Z + (double)sz;
+    const double xc = x * MG_SECOND_STACK, zc = z * MG_SECOND_STACK;
+    const float tv = nn_f_y0(W.noise[1], T, x, z, xc, zc);
+    const float hv = nn_f_y0(W.noise[2], T, x, z, xc, zc);
+    const float cv = nn_f_y0(W.noise[3], T, x, z, xc, zc);
+    const float ev = nn_f_y0(W.noise[4], T, x, z, xc, zc);
+    const float rv = nn_f_y0(W.noise[5], T, x, z, xc, zc);
+    climate_finish_f(W, S, tv, hv, cv, ev, rv, qy * 4, tg);
+}
+
 /* climate_ow_d_tab with the deferral of climate_ow_d_rest_defer */
 template <int TW, int TH>
 __device__ __forceinline__ bool climate_ow_d_tab_defer(const MgWorldDesc &W, const MgSpline &S,
