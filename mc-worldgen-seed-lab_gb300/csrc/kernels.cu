@@ -204,18 +204,24 @@ __global__ void __launch_bounds__(128) k_grid(const __grid_constant__ MgWorldDes
     MgSpline *S = reinterpret_cast<MgSpline *>(smem_raw);
     MgLattice *T = reinterpret_cast<MgLattice *>(S + 1);
     stage(W, state, W.ntables, T, S, DIM == MG_OVERWORLD);
-    /* 8 x 16-cell tiles: a double-branch Overworld tile computes its shift noises' splits once per column and
-     * row (shift_table_fill) */
+    /* 8 x 16-cell tiles: an Overworld tile computes its shift noises' splits once per column and row
+     * (shift_table_fill, shift_table_fill_f) */
     const int tw = (nx + 7) / 8;
     const int col = threadIdx.x % 8, row = threadIdx.x / 8;
     const int tx0 = (int)(blockIdx.x % (unsigned)tw) * 8, tz0 = (int)(blockIdx.x / (unsigned)tw) * 16;
     ShiftTable<8, 16> *tab = nullptr;
+    ShiftTableF<8, 16> *tabf = nullptr;
     __shared__ double depth_g; /* with a table: the depth gradient at qy (depth_grad_d), once per CTA */
-    if (!FM && DIM == MG_OVERWORLD && shift_table_ok(W)) {
-        tab = reinterpret_cast<ShiftTable<8, 16> *>(T + W.ntables);
+    if (DIM == MG_OVERWORLD && shift_table_ok(W)) {
         __syncthreads(); /* the lattices are staged */
-        shift_table_fill<8, 16, 128>(W.noise[0], T, qx0 + tx0, qz0 + tz0, *tab);
-        if (threadIdx.x == 127) depth_g = depth_grad_d(W, qy * 4);
+        if (FM) {
+            tabf = reinterpret_cast<ShiftTableF<8, 16> *>(T + W.ntables);
+            shift_table_fill_f<8, 16, 128>(W.noise[0], T, qx0 + tx0, qz0 + tz0, *tabf);
+        } else {
+            tab = reinterpret_cast<ShiftTable<8, 16> *>(T + W.ntables);
+            shift_table_fill<8, 16, 128>(W.noise[0], T, qx0 + tx0, qz0 + tz0, *tab);
+            if (threadIdx.x == 127) depth_g = depth_grad_d(W, qy * 4);
+        }
     }
     __syncthreads();
     const int ix = tx0 + col, iz = tz0 + row;
@@ -225,7 +231,7 @@ __global__ void __launch_bounds__(128) k_grid(const __grid_constant__ MgWorldDes
         __shared__ WarpTreeScratch wt[4];
         int32_t tg[6] = {0, 0, 0, 0, 0, 0};
         if (in) {
-            if (!FM && tab) climate_ow_d_tab(W, *S, T, *tab, col, row, qx0 + ix, qy, qz0 + iz, depth_g, tg);
+            if (FM && tabf) climate_ow_f_tab(W, *S, T, *tabf, col, row, qx0 + ix, qy, qz0 + iz, tg);
             else cell_target<FM, DIM>(W, *S, T, qx0 + ix, qy, qz0 + iz, tg);
         }
         const int leaf = tree_search_warp(tree, tg, in, wt[threadIdx.x >> 5]);
@@ -235,6 +241,7 @@ __global__ void __launch_bounds__(128) k_grid(const __grid_constant__ MgWorldDes
     if (!in) return;
     int32_t tg[6];
     if (!FM && DIM == MG_OVERWORLD && tab) climate_ow_d_tab(W, *S, T, *tab, col, row, qx0 + ix, qy, qz0 + iz, depth_g, tg);
+    else if (FM && DIM == MG_OVERWORLD && tabf) climate_ow_f_tab(W, *S, T, *tabf, col, row, qx0 + ix, qy, qz0 + iz, tg);
     else cell_target<FM, DIM>(W, *S, T, qx0 + ix, qy, qz0 + iz, tg);
     uint64_t d;
     if (CHAIN) {
@@ -367,9 +374,9 @@ static unsigned end_tiles(int ncx, int ncz) {
     return (unsigned)(((long long)(ncx + END_TC - 1) / END_TC) * ((ncz + END_TC - 1) / END_TC));
 }
 static size_t grid_smem(const MgWorldDesc &W) { return sizeof(MgSpline) + (size_t)W.ntables * sizeof(MgLattice); }
-/* k_grid's: the double-branch Overworld adds its tiles' shift table */
+/* k_grid's: the Overworld adds its tiles' shift table */
 static size_t grid_smem_k(const MgWorldDesc &W) {
-    return grid_smem(W) + (W.dim == MG_OVERWORLD && !W.fmode ? sizeof(ShiftTable<8, 16>) : 0);
+    return grid_smem(W) + (W.dim == MG_OVERWORLD ? (W.fmode ? sizeof(ShiftTableF<8, 16>) : sizeof(ShiftTable<8, 16>)) : 0);
 }
 
 int launch_setup(const MgWorldDesc &W, const int64_t *d_seeds, int ns, MgLattice *d_states, cudaStream_t st) {
