@@ -129,14 +129,15 @@ __global__ void __launch_bounds__(LNT) k_setup_list_end(const MgSetupEntry *__re
 }
 
 /* ---------------------------------------------------------------- the persistent batch kernel */
-/* The lattices of an Overworld/Nether request (with a double-branch Overworld tile's shift table) and the
+/* The lattices of an Overworld/Nether request (with an Overworld tile's shift table) and the
  * End's scratch are never live in the same tile, so they share storage: 21 KB per CTA, which leaves the
  * register budget as the occupancy limit (up to 9 CTAs per SM). */
 struct BatchEnd {
     uint8_t endp[256];
     EndTile tile;
 };
-/* the lattices of an Overworld/Nether request, and the shift table of a double-branch Overworld tile */
+/* the lattices of an Overworld/Nether request, and the shift table of an Overworld tile (double or float
+ * branch) */
 struct BatchLat {
     MgLattice lat[MG_MAX_TABLES];
     union {
@@ -159,8 +160,8 @@ struct BatchSmem {
  * (evict-first) policy, which keeps the streamed output from evicting the threads' local memory from L2 */
 __device__ __forceinline__ void put_id(uint8_t *p, int v) { __stcs(p, (unsigned char)v); }
 
-/* tab: the tile's shift table (double-branch Overworld, ENGINE rule) or null; g: with a table, the tile's
- * depth gradient.  Each code path's cells (and the End's tiles, batch_end) are a function of their own, out of
+/* tab, tabf: the tile's shift table (double- or float-branch Overworld, ENGINE rule) or null; g: with the
+ * double branch's table, the tile's depth gradient.  Each code path's cells (and the End's tiles, batch_end) are a function of their own, out of
  * line: the persistent kernel is then a dispatcher, and each path's registers are allocated for that path
  * alone (measured 0.3 % faster on the mixed batch than all paths inlined into the kernel). */
 template <bool FM, int DIM, int TILE_W>
