@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <map>
+#include <unordered_map>
 #include <mutex>
 #include <vector>
 
@@ -55,6 +56,14 @@ struct McGb300Plan {
 };
 
 namespace {
+
+/* hash of a (world index, seed) key */
+struct SeedKeyHash {
+    size_t operator()(const std::pair<int, int64_t> &k) const {
+        uint64_t x = (uint64_t)k.second * 0x9E3779B97F4A7C15ULL ^ (uint64_t)(uint32_t)k.first * 0xC2B2AE3D27D4EB4FULL;
+        return (size_t)(x ^ (x >> 31));
+    }
+};
 
 int cuda_rc(cudaError_t e) { return e == cudaSuccess ? MCGEN_OK : e == cudaErrorMemoryAllocation ? MCGEN_E_NOMEM : MCGEN_E_INTERNAL; }
 
@@ -161,8 +170,10 @@ MCGEN_API int mcgen_gb300_plan_new(const McGb300Request *reqs, int n, int tie_ru
         free_plan(p);
         return cuda_rc(ee);
     }
-    /* distinct (world, seed) -> pool slots, grouped by dimension */
-    std::map<std::pair<int, int64_t>, int> slot_of;
+    /* distinct (world, seed) -> pool slots, grouped by dimension (a hashed map: an ordered one cost most of a
+     * 10,000-request plan's host time; slots follow the requests' first occurrences either way) */
+    std::unordered_map<std::pair<int, int64_t>, int, SeedKeyHash> slot_of;
+    slot_of.reserve((size_t)n * 2);
     std::vector<int> slot((size_t)n); /* pool slot of each request */
     std::vector<MgSetupEntry> ent[3];
     std::vector<int> first;
@@ -185,6 +196,7 @@ MCGEN_API int mcgen_gb300_plan_new(const McGb300Request *reqs, int n, int tie_ru
     p->ow_lattices = ow;
     /* requests and tiles for every shape; outputs back to back */
     std::vector<MgBatchReq> rq[BATCH_SHAPES];
+    for (auto &v : rq) v.reserve((size_t)n);
     p->out_off.resize((size_t)n);
     p->cells.resize((size_t)n);
     long long off = 0;
